@@ -1,0 +1,246 @@
+/**
+ * @file tt_cuda.h
+ * @brief GB300 (sm_103a) implementation of libtopotoolbox's D8 flow pipeline.
+ *
+ * Drop-in C ABI.  Every `tt_cuda_<name>` below with host pointers has exactly
+ * the parameter list of `<name>` in libtopotoolbox's public header
+ * include/topotoolbox.h (line numbers cited per function), so a caller swaps
+ * `fillsinks(...)` for `tt_cuda_fillsinks(...)` and nothing else changes:
+ *
+ *  - arrays are column-major with `dims = {nrows, ncols}` (fastest dimension
+ *    first, include/topotoolbox.h:284-290);
+ *  - DEMs are float32, boundary-condition and direction grids uint8, flat
+ *    flags int32, node lists and labels ptrdiff_t;
+ *  - the caller owns every buffer; nothing is retained after return.
+ *
+ * Unlike the reference, no call mutates its inputs (the reference's
+ * fillsinks negates `dem` in place while it runs, src/fillsinks.c:14-16).
+ * The reference reports no errors; these functions keep its return types and
+ * record a status per calling thread, read with tt_cuda_last_error().
+ *
+ * Scratch parameters of the reference (`queue`, `heap`, `back`) are accepted
+ * and ignored: the GPU algorithms keep their scratch in a per-device
+ * workspace owned by this library.
+ *
+ * The `_dev` variants take DEVICE pointers and a `cudaStream_t` (passed as
+ * `void *`, NULL = legacy default stream), enqueue their work on that stream
+ * and return a status.  Iterative stages (fill, gwdt) read a small
+ * convergence counter back to the host between device sweeps, so these calls
+ * synchronise the stream before they return.
+ *
+ * Calls are serialised per device by an internal mutex.
+ */
+#ifndef TT_CUDA_H
+#define TT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define TT_CUDA_API __declspec(dllexport)
+#else
+#define TT_CUDA_API __attribute__((visibility("default")))
+#endif
+
+/** Status codes recorded by every call. */
+typedef enum {
+  TT_CUDA_SUCCESS = 0,
+  TT_CUDA_ERR_INVALID_ARGUMENT = 1, /**< bad dims, NULL pointer, bad order */
+  TT_CUDA_ERR_ALLOC = 2,            /**< device or pinned allocation failed */
+  TT_CUDA_ERR_CUDA = 3,             /**< a CUDA runtime call failed */
+  TT_CUDA_ERR_NOT_CONVERGED = 4,    /**< an iteration cap was reached */
+  TT_CUDA_ERR_CYCLE = 5,            /**< the direction grid contains a cycle */
+  TT_CUDA_ERR_NO_DEVICE = 6         /**< no CUDA device is visible */
+} tt_cuda_status;
+
+/* ------------------------------------------------------------------ */
+/* Library state                                                        */
+/* ------------------------------------------------------------------ */
+
+/** 1 when a CUDA device is usable.  Counterpart of has_topotoolbox()
+ *  (include/topotoolbox.h:41, src/topotoolbox.c:4). */
+TT_CUDA_API int tt_cuda_has_gpu(void);
+/** Status of the last tt_cuda_* call made by this thread. */
+TT_CUDA_API tt_cuda_status tt_cuda_last_error(void);
+/** Human-readable text of a status code. */
+TT_CUDA_API const char *tt_cuda_status_string(tt_cuda_status status);
+/** Iteration caps (0 restores the default).  `sweeps` caps the device
+ *  rounds of the iterative stages (fill, gwdt); the environment variable
+ *  TT_CUDA_MAX_ROUNDS sets the same cap at load time. */
+TT_CUDA_API void tt_cuda_set_max_rounds(int64_t rounds);
+/** Release the per-device workspace of the current device. */
+TT_CUDA_API void tt_cuda_release_workspace(void);
+/** Number of kernel launches this library has issued on this thread since
+ *  the last reset (for launch accounting in benchmarks). */
+TT_CUDA_API int64_t tt_cuda_launch_count(int reset);
+/** Device rounds used by the last fill / gwdt call on this thread. */
+TT_CUDA_API int64_t tt_cuda_last_rounds(void);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in host-pointer entry points                                    */
+/* ------------------------------------------------------------------ */
+
+/** include/topotoolbox.h:293 fillsinks (src/fillsinks.c:23-48). */
+TT_CUDA_API void tt_cuda_fillsinks(float *output, float *dem, uint8_t *bc,
+                                   ptrdiff_t dims[2]);
+/** include/topotoolbox.h:351 fillsinks_hybrid (src/fillsinks.c:51-77).
+ *  `queue` is not used. */
+TT_CUDA_API void tt_cuda_fillsinks_hybrid(float *output, ptrdiff_t *queue,
+                                          float *dem, uint8_t *bc,
+                                          ptrdiff_t dims[2]);
+/** include/topotoolbox.h:1056 reconstruct (src/reconstruct.c:270-278):
+ *  grayscale reconstruction by dilation of `marker` under `mask`, in place. */
+TT_CUDA_API void tt_cuda_reconstruct(float *marker, float *mask,
+                                     ptrdiff_t dims[2]);
+/** include/topotoolbox.h:1070 reconstruct_hybrid (src/reconstruct.c:291-312).
+ *  Returns 0 on convergence, 1 if the round cap was hit. */
+TT_CUDA_API int tt_cuda_reconstruct_hybrid(float *marker, ptrdiff_t *queue,
+                                           float *mask, ptrdiff_t dims[2]);
+/** include/topotoolbox.h:405 identifyflats (src/identifyflats.c:33-121).
+ *  Returns the number of flat pixels. */
+TT_CUDA_API ptrdiff_t tt_cuda_identifyflats(int32_t *output, float *dem,
+                                            ptrdiff_t dims[2]);
+/** include/topotoolbox.h:464 gwdt_computecosts (src/gwdt.c:167-278).
+ *  `costs` are bit-identical to the reference.  `conncomps` holds, for every
+ *  flat, the linear index of a pixel of maximal depth in its component (the
+ *  smallest such index; the reference's choice among equal depths follows
+ *  its scan order), 0 elsewhere. */
+TT_CUDA_API void tt_cuda_gwdt_computecosts(float *costs, ptrdiff_t *conncomps,
+                                           int32_t *flats, float *original_dem,
+                                           float *filled_dem,
+                                           ptrdiff_t dims[2]);
+/** include/topotoolbox.h:533 gwdt (src/gwdt.c:290-351).  `dist` is
+ *  bit-identical to the reference; `prev` (may be NULL) holds a valid
+ *  back-link for every reached flat (dist[v] == dist[prev[v]] + edge
+ *  weight), self elsewhere.  `heap` and `back` are not used. */
+TT_CUDA_API void tt_cuda_gwdt(float *dist, ptrdiff_t *prev, float *costs,
+                              int32_t *flats, ptrdiff_t *heap, ptrdiff_t *back,
+                              ptrdiff_t dims[2]);
+/** include/topotoolbox.h:860 flow_routing_d8_carve
+ *  (src/flow_routing.c:135-256).  `direction` is bit-identical; `node` is a
+ *  topological order (every donor before its receiver). */
+TT_CUDA_API void tt_cuda_flow_routing_d8_carve(ptrdiff_t *node,
+                                               uint8_t *direction, float *dem,
+                                               float *dist, int32_t *flats,
+                                               ptrdiff_t dims[2],
+                                               unsigned int order);
+/** include/topotoolbox.h:962 flow_accumulation
+ *  (src/flow_accumulation.c:32-80).  The sum is exact in 64-bit fixed point
+ *  and rounded once to float32, so it does not depend on the order in
+ *  `source`; `source` is accepted and not read. */
+TT_CUDA_API void tt_cuda_flow_accumulation(float *acc, ptrdiff_t *source,
+                                           uint8_t *direction, float *weights,
+                                           ptrdiff_t dims[2]);
+/** include/topotoolbox.h:2347 gradient_secondorder (src/hillshade.c:23-76). */
+TT_CUDA_API void tt_cuda_gradient_secondorder(float *p0, float *p1, float *dem,
+                                              float cellsize,
+                                              ptrdiff_t dims[2]);
+/** include/topotoolbox.h:2400 hillshade (src/hillshade.c:79-97). */
+TT_CUDA_API void tt_cuda_hillshade(float *output, float *dx, float *dy,
+                                   float *dem, float azimuth, float altitude,
+                                   float cellsize, ptrdiff_t dims[2]);
+/** include/topotoolbox.h:2449 hillshade_fused (src/hillshade.c:102-213). */
+TT_CUDA_API void tt_cuda_hillshade_fused(float *output, float *dem,
+                                         float azimuth, float altitude,
+                                         float cellsize, ptrdiff_t dims[2]);
+
+/* ------------------------------------------------------------------ */
+/* Adjoints (no counterpart in the reference)                           */
+/* ------------------------------------------------------------------ */
+
+/** Adjoint of weighted flow_accumulation with the receivers held fixed:
+ *  grad_weights[u] = sum of grad_acc over the flow path from u to its
+ *  outlet, u included.  `source` is accepted and not read. */
+TT_CUDA_API void tt_cuda_flow_accumulation_backward(float *grad_weights,
+                                                    ptrdiff_t *source,
+                                                    uint8_t *direction,
+                                                    float *grad_acc,
+                                                    ptrdiff_t dims[2]);
+/** Adjoint of hillshade_fused with respect to the DEM:
+ *  grad_dem = J^T grad_output.  Cells whose hillshade is NaN contribute
+ *  nothing. */
+TT_CUDA_API void tt_cuda_hillshade_backward(float *grad_dem, float *dem,
+                                            float *grad_output, float azimuth,
+                                            float altitude, float cellsize,
+                                            ptrdiff_t dims[2]);
+
+/* ------------------------------------------------------------------ */
+/* Whole pipeline (composition of the calls above, no single reference  */
+/* counterpart).  Host pointers.  Any output may be NULL to skip it.    */
+/* ------------------------------------------------------------------ */
+
+/** fillsinks -> identifyflats -> gwdt_computecosts -> gwdt ->
+ *  flow_routing_d8_carve (order 0) -> flow_accumulation (the call sequence of
+ *  test/random_dem.cpp:682-724).  `dem` follows the caller's NaN convention:
+ *  NaN cells stay NaN (barriers); callers that want the reference test
+ *  harness's behaviour pass -INF with bc = 1 there.  `weights` may be NULL
+ *  (unit weights). */
+TT_CUDA_API void tt_cuda_d8_pipeline(float *filled, int32_t *flats,
+                                     float *dist, ptrdiff_t *node,
+                                     uint8_t *direction, float *acc,
+                                     float *dem, uint8_t *bc, float *weights,
+                                     ptrdiff_t dims[2]);
+
+/* ------------------------------------------------------------------ */
+/* Device-pointer entry points                                          */
+/* ------------------------------------------------------------------ */
+
+TT_CUDA_API tt_cuda_status tt_cuda_fillsinks_dev(float *output,
+                                                 const float *dem,
+                                                 const uint8_t *bc,
+                                                 const ptrdiff_t dims[2],
+                                                 void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_reconstruct_dev(float *marker,
+                                                   const float *mask,
+                                                   const ptrdiff_t dims[2],
+                                                   void *stream);
+/** `count` (may be NULL) receives the number of flats (device int64). */
+TT_CUDA_API tt_cuda_status tt_cuda_identifyflats_dev(int32_t *output,
+                                                     const float *dem,
+                                                     const ptrdiff_t dims[2],
+                                                     int64_t *count_dev,
+                                                     void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_gwdt_computecosts_dev(
+    float *costs, ptrdiff_t *conncomps, const int32_t *flats,
+    const float *original_dem, const float *filled_dem,
+    const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_gwdt_dev(float *dist, ptrdiff_t *prev,
+                                            const float *costs,
+                                            const int32_t *flats,
+                                            const ptrdiff_t dims[2],
+                                            void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_flow_routing_d8_carve_dev(
+    ptrdiff_t *node, uint8_t *direction, const float *dem, const float *dist,
+    const int32_t *flats, const ptrdiff_t dims[2], unsigned int order,
+    void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_flow_accumulation_dev(
+    float *acc, const uint8_t *direction, const float *weights,
+    const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_flow_accumulation_backward_dev(
+    float *grad_weights, const uint8_t *direction, const float *grad_acc,
+    const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_gradient_secondorder_dev(
+    float *p0, float *p1, const float *dem, float cellsize,
+    const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_hillshade_fused_dev(
+    float *output, const float *dem, float azimuth, float altitude,
+    float cellsize, const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_hillshade_backward_dev(
+    float *grad_dem, const float *dem, const float *grad_output, float azimuth,
+    float altitude, float cellsize, const ptrdiff_t dims[2], void *stream);
+/** Device form of tt_cuda_d8_pipeline.  `hillshade` (may be NULL) adds the
+ *  hillshade of the input DEM with the given angles. */
+TT_CUDA_API tt_cuda_status tt_cuda_d8_pipeline_dev(
+    float *filled, int32_t *flats, float *dist, ptrdiff_t *node,
+    uint8_t *direction, float *acc, float *hillshade, const float *dem,
+    const uint8_t *bc, const float *weights, float azimuth, float altitude,
+    float cellsize, const ptrdiff_t dims[2], void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TT_CUDA_H */

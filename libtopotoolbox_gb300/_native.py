@@ -1,0 +1,108 @@
+"""ctypes binding of the native library ``libtt_cuda.so`` (include/tt_cuda.h).
+
+The library is loaded from this package directory.  There is no fallback:
+if it is missing or cannot be loaded, ``lib()`` raises, so every compute
+entry point of this package fails loudly instead of running elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libtt_cuda.so"
+
+P = C.c_void_p
+F = C.c_float
+I64 = C.c_int64
+PD = C.POINTER(C.c_int64)  # ptrdiff_t dims[2]
+U = C.c_uint
+ST = C.c_int  # tt_cuda_status
+
+# name -> (restype, argtypes), mirroring include/tt_cuda.h
+SIGNATURES = {
+    "tt_cuda_has_gpu": (C.c_int, []),
+    "tt_cuda_last_error": (ST, []),
+    "tt_cuda_status_string": (C.c_char_p, [ST]),
+    "tt_cuda_set_max_rounds": (None, [I64]),
+    "tt_cuda_release_workspace": (None, []),
+    "tt_cuda_launch_count": (I64, [C.c_int]),
+    "tt_cuda_last_rounds": (I64, []),
+    # drop-in host-pointer forms
+    "tt_cuda_fillsinks": (None, [P, P, P, PD]),
+    "tt_cuda_fillsinks_hybrid": (None, [P, P, P, P, PD]),
+    "tt_cuda_reconstruct": (None, [P, P, PD]),
+    "tt_cuda_reconstruct_hybrid": (C.c_int, [P, P, P, PD]),
+    "tt_cuda_identifyflats": (C.c_int64, [P, P, PD]),
+    "tt_cuda_gwdt_computecosts": (None, [P, P, P, P, P, PD]),
+    "tt_cuda_gwdt": (None, [P, P, P, P, P, P, PD]),
+    "tt_cuda_flow_routing_d8_carve": (None, [P, P, P, P, P, PD, U]),
+    "tt_cuda_flow_accumulation": (None, [P, P, P, P, PD]),
+    "tt_cuda_gradient_secondorder": (None, [P, P, P, F, PD]),
+    "tt_cuda_hillshade": (None, [P, P, P, P, F, F, F, PD]),
+    "tt_cuda_hillshade_fused": (None, [P, P, F, F, F, PD]),
+    "tt_cuda_flow_accumulation_backward": (None, [P, P, P, P, PD]),
+    "tt_cuda_hillshade_backward": (None, [P, P, P, F, F, F, PD]),
+    "tt_cuda_d8_pipeline": (None, [P, P, P, P, P, P, P, P, P, PD]),
+    # device-pointer forms
+    "tt_cuda_fillsinks_dev": (ST, [P, P, P, PD, P]),
+    "tt_cuda_reconstruct_dev": (ST, [P, P, PD, P]),
+    "tt_cuda_identifyflats_dev": (ST, [P, P, PD, P, P]),
+    "tt_cuda_gwdt_computecosts_dev": (ST, [P, P, P, P, P, PD, P]),
+    "tt_cuda_gwdt_dev": (ST, [P, P, P, P, PD, P]),
+    "tt_cuda_flow_routing_d8_carve_dev": (ST, [P, P, P, P, P, PD, U, P]),
+    "tt_cuda_flow_accumulation_dev": (ST, [P, P, P, PD, P]),
+    "tt_cuda_flow_accumulation_backward_dev": (ST, [P, P, P, PD, P]),
+    "tt_cuda_gradient_secondorder_dev": (ST, [P, P, P, F, PD, P]),
+    "tt_cuda_hillshade_fused_dev": (ST, [P, P, F, F, F, PD, P]),
+    "tt_cuda_hillshade_backward_dev": (ST, [P, P, P, F, F, F, PD, P]),
+    "tt_cuda_d8_pipeline_dev": (ST, [P, P, P, P, P, P, P, P, P, P, F, F, F, PD, P]),
+}
+
+STATUS = {
+    0: "success",
+    1: "invalid argument",
+    2: "allocation failed",
+    3: "CUDA runtime error",
+    4: "iteration cap reached",
+    5: "direction grid contains a cycle",
+    6: "no CUDA device",
+}
+
+_LIB = None
+
+
+class TTCudaError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)} (status {status})")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """Load libtt_cuda.so (once).  Raises if it is absent: no CPU fallback."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"{LIB_PATH} is missing; build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        h = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = h
+    return _LIB
+
+
+def dims_arg(dims):
+    arr = (C.c_int64 * 2)(int(dims[0]), int(dims[1]))
+    return C.cast(arr, PD), arr  # keep `arr` alive alongside the pointer
+
+
+def check(status: int, where: str) -> None:
+    if status != 0:
+        raise TTCudaError(status, where)
+
+
+def last_status() -> int:
+    return int(lib().tt_cuda_last_error())

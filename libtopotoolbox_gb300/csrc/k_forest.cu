@@ -1,0 +1,866 @@
+// Receiver-forest kernels: flow accumulation (src/flow_accumulation.c:32-80),
+// a topological node order for flow_routing_d8_carve
+// (src/flow_routing.c:135-256), and the adjoint of weighted accumulation.
+//
+// The D8 directions define a forest (every pixel has at most one receiver).
+// The reference walks it sequentially (a DFS for the order, then one pass in
+// that order for the sums).  Here the forest is contracted in two levels:
+//
+//  1. Tile level (one warp per 32 x 32 tile, shared memory).  Pixels whose
+//     receiver lies outside their tile are the tile's exits E.  Inside a tile
+//     sums are taken with a "last arriver continues" walk: every in-tile leaf
+//     starts a lane that adds its value into its receiver and decrements the
+//     receiver's count of pending in-tile donors; the lane that brings the
+//     count to zero owns the now-complete receiver and continues downstream.
+//     For each entry pixel (one with a donor in another tile) the walk also
+//     records the exit its in-tile path reaches and the number of steps.
+//  2. Coarse level (global memory).  The exits form a smaller forest
+//     e -> exit reached from receiver(e); the same last-arriver walk runs on
+//     it with global atomics.  A final tile pass injects each entry pixel's
+//     inflow and repeats the in-tile walk to produce every pixel's total.
+//
+// Sums are exact: weights are converted to 64-bit fixed point with a
+// power-of-two scale chosen from max|w| * N so no partial sum can overflow,
+// and integer addition is associative, so the result is independent of the
+// order of the walk and identical from run to run (no float atomics).  Unit
+// weights use scale 1 (exact pixel counts).  Each total is rounded once to
+// float32.
+//
+// The node order sorts pixels by the length of their longest upstream path
+// h (0 at sources): a receiver's h exceeds each donor's, so ascending h is a
+// topological order.  h is computed by the same two-level walk with max
+// instead of sum, then a counting sort places pixels by h.  Pixels with equal
+// h have no mutual constraint; their relative order follows atomic slot
+// reservation and may vary between runs.
+//
+// The adjoint grad_w(u) = sum of grad_acc over the path from u to its outlet
+// is a root-ward path sum: pointer jumping inside each tile (10 synchronous
+// rounds in shared memory) and over the exits, in float-float (two-float)
+// arithmetic.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "tt_internal.cuh"
+
+namespace tt {
+namespace {
+
+constexpr int kTileCells = kTile * kTile;
+constexpr int kUpWarps = 2;
+
+enum : int {
+  RL_NONE = -4,    // outside the grid (partial tile)
+  RL_BADDIR = -3,  // direction points off the grid: treated as an outlet
+  RL_EXIT = -2,    // receiver lies in another tile
+  RL_ROOT = -1     // outlet or sink (direction 0)
+};
+
+enum : int { ERR_CYCLE = 1, ERR_BADDIR = 2, ERR_WEIGHT = 4 };
+
+struct UpArgs {
+  const uint8_t *dir;
+  int64_t m, n;
+  int tm, tn;
+  unsigned order;
+  const float *w;  // nullptr: unit weights
+  int wshift;      // fixed-point scale 2^wshift
+  int phase;       // 1: local pass, 3: final pass
+  bool want_acc;
+  bool want_h;
+  long long *cacc;  // per exit: local (then total) fixed-point sum
+  int *cH;          // per exit: longest upstream path
+  int *cpend;       // per exit: pending coarse donors
+  int *xmap;        // per entry pixel: exit reached in-tile, or -1
+  int *xsteps;      // per entry pixel: steps to that exit
+  int *elist;       // list of exits
+  int *ecount;
+  float *acc_out;
+  int *h_out;
+  int *hmax;
+  int *err;
+};
+
+struct UpTile {
+  uint8_t dir[kHalo][36];  // [c][r], one-pixel halo
+  int16_t rl[kTileCells];  // local receiver or an RL_* code
+  uint8_t ent[kTileCells]; // external donors
+  int pend[kTileCells];
+  long long acc[kTileCells];
+  int h[kTileCells];
+  int16_t list[kTileCells];
+  int nlist;
+};
+
+__device__ __forceinline__ long long to_fixed(float w, int k, int *err) {
+  unsigned bits = __float_as_uint(w);
+  int e = (bits >> 23) & 0xff;
+  unsigned mant = bits & 0x7fffffu;
+  if (e == 255) {
+    atomicOr(err, ERR_WEIGHT);
+    return 0;
+  }
+  if (e == 0)
+    e = 1;
+  else
+    mant |= 0x800000u;
+  int sh = e - 150 + k;  // value = mant * 2^(e-150)
+  long long v;
+  if (sh >= 0)
+    v = sh < 39 ? ((long long)mant << sh) : 0;
+  else if (sh > -40)
+    v = ((long long)mant + (1LL << (-sh - 1))) >> (-sh);
+  else
+    v = 0;
+  return (bits >> 31) ? -v : v;
+}
+
+__device__ __forceinline__ void load_dir_tile(uint8_t (*dir)[36],
+                                              const uint8_t *__restrict__ g,
+                                              int64_t m, int64_t n, int64_t i0,
+                                              int64_t j0, int lane) {
+  for (int c = 0; c < kHalo; c++) {
+    int64_t j = j0 - 1 + c;
+    for (int r = lane; r < kHalo; r += 32) {
+      int64_t i = i0 - 1 + r;
+      uint8_t v = 0;
+      if (i >= 0 && i < m && j >= 0 && j < n) v = g[j * m + i];
+      dir[c][r] = v;
+    }
+  }
+}
+
+// Receiver code of tile pixel (ii, jj).
+__device__ __forceinline__ int local_receiver(const uint8_t (*dir)[36], int ii,
+                                              int jj, int64_t i, int64_t j,
+                                              int64_t m, int64_t n,
+                                              unsigned order) {
+  if (i >= m || j >= n) return RL_NONE;
+  unsigned d = dir[jj + 1][ii + 1];
+  if (d == 0) return RL_ROOT;
+  int k = d8_bit(d);
+  int di = d8_di(k, order), dj = d8_dj(k, order);
+  int64_t gi = i + di, gj = j + dj;
+  if (gi < 0 || gi >= m || gj < 0 || gj >= n) return RL_BADDIR;
+  int ti = ii + di, tj = jj + dj;
+  if (ti >= 0 && ti < kTile && tj >= 0 && tj < kTile) return tj * kTile + ti;
+  return RL_EXIT;
+}
+
+__global__ void __launch_bounds__(kUpWarps * 32) forest_up_kernel(UpArgs a) {
+  __shared__ UpTile tiles[kUpWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  UpTile &t = tiles[warp];
+  const int T = a.tm * a.tn;
+  for (int tile = blockIdx.x * kUpWarps + warp; tile < T;
+       tile += gridDim.x * kUpWarps) {
+    const int ti = tile % a.tm, tj = tile / a.tm;
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    load_dir_tile(t.dir, a.dir, a.m, a.n, i0, j0, lane);
+    if (lane == 0) t.nlist = 0;
+    __syncwarp();
+
+    // Receivers, donor counts, initial values.
+    int nvalid = 0, bad = 0;
+    const int ii = lane;
+    const int64_t i = i0 + ii;
+    for (int jj = 0; jj < kTile; jj++) {
+      const int64_t j = j0 + jj;
+      const int loc = jj * kTile + ii;
+      int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
+      t.rl[loc] = (int16_t)rl;
+      if (rl == RL_BADDIR) bad = 1;
+      int np = 0, ne = 0;
+      long long inflow = 0;
+      int hin = 0;
+      if (rl != RL_NONE) {
+        nvalid++;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
+          int qr = ii + 1 - di, qc = jj + 1 - dj;  // halo coordinates of q
+          unsigned dq = t.dir[qc][qr];
+          if (dq == 0 || d8_bit(dq) != k) continue;
+          if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) {
+            np++;
+          } else {
+            ne++;
+            if (a.phase == 3) {
+              int64_t gq = (j - dj) * a.m + (i - di);
+              if (a.want_acc) inflow += a.cacc[gq];
+              if (a.want_h) hin = max(hin, a.cH[gq] + 1);
+            }
+          }
+        }
+      }
+      t.pend[loc] = np;
+      t.ent[loc] = (uint8_t)ne;
+      long long w0 = 0;
+      if (a.want_acc && rl != RL_NONE)
+        w0 = a.w ? to_fixed(a.w[j * a.m + i], a.wshift, a.err) : 1LL;
+      t.acc[loc] = w0 + inflow;
+      t.h[loc] = hin;
+      if (rl != RL_NONE && np == 0) {
+        int s = atomicAdd(&t.nlist, 1);
+        t.list[s] = (int16_t)loc;
+      }
+    }
+    __syncwarp();
+    if (bad && lane == 0) atomicOr(a.err, ERR_BADDIR);
+    __syncwarp();
+
+    // Last-arriver walks.
+    const int nl = *(volatile int *)&t.nlist;
+    int done = 0;
+    volatile long long *vacc = t.acc;
+    volatile int *vh = t.h;
+    for (int idx = lane; idx < nl; idx += 32) {
+      int p = t.list[idx];
+      for (int guard = 0; guard < kTileCells; guard++) {
+        long long v = vacc[p];
+        int hv = vh[p];
+        done++;
+        int q = t.rl[p];
+        if (q < 0) {
+          if (q == RL_EXIT && a.phase == 1) {
+            int64_t gp = (j0 + p / kTile) * a.m + (i0 + p % kTile);
+            if (a.want_acc) a.cacc[gp] = v;
+            if (a.want_h) a.cH[gp] = hv;
+            a.cpend[gp] = 0;
+            a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
+          }
+          break;
+        }
+        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
+        if (a.want_h) atomicMax(&t.h[q], hv + 1);
+        __threadfence_block();
+        if (atomicSub(&t.pend[q], 1) != 1) break;
+        __threadfence_block();
+        p = q;
+      }
+    }
+    __syncwarp();
+    for (int o = 16; o > 0; o >>= 1) {
+      done += __shfl_down_sync(0xffffffffu, done, o);
+      nvalid += __shfl_down_sync(0xffffffffu, nvalid, o);
+    }
+    if (lane == 0 && done != nvalid) atomicOr(a.err, ERR_CYCLE);
+    __syncwarp();
+
+    if (a.phase == 1) {
+      // Entry pixels: exit reached in-tile and the number of steps.
+      for (int jj = 0; jj < kTile; jj++) {
+        const int loc = jj * kTile + ii;
+        if (!t.ent[loc]) continue;
+        int p = loc, steps = 0;
+        while (t.rl[p] >= 0 && steps < kTileCells) {
+          p = t.rl[p];
+          steps++;
+        }
+        int64_t gr = (j0 + jj) * a.m + i;
+        int x = -1;
+        if (t.rl[p] == RL_EXIT) x = (int)((j0 + p / kTile) * a.m + (i0 + p % kTile));
+        a.xmap[gr] = x;
+        a.xsteps[gr] = steps;
+      }
+    } else {
+      int hm = 0;
+      for (int jj = 0; jj < kTile; jj++) {
+        const int64_t j = j0 + jj;
+        if (i >= a.m || j >= a.n) continue;
+        const int loc = jj * kTile + ii;
+        int64_t gp = j * a.m + i;
+        if (a.want_acc) {
+          float v = __ll2float_rn(t.acc[loc]);
+          a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
+        }
+        if (a.want_h) {
+          int hv = t.h[loc];
+          a.h_out[gp] = hv;
+          hm = max(hm, hv);
+        }
+      }
+      if (a.want_h) {
+        for (int o = 16; o > 0; o >>= 1) hm = max(hm, __shfl_down_sync(0xffffffffu, hm, o));
+        if (lane == 0) atomicMax(a.hmax, hm);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ int64_t receiver_of(const uint8_t *dir, int64_t p,
+                                               int64_t m, unsigned order) {
+  unsigned d = dir[p];
+  int k = d8_bit(d);
+  int64_t i = p % m, j = p / m;
+  return (j + d8_dj(k, order)) * m + (i + d8_di(k, order));
+}
+
+// Coarse links: cnext(e) = exit reached from receiver(e), hop = 1 + steps.
+__global__ void coarse_link_kernel(const int *__restrict__ elist,
+                                   const int *__restrict__ ecount,
+                                   const uint8_t *__restrict__ dir, int64_t m,
+                                   unsigned order, const int *__restrict__ xmap,
+                                   const int *__restrict__ xsteps,
+                                   int *__restrict__ cnext, int *__restrict__ chop,
+                                   int *__restrict__ cpend) {
+  const int E = *ecount;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
+    int e = elist[a];
+    int64_t r = receiver_of(dir, e, m, order);
+    int nx = xmap[r];
+    cnext[e] = nx;
+    chop[e] = 1 + xsteps[r];
+    if (nx >= 0) atomicAdd(&cpend[nx], 1);
+  }
+}
+
+__global__ void coarse_leaves_kernel(const int *__restrict__ elist,
+                                     const int *__restrict__ ecount,
+                                     const int *__restrict__ cpend,
+                                     int *__restrict__ leaves,
+                                     int *__restrict__ lcount) {
+  const int E = *ecount;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
+    int e = elist[a];
+    if (cpend[e] == 0) leaves[atomicAdd(lcount, 1)] = e;
+  }
+}
+
+__global__ void coarse_walk_kernel(const int *__restrict__ leaves,
+                                   const int *__restrict__ lcount,
+                                   const int *__restrict__ cnext,
+                                   const int *__restrict__ chop,
+                                   long long *cacc, int *cH, int *cpend,
+                                   bool want_acc, bool want_h, int *processed,
+                                   int limit) {
+  const int L = *lcount;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < L; a += gridDim.x * blockDim.x) {
+    int e = leaves[a];
+    int n_done = 0;
+    for (int guard = 0; guard < limit; guard++) {
+      n_done++;
+      int nx = cnext[e];
+      if (nx < 0) break;
+      if (want_acc) {
+        long long v = atomicAdd((unsigned long long *)&cacc[e], 0ULL);
+        atomicAdd((unsigned long long *)&cacc[nx], (unsigned long long)v);
+      }
+      if (want_h) {
+        int hv = atomicAdd(&cH[e], 0);
+        atomicMax(&cH[nx], hv + chop[e]);
+      }
+      __threadfence();
+      if (atomicSub(&cpend[nx], 1) != 1) break;
+      __threadfence();
+      e = nx;
+    }
+    atomicAdd(processed, n_done);
+  }
+}
+
+// ------------------------------------------------------------------
+// Node order: histogram of h, exclusive scan, scatter.
+// ------------------------------------------------------------------
+constexpr int kSmallBins = 256;
+
+__global__ void h_hist_kernel(const int *__restrict__ h, int64_t N,
+                              int *__restrict__ hist) {
+  __shared__ int sb[kSmallBins];
+  for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x) sb[b] = 0;
+  __syncthreads();
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int v = h[p];
+    if (v < kSmallBins) {
+      atomicAdd(&sb[v], 1);
+    } else {
+      unsigned grp = __match_any_sync(__activemask(), v);
+      int leader = __ffs(grp) - 1;
+      if ((int)(threadIdx.x & 31) == leader) atomicAdd(&hist[v], __popc(grp));
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x)
+    if (sb[b]) atomicAdd(&hist[b], sb[b]);
+}
+
+// Exclusive scan of n ints by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) scan_kernel(const int *__restrict__ in,
+                                                    int *__restrict__ out, int n) {
+  __shared__ int part[1024];
+  const int tid = threadIdx.x;
+  const int chunk = (n + 1023) / 1024;
+  const int b0 = tid * chunk, b1 = min(n, b0 + chunk);
+  int s = 0;
+  for (int k = b0; k < b1; k++) s += in[k];
+  part[tid] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int run = tid > 0 ? part[tid - 1] : 0;
+  for (int k = b0; k < b1; k++) {
+    int v = in[k];
+    out[k] = run;
+    run += v;
+  }
+}
+
+__global__ void node_scatter_kernel(const int *__restrict__ h, int64_t N,
+                                    const int *__restrict__ off,
+                                    int *__restrict__ cursor,
+                                    ptrdiff_t *__restrict__ node) {
+  __shared__ int cnt[kSmallBins];
+  __shared__ int base[kSmallBins];
+  // One pass per block-sized chunk so that small bins are reserved once per
+  // block: count, reserve, then place.
+  for (int64_t start = (int64_t)blockIdx.x * blockDim.x; start < N;
+       start += (int64_t)gridDim.x * blockDim.x) {
+    for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x) cnt[b] = 0;
+    __syncthreads();
+    int64_t p = start + threadIdx.x;
+    int v = p < N ? h[p] : -1;
+    int rank = 0;
+    if (v >= 0 && v < kSmallBins) rank = atomicAdd(&cnt[v], 1);
+    __syncthreads();
+    for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x)
+      base[b] = cnt[b] ? atomicAdd(&cursor[b], cnt[b]) : 0;
+    __syncthreads();
+    if (v >= 0) {
+      int slot;
+      if (v < kSmallBins) {
+        slot = base[v] + rank;
+      } else {
+        unsigned grp = __match_any_sync(__activemask(), v);
+        int leader = __ffs(grp) - 1;
+        int lane = threadIdx.x & 31;
+        int b0 = 0;
+        if (lane == leader) b0 = atomicAdd(&cursor[v], __popc(grp));
+        b0 = __shfl_sync(grp, b0, leader);
+        slot = b0 + __popc(grp & ((1u << lane) - 1));
+      }
+      node[off[v] + slot] = (ptrdiff_t)p;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------
+// Adjoint: root-ward path sums in float-float.
+// ------------------------------------------------------------------
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s = __fadd_rn(a.hi, b.hi);
+  float bb = __fsub_rn(s, a.hi);
+  float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  float lo = __fadd_rn(__fadd_rn(err, a.lo), b.lo);
+  float hi = __fadd_rn(s, lo);
+  lo = __fsub_rn(lo, __fsub_rn(hi, s));
+  return {hi, lo};
+}
+
+struct DownArgs {
+  const uint8_t *dir;
+  const float *g;  // grad_acc
+  int64_t m, n;
+  int tm, tn;
+  unsigned order;
+  int phase;     // 1: coarse inputs, 3: output
+  float *clhi;   // per entry pixel: path sum to its in-tile end
+  float *cllo;
+  int *cx;       // per entry pixel: exit reached, or -1
+  int *eidx;     // per exit: its index in elist
+  int *elist;
+  int *ecount;
+  const float *Dhi;  // per exit index: sum from its receiver to the outlet
+  const float *Dlo;
+  float *out;
+  int *err;
+};
+
+struct DownTile {
+  uint8_t dir[kHalo][36];
+  int16_t rl[kTileCells];
+  float hi[2][kTileCells];
+  float lo[2][kTileCells];
+  int16_t nx[2][kTileCells];
+  int16_t last[2][kTileCells];
+};
+
+__global__ void __launch_bounds__(32) forest_down_kernel(DownArgs a) {
+  __shared__ DownTile t;
+  const int lane = threadIdx.x;
+  const int T = a.tm * a.tn;
+  for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
+    const int ti = tile % a.tm, tj = tile / a.tm;
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    load_dir_tile(t.dir, a.dir, a.m, a.n, i0, j0, lane);
+    __syncwarp();
+    const int ii = lane;
+    const int64_t i = i0 + ii;
+    int bad = 0;
+    for (int jj = 0; jj < kTile; jj++) {
+      const int64_t j = j0 + jj;
+      const int loc = jj * kTile + ii;
+      int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
+      if (rl == RL_BADDIR) bad = 1;
+      t.rl[loc] = (int16_t)rl;
+      t.hi[0][loc] = (rl != RL_NONE) ? a.g[j * a.m + i] : 0.0f;
+      t.lo[0][loc] = 0.0f;
+      t.nx[0][loc] = (int16_t)(rl >= 0 ? rl : -1);
+      t.last[0][loc] = (int16_t)loc;
+    }
+    if (bad) atomicOr(a.err, ERR_BADDIR);
+    __syncwarp();
+    int cur = 0;
+    for (int round = 0; round < 10; round++) {
+      for (int jj = 0; jj < kTile; jj++) {
+        const int loc = jj * kTile + ii;
+        int q = t.nx[cur][loc];
+        FF v{t.hi[cur][loc], t.lo[cur][loc]};
+        int nq = -1, lq = t.last[cur][loc];
+        if (q >= 0) {
+          v = ff_add(v, FF{t.hi[cur][q], t.lo[cur][q]});
+          nq = t.nx[cur][q];
+          lq = t.last[cur][q];
+        }
+        t.hi[cur ^ 1][loc] = v.hi;
+        t.lo[cur ^ 1][loc] = v.lo;
+        t.nx[cur ^ 1][loc] = (int16_t)nq;
+        t.last[cur ^ 1][loc] = (int16_t)lq;
+      }
+      cur ^= 1;
+      __syncwarp();
+    }
+    for (int jj = 0; jj < kTile; jj++) {
+      const int64_t j = j0 + jj;
+      if (i >= a.m || j >= a.n) continue;
+      const int loc = jj * kTile + ii;
+      const int64_t gp = j * a.m + i;
+      int e = t.last[cur][loc];
+      int64_t ge = -1;
+      if (t.rl[e] == RL_EXIT) ge = (j0 + e / kTile) * a.m + (i0 + e % kTile);
+      if (a.phase == 1) {
+        if (t.rl[loc] == RL_EXIT) {
+          int slot = atomicAdd(a.ecount, 1);
+          a.eidx[gp] = slot;
+          a.elist[slot] = (int)gp;
+        }
+        // Entry pixel: some neighbour in another tile drains here.
+        bool entry = false;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
+          int qr = ii + 1 - di, qc = jj + 1 - dj;
+          unsigned dq = t.dir[qc][qr];
+          if (dq && d8_bit(dq) == k && !(qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile))
+            entry = true;
+        }
+        if (entry) {
+          a.clhi[gp] = t.hi[cur][loc];
+          a.cllo[gp] = t.lo[cur][loc];
+          a.cx[gp] = (int)ge;
+        }
+      } else {
+        FF v{t.hi[cur][loc], t.lo[cur][loc]};
+        if (ge >= 0) {
+          int ex = a.eidx[ge];
+          v = ff_add(v, FF{a.Dhi[ex], a.Dlo[ex]});
+        }
+        a.out[gp] = __fadd_rn(v.hi, v.lo);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// D(e) = path sum from receiver(e) to its outlet:
+//   D(e) = lps(receiver(e)) + D(exit reached from receiver(e)).
+__global__ void down_init_kernel(const int *__restrict__ elist,
+                                 const int *__restrict__ ecount,
+                                 const uint8_t *__restrict__ dir, int64_t m,
+                                 unsigned order, const float *__restrict__ clhi,
+                                 const float *__restrict__ cllo,
+                                 const int *__restrict__ cx,
+                                 const int *__restrict__ eidx,
+                                 float *Dhi, float *Dlo, int *nx) {
+  const int E = *ecount;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
+    int e = elist[a];
+    int64_t r = receiver_of(dir, e, m, order);
+    Dhi[a] = clhi[r];
+    Dlo[a] = cllo[r];
+    int x = cx[r];
+    nx[a] = x >= 0 ? eidx[x] : -1;
+  }
+}
+
+__global__ void down_jump_kernel(const int *__restrict__ ecount,
+                                 const float *__restrict__ Dhi0,
+                                 const float *__restrict__ Dlo0,
+                                 const int *__restrict__ nx0, float *Dhi1,
+                                 float *Dlo1, int *nx1, int *active) {
+  const int E = *ecount;
+  int act = 0;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
+    int q = nx0[a];
+    FF v{Dhi0[a], Dlo0[a]};
+    int nq = -1;
+    if (q >= 0) {
+      v = ff_add(v, FF{Dhi0[q], Dlo0[q]});
+      nq = nx0[q];
+    }
+    Dhi1[a] = v.hi;
+    Dlo1[a] = v.lo;
+    nx1[a] = nq;
+    act |= nq >= 0;
+  }
+  if (__any_sync(__activemask(), act) && (threadIdx.x & 31) == 0) atomicAdd(active, 1);
+}
+
+__global__ void maxabs_kernel(const float *__restrict__ w, int64_t N,
+                              unsigned *__restrict__ out) {
+  unsigned mx = 0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    unsigned b = __float_as_uint(w[p]) & 0x7fffffffu;
+    if (b > mx) mx = b;  // NaN/INF sort above every finite value
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+int list_grid(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  int64_t cap = (int64_t)sm_count() * 16;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+struct UpWork {
+  long long *cacc;
+  int *cH, *cpend, *cnext, *chop, *xmap, *xsteps, *elist, *leaves, *h;
+  int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err, [5] maxabs
+};
+
+tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
+                        UpWork &w) {
+  const size_t N = (size_t)g.cells();
+  Workspace &ws = workspace();
+  size_t need = 256 + 8 * align_up(N * 4) + (want_acc ? align_up(N * 8) : 0) +
+                (want_h ? 2 * align_up(N * 4) : 0) + 4096;
+  if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
+  w.counters = (int *)ws.take(256);
+  w.cacc = want_acc ? (long long *)ws.take(N * 8) : nullptr;
+  w.cH = want_h ? (int *)ws.take(N * 4) : nullptr;
+  w.h = want_h ? (int *)ws.take(N * 4) : nullptr;
+  w.cpend = (int *)ws.take(N * 4);
+  w.cnext = (int *)ws.take(N * 4);
+  w.chop = (int *)ws.take(N * 4);
+  w.xmap = (int *)ws.take(N * 4);
+  w.xsteps = (int *)ws.take(N * 4);
+  w.elist = (int *)ws.take(N * 4);
+  w.leaves = (int *)ws.take(N * 4);
+  return TT_CUDA_SUCCESS;
+}
+
+// Runs both tile passes and the coarse walk.
+tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
+                      const GridDims &g, unsigned order, bool want_acc,
+                      bool want_h, float *acc_out, UpWork &w, cudaStream_t st) {
+  const int T = g.tiles();
+  TT_CHECK(cudaMemsetAsync(w.counters, 0, 256, st));
+  UpArgs a{};
+  a.dir = dir;
+  a.m = g.m;
+  a.n = g.n;
+  a.tm = g.tm;
+  a.tn = g.tn;
+  a.order = order;
+  a.w = weights;
+  a.wshift = wshift;
+  a.phase = 1;
+  a.want_acc = want_acc;
+  a.want_h = want_h;
+  a.cacc = w.cacc;
+  a.cH = w.cH;
+  a.cpend = w.cpend;
+  a.xmap = w.xmap;
+  a.xsteps = w.xsteps;
+  a.elist = w.elist;
+  a.ecount = w.counters + 0;
+  a.acc_out = acc_out;
+  a.h_out = w.h;
+  a.hmax = w.counters + 3;
+  a.err = w.counters + 4;
+  const int tgrid = (int)std::min<int64_t>((T + kUpWarps - 1) / kUpWarps,
+                                           (int64_t)sm_count() * 32);
+  TT_LAUNCH(forest_up_kernel, tgrid, kUpWarps * 32, 0, st, a);
+  const int lg = list_grid(g.cells() / 8 + 1);
+  TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
+            g.m, order, w.xmap, w.xsteps, w.cnext, w.chop, w.cpend);
+  TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.elist, w.counters + 0,
+            w.cpend, w.leaves, w.counters + 1);
+  TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1,
+            w.cnext, w.chop, w.cacc, w.cH, w.cpend, want_acc, want_h,
+            w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
+  a.phase = 3;
+  TT_LAUNCH(forest_up_kernel, tgrid, kUpWarps * 32, 0, st, a);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+// Reads the counters back and maps error bits to a status.
+tt_cuda_status up_status(UpWork &w, cudaStream_t st, int *host6) {
+  int *h = (int *)pinned_scratch();
+  if (!h) return TT_CUDA_ERR_ALLOC;
+  TT_CHECK(cudaMemcpyAsync(h, w.counters, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaStreamSynchronize(st));
+  for (int k = 0; k < 6; k++) host6[k] = h[k];
+  if (host6[2] != host6[0]) return TT_CUDA_ERR_CYCLE;  // coarse nodes not all reached
+  if (host6[4] & ERR_CYCLE) return TT_CUDA_ERR_CYCLE;
+  if (host6[4] & (ERR_BADDIR | ERR_WEIGHT)) return TT_CUDA_ERR_INVALID_ARGUMENT;
+  return TT_CUDA_SUCCESS;
+}
+
+}  // namespace
+
+tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
+                              const float *weights, const GridDims &g,
+                              cudaStream_t st) {
+  UpWork w;
+  {
+    tt_cuda_status s = up_alloc(g, true, false, w);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  int wshift = 0;
+  if (weights) {
+    unsigned *mx = (unsigned *)(w.counters + 5);
+    TT_CHECK(cudaMemsetAsync(mx, 0, 4, st));
+    TT_LAUNCH(maxabs_kernel, list_grid(g.cells()), 256, 0, st, weights, g.cells(), mx);
+    unsigned *h = (unsigned *)pinned_scratch();
+    if (!h) return TT_CUDA_ERR_ALLOC;
+    TT_CHECK(cudaMemcpyAsync(h, mx, 4, cudaMemcpyDeviceToHost, st));
+    TT_CHECK(cudaStreamSynchronize(st));
+    unsigned bits = *h;
+    float mxv;
+    std::memcpy(&mxv, &bits, 4);
+    if (bits >= 0x7f800000u) mxv = 0.0f;  // non-finite weights are flagged per pixel
+    if (mxv > 0.0f) {
+      double bound = (double)mxv * (double)g.cells();
+      int e = (int)std::ceil(std::log2(bound));
+      wshift = 62 - e;
+    }
+  }
+  {
+    tt_cuda_status s = up_run(dir, weights, wshift, g, 0, true, false, acc, w, st);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  int h6[6];
+  return up_status(w, st, h6);
+}
+
+tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
+                              const GridDims &g, unsigned order,
+                              cudaStream_t st) {
+  UpWork w;
+  {
+    tt_cuda_status s = up_alloc(g, false, true, w);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  {
+    tt_cuda_status s = up_run(dir, nullptr, 0, g, order, false, true, nullptr, w, st);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  int h6[6];
+  tt_cuda_status s = up_status(w, st, h6);
+  if (s == TT_CUDA_ERR_CYCLE) return s;
+  const int H = h6[3] + 1;
+  // hist, off and cursor reuse the coarse arrays (no longer needed).
+  int *hist = w.cpend, *off = w.cnext, *cursor = w.chop;
+  if ((int64_t)H > g.cells()) return TT_CUDA_ERR_CYCLE;
+  TT_CHECK(cudaMemsetAsync(hist, 0, (size_t)H * 4, st));
+  TT_CHECK(cudaMemsetAsync(cursor, 0, (size_t)H * 4, st));
+  const int eg = list_grid(g.cells());
+  TT_LAUNCH(h_hist_kernel, eg, 256, 0, st, w.h, g.cells(), hist);
+  TT_LAUNCH(scan_kernel, 1, 1024, 0, st, hist, off, H);
+  TT_LAUNCH(node_scatter_kernel, eg, 256, 0, st, w.h, g.cells(), off, cursor, node);
+  TT_CHECK(cudaGetLastError());
+  return s;
+}
+
+tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
+                                       const float *grad_acc, const GridDims &g,
+                                       cudaStream_t st) {
+  const size_t N = (size_t)g.cells();
+  Workspace &ws = workspace();
+  size_t need = 256 + 11 * align_up(N * 4) + 4096;
+  if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
+  int *counters = (int *)ws.take(256);
+  float *clhi = (float *)ws.take(N * 4);
+  float *cllo = (float *)ws.take(N * 4);
+  int *cx = (int *)ws.take(N * 4);
+  int *eidx = (int *)ws.take(N * 4);
+  int *elist = (int *)ws.take(N * 4);
+  float *D[2][2] = {{(float *)ws.take(N * 4), (float *)ws.take(N * 4)},
+                    {(float *)ws.take(N * 4), (float *)ws.take(N * 4)}};
+  int *nx[2] = {(int *)ws.take(N * 4), (int *)ws.take(N * 4)};
+  TT_CHECK(cudaMemsetAsync(counters, 0, 256, st));
+  DownArgs a{};
+  a.dir = dir;
+  a.g = grad_acc;
+  a.m = g.m;
+  a.n = g.n;
+  a.tm = g.tm;
+  a.tn = g.tn;
+  a.order = 0;
+  a.phase = 1;
+  a.clhi = clhi;
+  a.cllo = cllo;
+  a.cx = cx;
+  a.eidx = eidx;
+  a.elist = elist;
+  a.ecount = counters + 0;
+  a.out = grad_w;
+  a.err = counters + 4;
+  const int T = g.tiles();
+  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 64);
+  TT_LAUNCH(forest_down_kernel, tgrid, 32, 0, st, a);
+  const int lg = list_grid(g.cells() / 8 + 1);
+  TT_LAUNCH(down_init_kernel, lg, 256, 0, st, elist, counters + 0, dir, g.m, 0u,
+            clhi, cllo, cx, eidx, D[0][0], D[0][1], nx[0]);
+  int *hcnt = (int *)pinned_scratch();
+  if (!hcnt) return TT_CUDA_ERR_ALLOC;
+  int cur = 0;
+  for (int round = 0; round < 40; round += 4) {
+    for (int b = 0; b < 4; b++) {
+      TT_CHECK(cudaMemsetAsync(counters + 1, 0, 4, st));
+      TT_LAUNCH(down_jump_kernel, lg, 256, 0, st, counters + 0, D[cur][0], D[cur][1],
+                nx[cur], D[cur ^ 1][0], D[cur ^ 1][1], nx[cur ^ 1], counters + 1);
+      cur ^= 1;
+    }
+    TT_CHECK(cudaMemcpyAsync(hcnt, counters + 1, 4, cudaMemcpyDeviceToHost, st));
+    TT_CHECK(cudaStreamSynchronize(st));
+    if (*hcnt == 0) break;
+    if (round + 4 >= 40) return TT_CUDA_ERR_CYCLE;
+  }
+  a.phase = 3;
+  a.Dhi = D[cur][0];
+  a.Dlo = D[cur][1];
+  TT_LAUNCH(forest_down_kernel, tgrid, 32, 0, st, a);
+  TT_CHECK(cudaGetLastError());
+  TT_CHECK(cudaMemcpyAsync(hcnt, counters + 4, 4, cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaStreamSynchronize(st));
+  if (*hcnt & ERR_BADDIR) return TT_CUDA_ERR_INVALID_ARGUMENT;
+  return TT_CUDA_SUCCESS;
+}
+
+}  // namespace tt

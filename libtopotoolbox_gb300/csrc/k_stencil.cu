@@ -1,0 +1,378 @@
+// 3x3 stencil kernels: flat/sill/presill labelling, D8 carve directions,
+// second-order gradients, hillshade and the hillshade adjoint.
+//
+// Every kernel is HBM-bound.  Tiles of 32 x 32 pixels (plus a halo) are
+// staged in shared memory with coalesced 128-byte column segments, so each
+// input byte is read from DRAM about once.
+#include <cmath>
+
+#include "tt_internal.cuh"
+
+namespace tt {
+namespace {
+
+constexpr int kBlockX = 32;  // along i
+constexpr int kBlockY = 8;   // along j
+
+// ------------------------------------------------------------------
+// identifyflats (src/identifyflats.c:33-121)
+//
+// One block handles a 32 x 32 tile.  Shared memory holds the DEM of the tile
+// with a two-pixel halo; flat bits are computed for the tile plus a one-pixel
+// ring, after which sill and presill bits are gathered per pixel:
+//   sill(s)    = !flat(s) && exists flat neighbour f with z_f == z_s
+//   presill(f) =  flat(f) && exists non-flat neighbour s with z_s == z_f
+// which is the scatter at src/identifyflats.c:83-119 restated as a gather.
+// ------------------------------------------------------------------
+constexpr int kFH = kTile + 4;  // 36: tile + 2-pixel halo
+
+__global__ void __launch_bounds__(kBlockX * kBlockY)
+identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
+                     int64_t m, int64_t n, unsigned long long *count) {
+  __shared__ float z[kFH][kFH + 1];           // [c][r], 2-pixel halo
+  __shared__ uint8_t flat[kTile + 2][kTile + 3];  // [c][r], 1-pixel ring
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kTile;
+  const int64_t j0 = (int64_t)blockIdx.y * kTile;
+
+  for (int c = ty; c < kFH; c += kBlockY) {
+    int64_t j = j0 - 2 + c;
+    for (int r = tx; r < kFH; r += kBlockX) {
+      int64_t i = i0 - 2 + r;
+      float v = NAN;
+      if (i >= 0 && i < m && j >= 0 && j < n) v = dem[j * m + i];
+      z[c][r] = v;
+    }
+  }
+  __syncthreads();
+
+  // Flat bits for the tile and its one-pixel ring.
+  for (int c = ty; c < kTile + 2; c += kBlockY) {
+    int64_t j = j0 - 1 + c;
+    for (int r = tx; r < kTile + 2; r += kBlockX) {
+      int64_t i = i0 - 1 + r;
+      uint8_t f = 0;
+      if (i >= 1 && i < m - 1 && j >= 1 && j < n - 1) {
+        float zc = z[c + 1][r + 1];
+        float lo = zc;
+#pragma unroll
+        for (int dc = -1; dc <= 1; dc++)
+#pragma unroll
+          for (int dr = -1; dr <= 1; dr++) {
+            if (dc == 0 && dr == 0) continue;
+            float zn = z[c + 1 + dc][r + 1 + dr];
+            lo = fminf(lo, isnan(zn) ? -INFINITY : zn);
+          }
+        f = (zc == lo) ? 1 : 0;
+      }
+      flat[c][r] = f;
+    }
+  }
+  __syncthreads();
+
+  unsigned local = 0;
+  for (int c = ty; c < kTile; c += kBlockY) {
+    int64_t j = j0 + c;
+    if (j >= n) break;
+    int r = tx;
+    int64_t i = i0 + r;
+    if (i >= m) continue;
+    float zc = z[c + 2][r + 2];
+    int fc = flat[c + 1][r + 1];
+    int32_t v = fc;
+    bool hit = false;
+#pragma unroll
+    for (int dc = -1; dc <= 1; dc++)
+#pragma unroll
+      for (int dr = -1; dr <= 1; dr++) {
+        if (dc == 0 && dr == 0) continue;
+        int64_t ni = i + dr, nj = j + dc;
+        if (ni < 0 || ni >= m || nj < 0 || nj >= n) continue;
+        int fn = flat[c + 1 + dc][r + 1 + dr];
+        if (fn != fc && z[c + 2 + dc][r + 2 + dr] == zc) hit = true;
+      }
+    if (hit) v |= fc ? 4 : 2;
+    out[j * m + i] = v;
+    local += fc;
+  }
+  // Block reduction of the flat count.
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+  __shared__ unsigned warp_sum[kBlockY];
+  if (tx == 0) warp_sum[ty] = local;
+  __syncthreads();
+  if (ty == 0 && tx == 0) {
+    unsigned s = 0;
+    for (int w = 0; w < kBlockY; w++) s += warp_sum[w];
+    if (s) atomicAdd(count, (unsigned long long)s);
+  }
+}
+
+// ------------------------------------------------------------------
+// D8 carve directions (src/flow_routing.c:15-76)
+//
+// z = flat ? dist : dem; neighbours higher than the centre (in dem) are
+// skipped; g = (z - z_n) / chamfer with chamfer = sqrtf(2) on odd bits; the
+// first strictly largest positive g wins.  The subtraction and the IEEE
+// division are written with explicit round-to-nearest intrinsics so that no
+// contraction changes a bit.
+// ------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlockX * kBlockY)
+directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
+                  const float *__restrict__ dist,
+                  const int32_t *__restrict__ flats, int64_t m, int64_t n,
+                  unsigned order) {
+  __shared__ float zs[kTile + 2][kTile + 3];
+  __shared__ float ds[kTile + 2][kTile + 3];
+  __shared__ uint8_t fs[kTile + 2][kTile + 3];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kTile;
+  const int64_t j0 = (int64_t)blockIdx.y * kTile;
+  for (int c = ty; c < kTile + 2; c += kBlockY) {
+    int64_t j = j0 - 1 + c;
+    for (int r = tx; r < kTile + 2; r += kBlockX) {
+      int64_t i = i0 - 1 + r;
+      float a = NAN, b = NAN;
+      uint8_t f = 0;
+      if (i >= 0 && i < m && j >= 0 && j < n) {
+        int64_t p = j * m + i;
+        a = dem[p];
+        b = dist[p];
+        f = (uint8_t)(flats[p] & 1);
+      }
+      zs[c][r] = a;
+      ds[c][r] = b;
+      fs[c][r] = f;
+    }
+  }
+  __syncthreads();
+  const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
+  for (int c = ty; c < kTile; c += kBlockY) {
+    int64_t j = j0 + c;
+    int64_t i = i0 + tx;
+    if (j >= n || i >= m) continue;
+    int r = tx;
+    bool fl = fs[c + 1][r + 1] != 0;
+    float zc = zs[c + 1][r + 1];
+    float z = fl ? ds[c + 1][r + 1] : zc;
+    float best = 0.0f;
+    uint8_t d = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      int di = d8_di(k, order), dj = d8_dj(k, order);
+      int64_t ni = i + di, nj = j + dj;
+      if (ni < 0 || ni >= m || nj < 0 || nj >= n) continue;
+      float zn = zs[c + 1 + dj][r + 1 + di];
+      if (zn > zc) continue;
+      float zz = fl ? ds[c + 1 + dj][r + 1 + di] : zn;
+      float g = __fdiv_rn(__fsub_rn(z, zz), (k & 1) ? sq2 : 1.0f);
+      if (g > best) {
+        best = g;
+        d = (uint8_t)(1u << k);
+      }
+    }
+    dir[j * m + i] = d;
+  }
+}
+
+// ------------------------------------------------------------------
+// Second-order gradient and hillshade (src/hillshade.c:11-213)
+// ------------------------------------------------------------------
+struct Grad {
+  float dx, dy;
+};
+
+// Gradient along one axis at position k of len, reading the stencil values
+// a(-2..2) around the centre.  Mirrors src/hillshade.c:113-155.
+__device__ __forceinline__ float axis_grad(float zm2, float zm1, float z0,
+                                           float zp1, float zp2, int64_t k,
+                                           int64_t len, float twoh) {
+  if (k == 0) return (-zp2 + 4 * zp1 - 3 * z0) / twoh;
+  if (k == len - 1) return (zm2 - 4 * zm1 + 3 * z0) / twoh;
+  return isnan(z0) ? NAN : (zp1 - zm1) / twoh;
+}
+
+__device__ __forceinline__ float shade(float dx, float dy, float sx, float sy,
+                                       float sz) {
+  float inv = 1.0f / sqrtf(dx * dx + dy * dy + 1.0f);
+  return (-dx * inv) * sx + (-dy * inv) * sy + inv * sz;
+}
+
+constexpr int kHS = kTile + 4;  // 2-pixel halo for one-sided borders
+
+template <int MODE>  // 0: hillshade, 1: gradients, 2: hillshade backward
+__global__ void __launch_bounds__(kBlockX * kBlockY)
+hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
+                 const float *__restrict__ dem, const float *__restrict__ gout,
+                 int64_t m, int64_t n, float twoh, float sx, float sy, float sz) {
+  __shared__ float z[kHS][kHS + 1];
+  __shared__ float hx[MODE == 2 ? kHS : 1][kHS + 1];
+  __shared__ float hy[MODE == 2 ? kHS : 1][kHS + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kTile;
+  const int64_t j0 = (int64_t)blockIdx.y * kTile;
+  for (int c = ty; c < kHS; c += kBlockY) {
+    int64_t j = j0 - 2 + c;
+    for (int r = tx; r < kHS; r += kBlockX) {
+      int64_t i = i0 - 2 + r;
+      z[c][r] = (i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : 0.0f;
+    }
+  }
+  __syncthreads();
+  if (MODE == 2) {
+    // dH/d(dx) and dH/d(dy) (times the upstream gradient) for the tile and a
+    // two-pixel ring: every DEM sample of the tile is read by stencils
+    // centred at most two pixels away.
+    for (int c = ty; c < kHS; c += kBlockY) {
+      int64_t j = j0 - 2 + c;
+      for (int r = tx; r < kHS; r += kBlockX) {
+        int64_t i = i0 - 2 + r;
+        float ax = 0.f, ay = 0.f;
+        if (i >= 0 && i < m && j >= 0 && j < n) {
+          auto zz = [&](int dc, int dr) {
+            int cc = c + dc, rr = r + dr;
+            if (cc < 0 || cc >= kHS || rr < 0 || rr >= kHS) {
+              int64_t gi = i + dr, gj = j + dc;
+              return (gi >= 0 && gi < m && gj >= 0 && gj < n) ? dem[gj * m + gi] : 0.0f;
+            }
+            return z[cc][rr];
+          };
+          float dx = axis_grad(zz(0, -2), zz(0, -1), zz(0, 0), zz(0, 1), zz(0, 2), i, m, twoh);
+          float dy = axis_grad(zz(-2, 0), zz(-1, 0), zz(0, 0), zz(1, 0), zz(2, 0), j, n, twoh);
+          float q = dx * dx + dy * dy + 1.0f;
+          float inv = 1.0f / sqrtf(q);
+          float num = -dx * sx - dy * sy + sz;
+          if (!isnan(num * inv)) {
+            float inv3 = inv * inv * inv;
+            float g = gout[j * m + i];
+            ax = g * (-sx * inv - num * dx * inv3);
+            ay = g * (-sy * inv - num * dy * inv3);
+          }
+        }
+        hx[c][r] = ax;
+        hy[c][r] = ay;
+      }
+    }
+    __syncthreads();
+  }
+  for (int c = ty; c < kTile; c += kBlockY) {
+    int64_t j = j0 + c;
+    int64_t i = i0 + tx;
+    if (j >= n || i >= m) continue;
+    int r = tx + 2, cc = c + 2;
+    int64_t p = j * m + i;
+    if (MODE == 0 || MODE == 1) {
+      float dx = axis_grad(z[cc][r - 2], z[cc][r - 1], z[cc][r], z[cc][r + 1],
+                           z[cc][r + 2], i, m, twoh);
+      float dy = axis_grad(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
+                           z[cc + 2][r], j, n, twoh);
+      if (MODE == 0) {
+        out0[p] = shade(dx, dy, sx, sy, sz);
+      } else {
+        out0[p] = dx;
+        out1[p] = dy;
+      }
+    } else {
+      // Transposed stencils: sample (i, j) receives from the centres whose
+      // stencil reads it.  Along i: centre i+1 reads i with -1 (central),
+      // centre i-1 reads i with +1; the one-sided border stencils at 0 and
+      // m-1 read i in {0,1,2} and {m-3,m-2,m-1}.
+      float acc = 0.0f;
+      // along i (axis length m)
+      for (int d = -2; d <= 2; d++) {
+        int64_t k = i + d;  // centre position
+        if (k < 0 || k >= m) continue;
+        float a = hx[cc][r + d];
+        float w = 0.0f;
+        int off = (int)(i - k);  // sample offset relative to the centre
+        if (k == 0) {
+          w = (off == 0) ? -3.f : (off == 1) ? 4.f : (off == 2) ? -1.f : 0.f;
+        } else if (k == m - 1) {
+          w = (off == 0) ? 3.f : (off == -1) ? -4.f : (off == -2) ? 1.f : 0.f;
+        } else {
+          w = (off == 1) ? 1.f : (off == -1) ? -1.f : 0.f;
+        }
+        if (w != 0.f) acc += w * a;
+      }
+      for (int d = -2; d <= 2; d++) {
+        int64_t k = j + d;
+        if (k < 0 || k >= n) continue;
+        float a = hy[cc + d][r];
+        float w = 0.0f;
+        int off = (int)(j - k);
+        if (k == 0) {
+          w = (off == 0) ? -3.f : (off == 1) ? 4.f : (off == 2) ? -1.f : 0.f;
+        } else if (k == n - 1) {
+          w = (off == 0) ? 3.f : (off == -1) ? -4.f : (off == -2) ? 1.f : 0.f;
+        } else {
+          w = (off == 1) ? 1.f : (off == -1) ? -1.f : 0.f;
+        }
+        if (w != 0.f) acc += w * a;
+      }
+      out0[p] = acc / twoh;
+    }
+  }
+}
+
+dim3 tile_grid(const GridDims &g) { return dim3(g.tm, g.tn); }
+
+}  // namespace
+
+tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
+                                 const GridDims &g,
+                                 unsigned long long *count_dev,
+                                 cudaStream_t st) {
+  unsigned long long *cnt = count_dev;
+  if (!cnt) {
+    Workspace &ws = workspace();
+    if (!ws.reserve(256)) return TT_CUDA_ERR_ALLOC;
+    cnt = (unsigned long long *)ws.take(8);
+  }
+  TT_CHECK(cudaMemsetAsync(cnt, 0, 8, st));
+  TT_LAUNCH(identifyflats_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
+            flags, dem, g.m, g.n, cnt);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status directions_dev(uint8_t *dir, const float *dem, const float *dist,
+                              const int32_t *flats, const GridDims &g,
+                              unsigned order, cudaStream_t st) {
+  TT_LAUNCH(directions_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st, dir,
+            dem, dist, flats, g.m, g.n, order);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status gradient2_dev(float *p0, float *p1, const float *dem,
+                             float cellsize, const GridDims &g,
+                             cudaStream_t st) {
+  TT_LAUNCH(hillshade_kernel<1>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
+            p0, p1, dem, nullptr, g.m, g.n, 2 * cellsize, 0.f, 0.f, 0.f);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
+                             float altitude, float cellsize, const GridDims &g,
+                             cudaStream_t st) {
+  float sx, sy, sz;
+  sun_vector(azimuth, altitude, &sx, &sy, &sz);
+  TT_LAUNCH(hillshade_kernel<0>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
+            out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,
+                                      const float *grad_out, float azimuth,
+                                      float altitude, float cellsize,
+                                      const GridDims &g, cudaStream_t st) {
+  float sx, sy, sz;
+  sun_vector(azimuth, altitude, &sx, &sy, &sz);
+  TT_LAUNCH(hillshade_kernel<2>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
+            grad_dem, nullptr, dem, grad_out, g.m, g.n, 2 * cellsize, sx, sy, sz);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+}  // namespace tt

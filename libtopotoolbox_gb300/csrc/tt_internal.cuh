@@ -1,0 +1,170 @@
+// Internal declarations shared by the CUDA translation units of libtt_cuda.
+//
+// Layout conventions (include/topotoolbox.h:284-290): a grid has m = dims[0]
+// rows along the fastest (contiguous) axis i and n = dims[1] columns along j;
+// pixel (i, j) lives at p = j * m + i.  Tiles are 32 x 32 pixels, numbered
+// column-major: tile (ti, tj) has id tj * tiles_m + ti.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/tt_cuda.h"
+
+namespace tt {
+
+constexpr int kTile = 32;          // tile side (pixels)
+constexpr int kHalo = kTile + 2;   // tile plus one-pixel halo ring
+constexpr int kPitch = kHalo + 1;  // padded row pitch in shared memory (35):
+                                   // (3c + r) mod 32 is conflict-free both
+                                   // along r and along c.
+
+struct GridDims {
+  int64_t m;  // dims[0], fastest
+  int64_t n;  // dims[1]
+  int tm;     // tiles along i
+  int tn;     // tiles along j
+  __host__ __device__ int64_t cells() const { return m * n; }
+  __host__ __device__ int tiles() const { return tm * tn; }
+};
+
+inline GridDims make_dims(const ptrdiff_t dims[2]) {
+  GridDims g;
+  g.m = dims[0];
+  g.n = dims[1];
+  g.tm = (int)((g.m + kTile - 1) / kTile);
+  g.tn = (int)((g.n + kTile - 1) / kTile);
+  return g;
+}
+
+// D8 neighbour offsets in the bit order of include/topotoolbox.h:807-816,
+// for column-major (order 0) arrays: bit k points to (i + di[k], j + dj[k]).
+// Row-major (order 1) swaps the two tables (src/flow_routing.c:39-49).
+__host__ __device__ inline int d8_di(int k, unsigned order) {
+  const int a[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+  const int b[8] = {1, 1, 0, -1, -1, -1, 0, 1};
+  return (order & 1) ? b[k] : a[k];
+}
+__host__ __device__ inline int d8_dj(int k, unsigned order) {
+  const int a[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+  const int b[8] = {1, 1, 0, -1, -1, -1, 0, 1};
+  return (order & 1) ? a[k] : b[k];
+}
+
+// Index of the highest set bit, as the reference decodes a direction byte
+// (src/flow_accumulation.c:63-67).
+__device__ __forceinline__ int d8_bit(unsigned d) { return 31 - __clz(d); }
+
+// ------------------------------------------------------------------
+// Status, launch accounting, workspace
+// ------------------------------------------------------------------
+
+void set_status(tt_cuda_status s);
+tt_cuda_status get_status();
+void note_launch(int count = 1);
+bool cuda_ok(cudaError_t e, const char *what);
+
+#define TT_LAUNCH(kernel, grid, block, smem, stream, ...)                   \
+  do {                                                                      \
+    kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);             \
+    ::tt::note_launch();                                                    \
+  } while (0)
+
+#define TT_CHECK(expr)                                                      \
+  do {                                                                      \
+    if (!::tt::cuda_ok((expr), #expr)) return TT_CUDA_ERR_CUDA;            \
+  } while (0)
+
+// A grow-only bump allocator over one device allocation per device.  Every
+// public call resets it on entry and carves its scratch from it; calls are
+// serialised per device (see DeviceLock).
+class Workspace {
+ public:
+  // Returns nullptr when the device allocation fails.
+  void *take(size_t bytes);
+  void reset() { used_ = 0; }
+  // Ensure `bytes` total capacity, reallocating if needed.  Must be called
+  // before take() in a call; invalidates earlier pointers.
+  bool reserve(size_t bytes);
+  void release();
+  size_t capacity() const { return cap_; }
+
+ private:
+  char *base_ = nullptr;
+  size_t cap_ = 0;
+  size_t used_ = 0;
+};
+
+Workspace &workspace();          // of the current device
+void *pinned_scratch();          // 4 KiB of pinned host memory per device
+int64_t max_rounds();
+void set_last_rounds(int64_t r);
+
+// RAII lock of the current device's call mutex.
+class DeviceLock {
+ public:
+  DeviceLock();
+  ~DeviceLock();
+
+ private:
+  int dev_;
+};
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+// Launch geometry: a persistent grid sized to the SM count.
+int sm_count();
+
+// ------------------------------------------------------------------
+// Stage entry points (device pointers, enqueued on `st`).  Each returns a
+// status; iterative stages synchronise `st`.
+// ------------------------------------------------------------------
+
+tt_cuda_status fill_dev(float *f, const float *dem, const uint8_t *bc,
+                        const GridDims &g, cudaStream_t st);
+// Grayscale reconstruction by dilation: marker := R(marker, mask).
+tt_cuda_status reconstruct_dev(float *marker, const float *mask,
+                               const GridDims &g, cudaStream_t st);
+tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
+                                 const GridDims &g,
+                                 unsigned long long *count_dev,
+                                 cudaStream_t st);
+tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
+                         const int32_t *flats, const float *orig,
+                         const float *filled, const GridDims &g,
+                         cudaStream_t st);
+tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
+                        const int32_t *flats, const GridDims &g,
+                        cudaStream_t st);
+tt_cuda_status directions_dev(uint8_t *dir, const float *dem,
+                              const float *dist, const int32_t *flats,
+                              const GridDims &g, unsigned order,
+                              cudaStream_t st);
+// Topological node order (every donor before its receiver) from directions.
+tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
+                              const GridDims &g, unsigned order,
+                              cudaStream_t st);
+tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
+                              const float *weights, const GridDims &g,
+                              cudaStream_t st);
+tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
+                                       const float *grad_acc,
+                                       const GridDims &g, cudaStream_t st);
+tt_cuda_status gradient2_dev(float *p0, float *p1, const float *dem,
+                             float cellsize, const GridDims &g,
+                             cudaStream_t st);
+tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
+                             float altitude, float cellsize, const GridDims &g,
+                             cudaStream_t st);
+tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,
+                                      const float *grad_out, float azimuth,
+                                      float altitude, float cellsize,
+                                      const GridDims &g, cudaStream_t st);
+
+// Sun vector of src/hillshade.c:104-106, evaluated in double and rounded.
+void sun_vector(float azimuth, float altitude, float *sx, float *sy, float *sz);
+
+}  // namespace tt

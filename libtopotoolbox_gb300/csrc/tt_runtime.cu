@@ -1,0 +1,715 @@
+// Runtime and C ABI of libtt_cuda: per-thread status, per-device
+// workspaces and call locks, and the public entry points of
+// include/tt_cuda.h.  Host-pointer entry points stage their arrays through
+// device buffers and call the device-pointer stage functions.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "tt_internal.cuh"
+
+namespace tt {
+
+namespace {
+thread_local tt_cuda_status g_status = TT_CUDA_SUCCESS;
+thread_local int64_t g_launches = 0;
+thread_local int64_t g_last_rounds = 0;
+int64_t g_max_rounds_override = 0;
+
+constexpr int kMaxDevices = 64;
+
+struct DeviceState {
+  std::mutex mu;
+  Workspace scratch;
+  Workspace io;
+  void *pinned = nullptr;
+  int sms = 0;
+};
+
+DeviceState g_dev[kMaxDevices];
+
+int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) d = 0;
+  return (d >= 0 && d < kMaxDevices) ? d : 0;
+}
+}  // namespace
+
+void set_status(tt_cuda_status s) { g_status = s; }
+tt_cuda_status get_status() { return g_status; }
+void note_launch(int count) { g_launches += count; }
+void set_last_rounds(int64_t r) { g_last_rounds = r; }
+
+bool cuda_ok(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  if (std::getenv("TT_CUDA_VERBOSE"))
+    std::fprintf(stderr, "tt_cuda: %s failed: %s\n", what, cudaGetErrorString(e));
+  return false;
+}
+
+int64_t max_rounds() {
+  if (g_max_rounds_override > 0) return g_max_rounds_override;
+  static int64_t env = [] {
+    const char *s = std::getenv("TT_CUDA_MAX_ROUNDS");
+    return s ? std::atoll(s) : 0LL;
+  }();
+  return env > 0 ? env : 1000000;
+}
+
+void *Workspace::take(size_t bytes) {
+  size_t need = align_up(used_) + align_up(bytes);
+  if (need > cap_) return nullptr;
+  void *p = base_ + align_up(used_);
+  used_ = need;
+  return p;
+}
+
+bool Workspace::reserve(size_t bytes) {
+  used_ = 0;
+  if (bytes <= cap_) return true;
+  if (base_) cudaFree(base_);
+  base_ = nullptr;
+  cap_ = 0;
+  size_t want = align_up(bytes, 1 << 20);
+  if (std::getenv("TT_CUDA_FAIL_ALLOC")) return false;  // fault injection
+  if (cudaMalloc(&base_, want) != cudaSuccess) {
+    cudaGetLastError();
+    base_ = nullptr;
+    return false;
+  }
+  cap_ = want;
+  return true;
+}
+
+void Workspace::release() {
+  if (base_) cudaFree(base_);
+  base_ = nullptr;
+  cap_ = used_ = 0;
+}
+
+Workspace &workspace() { return g_dev[current_device()].scratch; }
+static Workspace &io_workspace() { return g_dev[current_device()].io; }
+
+void *pinned_scratch() {
+  DeviceState &d = g_dev[current_device()];
+  if (!d.pinned) {
+    if (cudaMallocHost(&d.pinned, 4096) != cudaSuccess) {
+      cudaGetLastError();
+      d.pinned = nullptr;
+    }
+  }
+  return d.pinned;
+}
+
+int sm_count() {
+  DeviceState &d = g_dev[current_device()];
+  if (d.sms == 0) {
+    int dev = current_device(), v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    d.sms = v > 0 ? v : 1;
+  }
+  return d.sms;
+}
+
+DeviceLock::DeviceLock() : dev_(current_device()) { g_dev[dev_].mu.lock(); }
+DeviceLock::~DeviceLock() { g_dev[dev_].mu.unlock(); }
+
+void sun_vector(float azimuth, float altitude, float *sx, float *sy,
+                float *sz) {
+  double zen = 1.57079632679489661923132169163975 - (double)altitude;
+  *sx = (float)(std::sin(zen) * std::cos((double)azimuth));
+  *sy = (float)(std::sin(zen) * std::sin((double)azimuth));
+  *sz = (float)std::cos(zen);
+}
+
+}  // namespace tt
+
+using namespace tt;
+
+// ------------------------------------------------------------------
+// Helpers for the host-pointer entry points
+// ------------------------------------------------------------------
+namespace {
+
+bool dims_ok(const ptrdiff_t dims[2]) {
+  return dims && dims[0] > 0 && dims[1] > 0 && dims[0] < (1LL << 31) &&
+         dims[1] < (1LL << 31) && dims[0] * dims[1] < (1LL << 31);
+}
+
+bool have_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
+// Device staging for one host-pointer call.
+struct Staging {
+  std::vector<std::pair<void *, size_t>> plan;
+  Workspace &ws = io_workspace();
+  size_t total = 0;
+  void add(size_t bytes) { total += align_up(bytes); }
+  bool reserve() { return ws.reserve(total); }
+  void *take(size_t bytes) { return ws.take(bytes); }
+};
+
+tt_cuda_status h2d(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  TT_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  return TT_CUDA_SUCCESS;
+}
+tt_cuda_status d2h(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  TT_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status finish(tt_cuda_status s, cudaStream_t st) {
+  if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED ||
+      s == TT_CUDA_ERR_CYCLE) {
+    if (!cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+      s = TT_CUDA_ERR_CUDA;
+  }
+  if (s == TT_CUDA_ERR_CUDA) cudaGetLastError();
+  set_status(s);
+  return s;
+}
+
+#define TT_TRY(expr)                                  \
+  do {                                                \
+    tt_cuda_status _s = (expr);                       \
+    if (_s != TT_CUDA_SUCCESS) return _s;             \
+  } while (0)
+
+#define TT_TRY_SOFT(expr, keep)                                            \
+  do {                                                                     \
+    tt_cuda_status _s = (expr);                                            \
+    if (_s == TT_CUDA_ERR_NOT_CONVERGED || _s == TT_CUDA_ERR_CYCLE)        \
+      keep = _s;                                                           \
+    else if (_s != TT_CUDA_SUCCESS)                                        \
+      return _s;                                                           \
+  } while (0)
+
+}  // namespace
+
+// ------------------------------------------------------------------
+// Library state
+// ------------------------------------------------------------------
+extern "C" {
+
+int tt_cuda_has_gpu(void) { return have_device() ? 1 : 0; }
+tt_cuda_status tt_cuda_last_error(void) { return get_status(); }
+
+const char *tt_cuda_status_string(tt_cuda_status s) {
+  switch (s) {
+    case TT_CUDA_SUCCESS: return "success";
+    case TT_CUDA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case TT_CUDA_ERR_ALLOC: return "allocation failed";
+    case TT_CUDA_ERR_CUDA: return "CUDA runtime error";
+    case TT_CUDA_ERR_NOT_CONVERGED: return "iteration cap reached";
+    case TT_CUDA_ERR_CYCLE: return "direction grid contains a cycle";
+    case TT_CUDA_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+void tt_cuda_set_max_rounds(int64_t rounds) {
+  g_max_rounds_override = rounds > 0 ? rounds : 0;
+}
+
+void tt_cuda_release_workspace(void) {
+  if (!have_device()) return;
+  DeviceLock lock;
+  workspace().release();
+  io_workspace().release();
+}
+
+int64_t tt_cuda_launch_count(int reset) {
+  int64_t v = g_launches;
+  if (reset) g_launches = 0;
+  return v;
+}
+
+int64_t tt_cuda_last_rounds(void) { return g_last_rounds; }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------
+// Device-pointer entry points
+// ------------------------------------------------------------------
+namespace {
+
+template <class F>
+tt_cuda_status dev_call(const ptrdiff_t dims[2], void *stream, F &&body) {
+  if (!dims_ok(dims)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return TT_CUDA_ERR_INVALID_ARGUMENT;
+  }
+  if (!have_device()) {
+    set_status(TT_CUDA_ERR_NO_DEVICE);
+    return TT_CUDA_ERR_NO_DEVICE;
+  }
+  DeviceLock lock;
+  cudaStream_t st = (cudaStream_t)stream;
+  GridDims g = make_dims(dims);
+  tt_cuda_status s = body(g, st);
+  return finish(s, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+tt_cuda_status tt_cuda_fillsinks_dev(float *output, const float *dem,
+                                     const uint8_t *bc, const ptrdiff_t dims[2],
+                                     void *stream) {
+  if (!output || !dem || !bc) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return fill_dev(output, dem, bc, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_reconstruct_dev(float *marker, const float *mask,
+                                       const ptrdiff_t dims[2], void *stream) {
+  if (!marker || !mask) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return reconstruct_dev(marker, mask, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_identifyflats_dev(int32_t *output, const float *dem,
+                                         const ptrdiff_t dims[2],
+                                         int64_t *count_dev, void *stream) {
+  if (!output || !dem) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return identifyflats_dev(output, dem, g, (unsigned long long *)count_dev, st);
+  });
+}
+
+tt_cuda_status tt_cuda_gwdt_computecosts_dev(float *costs, ptrdiff_t *conncomps,
+                                             const int32_t *flats,
+                                             const float *original_dem,
+                                             const float *filled_dem,
+                                             const ptrdiff_t dims[2],
+                                             void *stream) {
+  if (!costs || !conncomps || !flats || !original_dem || !filled_dem)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return costs_dev(costs, conncomps, flats, original_dem, filled_dem, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
+                                const int32_t *flats, const ptrdiff_t dims[2],
+                                void *stream) {
+  if (!dist || !costs || !flats) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return gwdt_dev(dist, prev, costs, flats, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_flow_routing_d8_carve_dev(ptrdiff_t *node,
+                                                 uint8_t *direction,
+                                                 const float *dem,
+                                                 const float *dist,
+                                                 const int32_t *flats,
+                                                 const ptrdiff_t dims[2],
+                                                 unsigned int order,
+                                                 void *stream) {
+  if (!direction || !dem || !dist || !flats || order > 1)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    TT_TRY(directions_dev(direction, dem, dist, flats, g, order, st));
+    if (!node) return TT_CUDA_SUCCESS;
+    return node_order_dev(node, direction, g, order, st);
+  });
+}
+
+tt_cuda_status tt_cuda_flow_accumulation_dev(float *acc,
+                                             const uint8_t *direction,
+                                             const float *weights,
+                                             const ptrdiff_t dims[2],
+                                             void *stream) {
+  if (!acc || !direction) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return accumulate_dev(acc, direction, weights, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_flow_accumulation_backward_dev(float *grad_weights,
+                                                      const uint8_t *direction,
+                                                      const float *grad_acc,
+                                                      const ptrdiff_t dims[2],
+                                                      void *stream) {
+  if (!grad_weights || !direction || !grad_acc)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return accumulate_backward_dev(grad_weights, direction, grad_acc, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_gradient_secondorder_dev(float *p0, float *p1,
+                                                const float *dem, float cellsize,
+                                                const ptrdiff_t dims[2],
+                                                void *stream) {
+  if (!p0 || !p1 || !dem || !dims || dims[0] < 3 || dims[1] < 3)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return gradient2_dev(p0, p1, dem, cellsize, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_hillshade_fused_dev(float *output, const float *dem,
+                                           float azimuth, float altitude,
+                                           float cellsize,
+                                           const ptrdiff_t dims[2],
+                                           void *stream) {
+  if (!output || !dem || !dims || dims[0] < 3 || dims[1] < 3)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return hillshade_dev(output, dem, azimuth, altitude, cellsize, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_hillshade_backward_dev(float *grad_dem, const float *dem,
+                                              const float *grad_output,
+                                              float azimuth, float altitude,
+                                              float cellsize,
+                                              const ptrdiff_t dims[2],
+                                              void *stream) {
+  if (!grad_dem || !dem || !grad_output || !dims || dims[0] < 3 || dims[1] < 3)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return hillshade_backward_dev(grad_dem, dem, grad_output, azimuth, altitude,
+                                  cellsize, g, st);
+  });
+}
+
+}  // extern "C"
+
+// The pipeline body shared by the device and host forms.  Missing
+// intermediates are carved from the io workspace by the caller.
+static tt_cuda_status pipeline_body(float *filled, int32_t *flats, float *dist,
+                                    ptrdiff_t *node, uint8_t *direction,
+                                    float *acc, float *hill, const float *dem,
+                                    const uint8_t *bc, const float *weights,
+                                    float az, float alt, float cs,
+                                    float *costs, ptrdiff_t *conncomps,
+                                    const GridDims &g, cudaStream_t st) {
+  tt_cuda_status soft = TT_CUDA_SUCCESS;
+  TT_TRY_SOFT(fill_dev(filled, dem, bc, g, st), soft);
+  TT_TRY(identifyflats_dev(flats, filled, g, nullptr, st));
+  TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));
+  TT_TRY_SOFT(gwdt_dev(dist, nullptr, costs, flats, g, st), soft);
+  TT_TRY(directions_dev(direction, filled, dist, flats, g, 0, st));
+  if (node) TT_TRY_SOFT(node_order_dev(node, direction, g, 0, st), soft);
+  if (acc) TT_TRY_SOFT(accumulate_dev(acc, direction, weights, g, st), soft);
+  if (hill) TT_TRY(hillshade_dev(hill, dem, az, alt, cs, g, st));
+  return soft;
+}
+
+extern "C" tt_cuda_status tt_cuda_d8_pipeline_dev(
+    float *filled, int32_t *flats, float *dist, ptrdiff_t *node,
+    uint8_t *direction, float *acc, float *hillshade, const float *dem,
+    const uint8_t *bc, const float *weights, float azimuth, float altitude,
+    float cellsize, const ptrdiff_t dims[2], void *stream) {
+  if (!dem || !bc) return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  if (hillshade && (dims[0] < 3 || dims[1] < 3))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    int64_t N = g.cells();
+    Staging sg;
+    sg.add(N * 4);  // costs
+    sg.add(N * 8);  // conncomps
+    if (!filled) sg.add(N * 4);
+    if (!flats) sg.add(N * 4);
+    if (!dist) sg.add(N * 4);
+    if (!direction) sg.add(N);
+    if (!sg.reserve()) return TT_CUDA_ERR_ALLOC;
+    float *costs = (float *)sg.take(N * 4);
+    ptrdiff_t *cc = (ptrdiff_t *)sg.take(N * 8);
+    if (!filled) filled = (float *)sg.take(N * 4);
+    if (!flats) flats = (int32_t *)sg.take(N * 4);
+    if (!dist) dist = (float *)sg.take(N * 4);
+    if (!direction) direction = (uint8_t *)sg.take(N);
+    return pipeline_body(filled, flats, dist, node, direction, acc, hillshade,
+                         dem, bc, weights, azimuth, altitude, cellsize, costs,
+                         cc, g, st);
+  });
+}
+
+// ------------------------------------------------------------------
+// Host-pointer (drop-in) entry points
+// ------------------------------------------------------------------
+namespace {
+
+// Runs `body` with device copies of host arrays.  `ins` are copied H2D,
+// `outs` are copied D2H after the body; an array may appear in both.
+struct HostArg {
+  void *host;
+  size_t bytes;
+  bool in;
+  bool out;
+  void *dev = nullptr;
+};
+
+template <class F>
+tt_cuda_status host_call(const ptrdiff_t dims[2], std::vector<HostArg> args,
+                         F &&body) {
+  if (!dims_ok(dims)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return TT_CUDA_ERR_INVALID_ARGUMENT;
+  }
+  for (auto &a : args)
+    if (!a.host && (a.in || a.out)) {
+      set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+      return TT_CUDA_ERR_INVALID_ARGUMENT;
+    }
+  if (!have_device()) {
+    set_status(TT_CUDA_ERR_NO_DEVICE);
+    return TT_CUDA_ERR_NO_DEVICE;
+  }
+  DeviceLock lock;
+  cudaStream_t st = 0;
+  GridDims g = make_dims(dims);
+  Staging sg;
+  for (auto &a : args) sg.add(a.bytes);
+  if (!sg.reserve()) return finish(TT_CUDA_ERR_ALLOC, st);
+  for (auto &a : args) {
+    a.dev = sg.take(a.bytes);
+    if (a.in) {
+      tt_cuda_status s = h2d(a.dev, a.host, a.bytes, st);
+      if (s != TT_CUDA_SUCCESS) return finish(s, st);
+    }
+  }
+  tt_cuda_status s = body(g, st, args);
+  if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED || s == TT_CUDA_ERR_CYCLE) {
+    for (auto &a : args)
+      if (a.out) {
+        tt_cuda_status c = d2h(a.host, a.dev, a.bytes, st);
+        if (c != TT_CUDA_SUCCESS) return finish(c, st);
+      }
+  }
+  return finish(s, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+void tt_cuda_fillsinks(float *output, float *dem, uint8_t *bc,
+                       ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims, {{output, N * 4, false, true}, {dem, N * 4, true, false}, {bc, N, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return fill_dev((float *)a[0].dev, (const float *)a[1].dev,
+                              (const uint8_t *)a[2].dev, g, st);
+            });
+}
+
+void tt_cuda_fillsinks_hybrid(float *output, ptrdiff_t *queue, float *dem,
+                              uint8_t *bc, ptrdiff_t dims[2]) {
+  (void)queue;
+  tt_cuda_fillsinks(output, dem, bc, dims);
+}
+
+void tt_cuda_reconstruct(float *marker, float *mask, ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims, {{marker, N * 4, true, true}, {mask, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return reconstruct_dev((float *)a[0].dev, (const float *)a[1].dev, g, st);
+            });
+}
+
+int tt_cuda_reconstruct_hybrid(float *marker, ptrdiff_t *queue, float *mask,
+                               ptrdiff_t dims[2]) {
+  (void)queue;
+  tt_cuda_reconstruct(marker, mask, dims);
+  return get_status() == TT_CUDA_ERR_NOT_CONVERGED ? 1 : 0;
+}
+
+ptrdiff_t tt_cuda_identifyflats(int32_t *output, float *dem, ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  int64_t count = 0;
+  host_call(dims, {{output, N * 4, false, true}, {dem, N * 4, true, false}, {&count, 8, false, true}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return identifyflats_dev((int32_t *)a[0].dev, (const float *)a[1].dev, g,
+                                       (unsigned long long *)a[2].dev, st);
+            });
+  return get_status() == TT_CUDA_SUCCESS ? (ptrdiff_t)count : 0;
+}
+
+void tt_cuda_gwdt_computecosts(float *costs, ptrdiff_t *conncomps,
+                               int32_t *flats, float *original_dem,
+                               float *filled_dem, ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{costs, N * 4, false, true}, {conncomps, N * 8, false, true},
+             {flats, N * 4, true, false}, {original_dem, N * 4, true, false},
+             {filled_dem, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return costs_dev((float *)a[0].dev, (ptrdiff_t *)a[1].dev,
+                               (const int32_t *)a[2].dev, (const float *)a[3].dev,
+                               (const float *)a[4].dev, g, st);
+            });
+}
+
+void tt_cuda_gwdt(float *dist, ptrdiff_t *prev, float *costs, int32_t *flats,
+                  ptrdiff_t *heap, ptrdiff_t *back, ptrdiff_t dims[2]) {
+  (void)heap;
+  (void)back;
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{dist, N * 4, false, true}, {prev, prev ? N * 8 : 0, false, prev != nullptr},
+             {costs, N * 4, true, false}, {flats, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return gwdt_dev((float *)a[0].dev, prev ? (ptrdiff_t *)a[1].dev : nullptr,
+                              (const float *)a[2].dev, (const int32_t *)a[3].dev, g, st);
+            });
+}
+
+void tt_cuda_flow_routing_d8_carve(ptrdiff_t *node, uint8_t *direction,
+                                   float *dem, float *dist, int32_t *flats,
+                                   ptrdiff_t dims[2], unsigned int order) {
+  if (order > 1) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{node, N * 8, false, true}, {direction, N, false, true},
+             {dem, N * 4, true, false}, {dist, N * 4, true, false},
+             {flats, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              TT_TRY(directions_dev((uint8_t *)a[1].dev, (const float *)a[2].dev,
+                                    (const float *)a[3].dev, (const int32_t *)a[4].dev,
+                                    g, order, st));
+              return node_order_dev((ptrdiff_t *)a[0].dev, (const uint8_t *)a[1].dev,
+                                    g, order, st);
+            });
+}
+
+void tt_cuda_flow_accumulation(float *acc, ptrdiff_t *source,
+                               uint8_t *direction, float *weights,
+                               ptrdiff_t dims[2]) {
+  (void)source;
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{acc, N * 4, false, true}, {direction, N, true, false},
+             {weights, weights ? N * 4 : 0, weights != nullptr, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return accumulate_dev((float *)a[0].dev, (const uint8_t *)a[1].dev,
+                                    weights ? (const float *)a[2].dev : nullptr, g, st);
+            });
+}
+
+void tt_cuda_flow_accumulation_backward(float *grad_weights, ptrdiff_t *source,
+                                        uint8_t *direction, float *grad_acc,
+                                        ptrdiff_t dims[2]) {
+  (void)source;
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{grad_weights, N * 4, false, true}, {direction, N, true, false},
+             {grad_acc, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return accumulate_backward_dev((float *)a[0].dev, (const uint8_t *)a[1].dev,
+                                             (const float *)a[2].dev, g, st);
+            });
+}
+
+void tt_cuda_gradient_secondorder(float *p0, float *p1, float *dem,
+                                  float cellsize, ptrdiff_t dims[2]) {
+  if (!dims || dims[0] < 3 || dims[1] < 3) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  size_t N = (size_t)(dims[0] * dims[1]);
+  host_call(dims,
+            {{p0, N * 4, false, true}, {p1, N * 4, false, true}, {dem, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return gradient2_dev((float *)a[0].dev, (float *)a[1].dev,
+                                   (const float *)a[2].dev, cellsize, g, st);
+            });
+}
+
+void tt_cuda_hillshade(float *output, float *dx, float *dy, float *dem,
+                       float azimuth, float altitude, float cellsize,
+                       ptrdiff_t dims[2]) {
+  if (!dims || dims[0] < 3 || dims[1] < 3) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  size_t N = (size_t)(dims[0] * dims[1]);
+  host_call(dims,
+            {{output, N * 4, false, true}, {dx, N * 4, false, true},
+             {dy, N * 4, false, true}, {dem, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              TT_TRY(gradient2_dev((float *)a[1].dev, (float *)a[2].dev,
+                                   (const float *)a[3].dev, cellsize, g, st));
+              return hillshade_dev((float *)a[0].dev, (const float *)a[3].dev, azimuth,
+                                   altitude, cellsize, g, st);
+            });
+}
+
+void tt_cuda_hillshade_fused(float *output, float *dem, float azimuth,
+                             float altitude, float cellsize, ptrdiff_t dims[2]) {
+  if (!dims || dims[0] < 3 || dims[1] < 3) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  size_t N = (size_t)(dims[0] * dims[1]);
+  host_call(dims, {{output, N * 4, false, true}, {dem, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return hillshade_dev((float *)a[0].dev, (const float *)a[1].dev, azimuth,
+                                   altitude, cellsize, g, st);
+            });
+}
+
+void tt_cuda_hillshade_backward(float *grad_dem, float *dem, float *grad_output,
+                                float azimuth, float altitude, float cellsize,
+                                ptrdiff_t dims[2]) {
+  if (!dims || dims[0] < 3 || dims[1] < 3) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  size_t N = (size_t)(dims[0] * dims[1]);
+  host_call(dims,
+            {{grad_dem, N * 4, false, true}, {dem, N * 4, true, false},
+             {grad_output, N * 4, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return hillshade_backward_dev((float *)a[0].dev, (const float *)a[1].dev,
+                                            (const float *)a[2].dev, azimuth, altitude,
+                                            cellsize, g, st);
+            });
+}
+
+void tt_cuda_d8_pipeline(float *filled, int32_t *flats, float *dist,
+                         ptrdiff_t *node, uint8_t *direction, float *acc,
+                         float *dem, uint8_t *bc, float *weights,
+                         ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  host_call(dims,
+            {{dem, N * 4, true, false}, {bc, N, true, false},
+             {weights, weights ? N * 4 : 0, weights != nullptr, false},
+             {filled, N * 4, false, filled != nullptr},
+             {flats, N * 4, false, flats != nullptr},
+             {dist, N * 4, false, dist != nullptr},
+             {node, node ? N * 8 : 0, false, node != nullptr},
+             {direction, N, false, direction != nullptr},
+             {acc, acc ? N * 4 : 0, false, acc != nullptr},
+             {nullptr, N * 4, false, false},   // costs
+             {nullptr, N * 8, false, false}},  // conncomps
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return pipeline_body((float *)a[3].dev, (int32_t *)a[4].dev,
+                                   (float *)a[5].dev, node ? (ptrdiff_t *)a[6].dev : nullptr,
+                                   (uint8_t *)a[7].dev, acc ? (float *)a[8].dev : nullptr,
+                                   nullptr, (const float *)a[0].dev,
+                                   (const uint8_t *)a[1].dev,
+                                   weights ? (const float *)a[2].dev : nullptr, 0.f, 0.f,
+                                   1.f, (float *)a[9].dev, (ptrdiff_t *)a[10].dev, g, st);
+            });
+}
+
+}  // extern "C"

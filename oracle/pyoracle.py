@@ -1,0 +1,228 @@
+"""ctypes wrappers of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries share one interface:
+
+* ``Oracle("port")`` loads ``oracle/liboracle.so`` -- the project-written C
+  restatement of libtopotoolbox's D8 path (oracle/tt_oracle.c), buildable on
+  any host with gcc;
+* ``Oracle("ref")`` loads ``oracle/_ref/libtopotoolbox_ref.so`` -- the
+  reference's own sources compiled by ``make -C oracle ref`` where they are
+  available.
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg use this module,
+and only as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libtopotoolbox_ref.so"
+REF_ROOT = Path(os.environ.get("TT_REFERENCE_ROOT", "/root/reference"))
+
+P = C.c_void_p
+PD = C.POINTER(C.c_int64)
+F = C.c_float
+D = C.c_double
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    return PORT_LIB
+
+
+def build_ref() -> Path | None:
+    if not (REF_ROOT / "src" / "fillsinks.c").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+    return REF_LIB
+
+
+def _f32(a):
+    return np.asfortranarray(a, dtype=np.float32)
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _dims(shape):
+    arr = (C.c_int64 * 2)(int(shape[0]), int(shape[1]))
+    return C.cast(arr, PD), arr
+
+
+class Oracle:
+    """CPU implementation of the D8 path: kind "port" or "ref"."""
+
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        path = PORT_LIB if kind == "port" else REF_LIB
+        if not path.exists():
+            if kind == "port":
+                build_port()
+            else:
+                build_ref()
+        if not path.exists():
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(str(path))
+        pre = "orc_" if kind == "port" else ""
+        self._pre = pre
+        sig = {
+            "fillsinks": (None, [P, P, P, PD]),
+            "fillsinks_hybrid": (C.c_int if kind == "port" else None, [P, P, P, P, PD]),
+            "identifyflats": (C.c_int64, [P, P, PD]),
+            "gwdt_computecosts": (None, [P, P, P, P, P, PD]),
+            "gwdt": (None, [P, P, P, P, P, P, PD]),
+            "flow_routing_d8_carve": (None, [P, P, P, P, P, PD, C.c_uint]),
+            "flow_accumulation": (None, [P, P, P, P, PD]),
+            "hillshade_fused": (None, [P, P, F, F, F, PD]),
+            "hillshade": (None, [P, P, P, P, F, F, F, PD]),
+        }
+        if kind == "port":
+            sig.update({
+                "flow_accumulation_f64": (None, [P, P, P, P, PD]),
+                "flow_accumulation_backward_f64": (None, [P, P, P, P, PD]),
+                "hillshade_f64": (None, [P, P, D, D, D, PD]),
+                "hillshade_backward_f64": (None, [P, P, P, D, D, D, PD]),
+            })
+        self.fn = {}
+        for name, (res, args) in sig.items():
+            f = getattr(self.lib, pre + name)
+            f.restype = res
+            f.argtypes = args
+            self.fn[name] = f
+
+    # The reference's fillsinks negates `dem` in place while it runs; every
+    # wrapper passes a private copy so callers' arrays are never touched.
+    def fillsinks(self, dem, bc):
+        dem = np.array(dem, dtype=np.float32, order="F", copy=True)
+        bc = np.asfortranarray(bc, dtype=np.uint8)
+        out = np.empty_like(dem, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["fillsinks"](_ptr(out), _ptr(dem), _ptr(bc), dp)
+        return out
+
+    def fillsinks_hybrid(self, dem, bc):
+        dem = np.array(dem, dtype=np.float32, order="F", copy=True)
+        bc = np.asfortranarray(bc, dtype=np.uint8)
+        out = np.empty_like(dem, order="F")
+        q = np.empty(dem.shape, dtype=np.int64, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["fillsinks_hybrid"](_ptr(out), _ptr(q), _ptr(dem), _ptr(bc), dp)
+        return out
+
+    def identifyflats(self, dem):
+        dem = _f32(dem)
+        out = np.empty(dem.shape, dtype=np.int32, order="F")
+        dp, k = _dims(dem.shape)
+        n = self.fn["identifyflats"](_ptr(out), _ptr(dem), dp)
+        return out, int(n)
+
+    def gwdt_computecosts(self, flats, dem, filled):
+        flats = np.asfortranarray(flats, dtype=np.int32)
+        dem, filled = _f32(dem), _f32(filled)
+        costs = np.empty(dem.shape, dtype=np.float32, order="F")
+        cc = np.empty(dem.shape, dtype=np.int64, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["gwdt_computecosts"](_ptr(costs), _ptr(cc), _ptr(flats), _ptr(dem),
+                                     _ptr(filled), dp)
+        return costs, cc
+
+    def gwdt(self, costs, flats, want_prev=True):
+        costs = _f32(costs)
+        flats = np.asfortranarray(flats, dtype=np.int32)
+        dist = np.empty(costs.shape, dtype=np.float32, order="F")
+        prev = np.empty(costs.shape, dtype=np.int64, order="F") if want_prev else None
+        heap = np.empty(costs.shape, dtype=np.int64, order="F")
+        back = np.empty(costs.shape, dtype=np.int64, order="F")
+        dp, k = _dims(costs.shape)
+        self.fn["gwdt"](_ptr(dist), _ptr(prev), _ptr(costs), _ptr(flats), _ptr(heap),
+                        _ptr(back), dp)
+        return (dist, prev) if want_prev else dist
+
+    def flow_routing_d8_carve(self, dem, dist, flats, order=0):
+        dem, dist = _f32(dem), _f32(dist)
+        flats = np.asfortranarray(flats, dtype=np.int32)
+        node = np.empty(dem.shape, dtype=np.int64, order="F")
+        direction = np.empty(dem.shape, dtype=np.uint8, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["flow_routing_d8_carve"](_ptr(node), _ptr(direction), _ptr(dem), _ptr(dist),
+                                         _ptr(flats), dp, int(order))
+        return node, direction
+
+    def flow_accumulation(self, node, direction, weights=None):
+        node = np.asfortranarray(node, dtype=np.int64)
+        direction = np.asfortranarray(direction, dtype=np.uint8)
+        w = _f32(weights) if weights is not None else None
+        acc = np.empty(direction.shape, dtype=np.float32, order="F")
+        dp, k = _dims(direction.shape)
+        self.fn["flow_accumulation"](_ptr(acc), _ptr(node), _ptr(direction), _ptr(w), dp)
+        return acc
+
+    def flow_accumulation_f64(self, node, direction, weights=None):
+        node = np.asfortranarray(node, dtype=np.int64)
+        direction = np.asfortranarray(direction, dtype=np.uint8)
+        w = _f32(weights) if weights is not None else None
+        acc = np.empty(direction.shape, dtype=np.float64, order="F")
+        dp, k = _dims(direction.shape)
+        self.fn["flow_accumulation_f64"](_ptr(acc), _ptr(node), _ptr(direction), _ptr(w), dp)
+        return acc
+
+    def flow_accumulation_backward_f64(self, node, direction, grad_acc):
+        node = np.asfortranarray(node, dtype=np.int64)
+        direction = np.asfortranarray(direction, dtype=np.uint8)
+        g = np.asfortranarray(grad_acc, dtype=np.float64)
+        out = np.empty(direction.shape, dtype=np.float64, order="F")
+        dp, k = _dims(direction.shape)
+        self.fn["flow_accumulation_backward_f64"](_ptr(out), _ptr(node), _ptr(direction),
+                                                  _ptr(g), dp)
+        return out
+
+    def hillshade_fused(self, dem, az, alt, cs):
+        dem = _f32(dem)
+        out = np.empty_like(dem, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["hillshade_fused"](_ptr(out), _ptr(dem), float(az), float(alt), float(cs), dp)
+        return out
+
+    def hillshade(self, dem, az, alt, cs):
+        dem = _f32(dem)
+        out, dx, dy = (np.empty_like(dem, order="F") for _ in range(3))
+        dp, k = _dims(dem.shape)
+        self.fn["hillshade"](_ptr(out), _ptr(dx), _ptr(dy), _ptr(dem), float(az), float(alt),
+                             float(cs), dp)
+        return out, dx, dy
+
+    def hillshade_f64(self, dem, az, alt, cs):
+        dem = np.asfortranarray(dem, dtype=np.float64)
+        out = np.empty(dem.shape, dtype=np.float64, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["hillshade_f64"](_ptr(out), _ptr(dem), float(az), float(alt), float(cs), dp)
+        return out
+
+    def hillshade_backward_f64(self, dem, grad_out, az, alt, cs):
+        dem = np.asfortranarray(dem, dtype=np.float64)
+        g = np.asfortranarray(grad_out, dtype=np.float64)
+        out = np.empty(dem.shape, dtype=np.float64, order="F")
+        dp, k = _dims(dem.shape)
+        self.fn["hillshade_backward_f64"](_ptr(out), _ptr(dem), _ptr(g), float(az), float(alt),
+                                          float(cs), dp)
+        return out
+
+    def pipeline(self, dem, bc, weights=None, hybrid=True):
+        """fill -> flats -> costs -> gwdt -> carve -> accumulation, the call
+        sequence of test/random_dem.cpp:682-724 (with flow_accumulation)."""
+        filled = self.fillsinks_hybrid(dem, bc) if hybrid else self.fillsinks(dem, bc)
+        flats, _ = self.identifyflats(filled)
+        costs, cc = self.gwdt_computecosts(flats, dem, filled)
+        dist = self.gwdt(costs, flats, want_prev=False)
+        node, direction = self.flow_routing_d8_carve(filled, dist, flats, 0)
+        acc = self.flow_accumulation(node, direction, weights)
+        return dict(filled=filled, flats=flats, costs=costs, conncomps=cc, dist=dist,
+                    node=node, direction=direction, acc=acc)

@@ -1,0 +1,84 @@
+/*
+ * tt_oracle.h -- CPU oracle for the D8 flow pipeline (TEST INFRASTRUCTURE).
+ *
+ * This library is the checker, never the product: only tests/, the smoke
+ * check in __graft_entry__.py and the CPU-baseline leg of bench.py load it.
+ * It restates, in plain C, the reference algorithms of libtopotoolbox for
+ * the hot path (fillsinks, identifyflats, gwdt_computecosts, gwdt,
+ * flow_routing_d8_carve, flow_accumulation, hillshade) plus FP64 versions of
+ * accumulation and hillshade and FP64 adjoints of both.  Each function names
+ * the reference file:line it follows.  Arrays are column-major with
+ * dims = {nrows, ncols} (fastest dimension first), exactly as in the
+ * reference header include/topotoolbox.h.
+ */
+#ifndef TT_ORACLE_H
+#define TT_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* src/fillsinks.c:23-48 + src/reconstruct.c:68-114,134-205,270-278 */
+void orc_fillsinks(float *output, const float *dem, const uint8_t *bc,
+                   const ptrdiff_t dims[2]);
+/* src/fillsinks.c:51-77 + src/reconstruct.c:13-45,207-251,291-312.
+ * Returns 1 when the queue overflowed on the last allowed scan. */
+int orc_fillsinks_hybrid(float *output, ptrdiff_t *queue, const float *dem,
+                         const uint8_t *bc, const ptrdiff_t dims[2]);
+/* src/identifyflats.c:33-121 */
+ptrdiff_t orc_identifyflats(int32_t *output, const float *dem,
+                            const ptrdiff_t dims[2]);
+/* src/gwdt.c:87-278 */
+void orc_gwdt_computecosts(float *costs, ptrdiff_t *conncomps,
+                           const int32_t *flats, const float *original_dem,
+                           const float *filled_dem, const ptrdiff_t dims[2]);
+/* src/gwdt.c:290-351 + src/helpers/priority_queue.c:52-133 */
+void orc_gwdt(float *dist, ptrdiff_t *prev, const float *costs,
+              const int32_t *flats, ptrdiff_t *heap, ptrdiff_t *back,
+              const ptrdiff_t dims[2]);
+/* src/flow_routing.c:15-76,135-256 */
+void orc_flow_routing_d8_carve(ptrdiff_t *node, uint8_t *direction,
+                               const float *dem, const float *dist,
+                               const int32_t *flats, const ptrdiff_t dims[2],
+                               unsigned int order);
+/* src/flow_accumulation.c:32-80 (float32, node order) */
+void orc_flow_accumulation(float *acc, const ptrdiff_t *source,
+                           const uint8_t *direction, const float *weights,
+                           const ptrdiff_t dims[2]);
+/* FP64 restatement of src/flow_accumulation.c:32-80 */
+void orc_flow_accumulation_f64(double *acc, const ptrdiff_t *source,
+                               const uint8_t *direction, const float *weights,
+                               const ptrdiff_t dims[2]);
+/* FP64 adjoint: grad_w[u] = sum of grad_acc over the flow path from u to its
+ * outlet (u included).  No counterpart in the reference. */
+void orc_flow_accumulation_backward_f64(double *grad_w, const ptrdiff_t *source,
+                                        const uint8_t *direction,
+                                        const double *grad_acc,
+                                        const ptrdiff_t dims[2]);
+/* src/hillshade.c:11-20,102-213 (float32) */
+void orc_hillshade_fused(float *output, const float *dem, float azimuth,
+                         float altitude, float cellsize,
+                         const ptrdiff_t dims[2]);
+/* src/hillshade.c:23-97 (float32, materialised gradients) */
+void orc_hillshade(float *output, float *dx, float *dy, const float *dem,
+                   float azimuth, float altitude, float cellsize,
+                   const ptrdiff_t dims[2]);
+/* FP64 restatement of src/hillshade.c:11-20,102-213; sun vector in double */
+void orc_hillshade_f64(double *output, const double *dem, double azimuth,
+                       double altitude, double cellsize,
+                       const ptrdiff_t dims[2]);
+/* FP64 adjoint of orc_hillshade_f64 with respect to dem: grad_dem =
+ * J^T grad_out.  Cells whose hillshade is NaN contribute nothing.  No
+ * counterpart in the reference. */
+void orc_hillshade_backward_f64(double *grad_dem, const double *dem,
+                                const double *grad_out, double azimuth,
+                                double altitude, double cellsize,
+                                const ptrdiff_t dims[2]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

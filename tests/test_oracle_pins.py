@@ -1,0 +1,124 @@
+"""Pin the CPU oracle (oracle/tt_oracle.c) to the reference.
+
+* Against the reference itself, compiled from its own sources by
+  `make -C oracle ref` (skipped where the sources are absent): every output
+  of the D8 path is compared bit for bit, including the node order, the
+  conncomps labels and the gwdt back-links.
+* Against the committed golden fixtures in tests/golden/ (produced by the
+  compiled reference with tests/golden/make_golden.py), which travel with the
+  repository and pin the oracle on hosts without the reference.
+* Against the reference's own property tests (test/random_dem.cpp:37-425),
+  restated here on the oracle's outputs.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import same_float, topo_positions_ok
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _dems():
+    from libtopotoolbox_gb300 import dems
+
+    out = []
+    for s in range(12):  # random_dem.cpp style: 100 x 200 pcg4d DEMs
+        d = dems.pcg4d_dem((100, 200), s)
+        out.append((f"pcg4d_{s}", d, dems.border_bc(d.shape)))
+    d, bc, _ = dems.plain_512(size=256)
+    out.append(("plain_256", d, bc))
+    d, bc, _ = dems.plain_4096(size=256)
+    out.append(("rounded_256", d, bc))
+    d, bc, _ = dems.plain_16384(size=320)
+    d2, bc2, _ = dems.nan_to_outlets(d, bc)
+    out.append(("nodata_ninf_320", d2, bc2))
+    out.append(("nodata_nan_320", d, bc))
+    for shp in [(1, 1), (2, 3), (3, 3), (17, 5)]:
+        rng = np.random.default_rng(shp[0] * 7 + shp[1])
+        out.append((f"rand_{shp}", np.asfortranarray(rng.uniform(0, 5, shp).astype(np.float32)),
+                    dems.border_bc(shp)))
+    return out
+
+
+DEMS = _dems()
+
+
+@pytest.mark.parametrize("idx", range(len(DEMS)))
+@pytest.mark.parametrize("hybrid", [False, True])
+def test_port_equals_reference(port, ref, idx, hybrid):
+    name, dem, bc = DEMS[idx]
+    rp = port.pipeline(dem, bc, hybrid=hybrid)
+    rr = ref.pipeline(dem, bc, hybrid=hybrid)
+    for k in rp:
+        a, b = rp[k], rr[k]
+        if a.dtype.kind == "f":
+            assert same_float(a, b), (name, k)
+        else:
+            assert np.array_equal(a, b), (name, k)
+    _, pp = port.gwdt(rp["costs"], rp["flats"], want_prev=True)
+    _, pr = ref.gwdt(rr["costs"], rr["flats"], want_prev=True)
+    assert np.array_equal(pp, pr), name
+
+
+@pytest.mark.parametrize("idx", range(len(DEMS)))
+def test_port_hillshade_equals_reference(port, ref, idx):
+    name, dem, bc = DEMS[idx]
+    if min(dem.shape) < 3:
+        pytest.skip("the reference reads out of bounds below 3 x 3")
+    d = np.where(np.isfinite(dem), dem, np.float32(0)).astype(np.float32)
+    for az, alt in [(3.9269908, 1.0471976), (0.3, 0.5)]:
+        assert same_float(port.hillshade_fused(d, az, alt, 30.0), ref.hillshade_fused(d, az, alt, 30.0))
+        for a, b in zip(port.hillshade(d, az, alt, 30.0), ref.hillshade(d, az, alt, 30.0)):
+            assert same_float(a, b)
+
+
+def test_port_order1_equals_reference(port, ref):
+    name, dem, bc = DEMS[0]
+    rp = port.pipeline(dem, bc)
+    for order in (0, 1):
+        a = port.flow_routing_d8_carve(rp["filled"], rp["dist"], rp["flats"], order)
+        b = ref.flow_routing_d8_carve(rp["filled"], rp["dist"], rp["flats"], order)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_golden_fixtures(port):
+    files = sorted(GOLDEN.glob("*.npz"))
+    assert files, "golden fixtures missing"
+    for f in files:
+        z = np.load(f)
+        dem, bc = z["dem"], z["bc"]
+        r = port.pipeline(dem, bc, hybrid=bool(z["hybrid"]))
+        for k in ("filled", "flats", "costs", "conncomps", "dist", "node", "direction", "acc"):
+            if r[k].dtype.kind == "f":
+                assert same_float(r[k], z[k]), (f.name, k)
+            else:
+                assert np.array_equal(r[k], z[k]), (f.name, k)
+        if "hillshade" in z:
+            assert same_float(port.hillshade_fused(np.nan_to_num(dem), float(z["az"]),
+                                                   float(z["alt"]), float(z["cs"])), z["hillshade"])
+
+
+@pytest.mark.parametrize("idx", range(12))
+def test_reference_properties(port, idx):
+    """The hot-path property tests of test/random_dem.cpp on oracle outputs."""
+    name, dem, bc = DEMS[idx]
+    r = port.pipeline(dem, bc)
+    filled, flats, dist, costs = r["filled"], r["flats"], r["dist"], r["costs"]
+    m, n = dem.shape
+    assert np.all(filled >= dem)  # :37-42
+    inner = filled[1:-1, 1:-1]
+    higher = np.zeros(inner.shape, dtype=int)
+    for di in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            if di or dj:
+                higher += filled[1 + di:m - 1 + di, 1 + dj:n - 1 + dj] > inner
+    assert not np.any(higher == 8)  # :48-53
+    assert np.all(dist >= 0)
+    assert np.all(dist[(flats & 4) > 0] == 1.0)  # :266-296
+    other = ((flats & 1) > 0) & ((flats & 4) == 0)
+    assert np.all(dist[other] > 1.0)
+    assert np.all((costs > 0) == ((flats & 1) > 0))  # :203-214
+    assert topo_positions_ok(r["node"], r["direction"])
+    assert np.all(r["acc"] <= dem.size)  # :417-425
