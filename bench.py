@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the D8 flow pipeline on GB300.
+
+One step = the plain pipeline (fillsinks -> identifyflats ->
+gwdt_computecosts -> gwdt -> flow_routing_d8_carve -> flow_accumulation, unit
+weights) plus hillshade on one synthetic DEM, through the library's device
+entry points with the DEM already in HBM.  The default workload is the
+4096 x 4096 fractal with 200 inverted Gaussian pits rounded to 1 m.
+
+Prints one JSON line (rank 0).  `--impl reference` times the CPU
+implementation of the same path (the oracle's C restatement of the
+reference) on the host cores instead.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcells/s fill+D8+acc on 1 GB300 vs CPU; adjoint/fwd time at 1e-5 rel err"
+UNIT = "Gcells/s"
+# Algorithmic bytes per cell: every API input read once, every output written
+# once, scratch excluded (unit weights, prev = NULL).
+BYTES = {
+    "fillsinks": 9, "identifyflats": 8, "gwdt_computecosts": 24, "gwdt": 12,
+    "flow_routing_d8_carve": 21, "flow_accumulation": 13, "hillshade_fused": 8,
+}
+PIPELINE_BYTES = sum(v for k, v in BYTES.items() if k != "hillshade_fused")  # 87
+HS_AZ, HS_ALT = 3.9269908, 1.0471976
+
+WORKLOADS = {
+    "plain_4096_hillshade": ("plain_4096", {}),
+    "plain_16384": ("plain_16384", {}),
+    "plain_512": ("plain_512", {}),
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(name):
+    from libtopotoolbox_gb300 import dems
+
+    gen, kw = WORKLOADS[name]
+    dem, bc, cs = getattr(dems, gen)(**kw)
+    if np.isnan(dem).any():
+        dem, bc, _ = dems.nan_to_outlets(dem, bc)
+    return dem, bc, cs
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic():
+    p = ROOT / "profiles" / "roofline_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
+def cpu_baseline_sample(dem, bc, seconds_target=20.0):
+    """The oracle port on a bounded crop of the workload, one host core."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    orc = pyoracle.Oracle("port")
+    side = min(dem.shape[0], 1024)
+    crop = np.asfortranarray(dem[:side, :side])
+    cb = np.zeros(crop.shape, np.uint8, order="F")
+    cb[0, :] = cb[-1, :] = cb[:, 0] = cb[:, -1] = 1
+    cb |= np.asfortranarray(bc[:side, :side])
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        orc.pipeline(crop, cb, hybrid=True)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_target or reps >= 50:
+            break
+    gcps = crop.size * reps / el / 1e9
+    return {"value": gcps, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{reps} x plain pipeline (hybrid fill) on a {side}x{side} crop of the "
+                      f"workload DEM, oracle C restatement of the reference, 1 thread, "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    orc = pyoracle.Oracle("port")
+    dem, bc, cs = make_workload(args.workload)
+    cores = os.cpu_count() or 1
+    side = min(dem.shape[0], 1024)
+    crops = []
+    for k in range(cores):
+        i0 = (k * 613) % max(1, dem.shape[0] - side + 1)
+        j0 = (k * 389) % max(1, dem.shape[1] - side + 1)
+        c = np.asfortranarray(dem[i0:i0 + side, j0:j0 + side])
+        b = np.zeros(c.shape, np.uint8, order="F")
+        b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 1
+        b |= np.asfortranarray(bc[i0:i0 + side, j0:j0 + side])
+        crops.append((c, b))
+
+    def one(cb):
+        orc.pipeline(cb[0], cb[1], hybrid=True)
+        orc.hillshade_fused(cb[0], HS_AZ, HS_ALT, cs)
+
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        for _ in range(args.warmup):
+            list(ex.map(one, crops))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            list(ex.map(one, crops))
+            times.append(time.perf_counter() - t0)
+    cells = side * side * cores
+    ms = 1e3 * float(np.mean(times))
+    value = cells / (ms * 1e-3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "sample": f"{cores} concurrent {side}x{side} crops"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"per step: plain pipeline + hillshade on {cores} crops of "
+                                   f"{side}x{side}, one per host thread (oracle C restatement; "
+                                   f"the reference sources are not on this host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="plain_4096_hillshade", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from libtopotoolbox_gb300 import api
+    from libtopotoolbox_gb300 import _native as N
+
+    lib = N.lib()
+    dem, bc, cs = make_workload(args.workload)
+    m, n = dem.shape
+    cells = m * n
+    # Device-resident inputs: column-major grid == (ncols, nrows) tensor.
+    d_dem = torch.from_numpy(np.ascontiguousarray(dem.T)).to(dev)
+    d_bc = torch.from_numpy(np.ascontiguousarray(bc.T)).to(dev)
+    o = {
+        "filled": torch.empty((n, m), dtype=torch.float32, device=dev),
+        "flats": torch.empty((n, m), dtype=torch.int32, device=dev),
+        "costs": torch.empty((n, m), dtype=torch.float32, device=dev),
+        "conncomps": torch.empty((n, m), dtype=torch.int64, device=dev),
+        "dist": torch.empty((n, m), dtype=torch.float32, device=dev),
+        "node": torch.empty((n, m), dtype=torch.int64, device=dev),
+        "direction": torch.empty((n, m), dtype=torch.uint8, device=dev),
+        "acc": torch.empty((n, m), dtype=torch.float32, device=dev),
+        "hillshade": torch.empty((n, m), dtype=torch.float32, device=dev),
+    }
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2
+    stream = torch.cuda.current_stream(dev)
+    sp = N.C.c_void_p(stream.cuda_stream)
+    dp, keep = N.dims_arg((m, n))
+    P = lambda t: N.C.c_void_p(t.data_ptr())  # noqa: E731
+
+    stages = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
+              "flow_routing_d8_carve", "flow_accumulation", "hillshade_fused"]
+
+    def step(events=None):
+        calls = [
+            lambda: lib.tt_cuda_fillsinks_dev(P(o["filled"]), P(d_dem), P(d_bc), dp, sp),
+            lambda: lib.tt_cuda_identifyflats_dev(P(o["flats"]), P(o["filled"]), dp, None, sp),
+            lambda: lib.tt_cuda_gwdt_computecosts_dev(P(o["costs"]), P(o["conncomps"]),
+                                                      P(o["flats"]), P(d_dem), P(o["filled"]),
+                                                      dp, sp),
+            lambda: lib.tt_cuda_gwdt_dev(P(o["dist"]), None, P(o["costs"]), P(o["flats"]), dp, sp),
+            lambda: lib.tt_cuda_flow_routing_d8_carve_dev(P(o["node"]), P(o["direction"]),
+                                                          P(o["filled"]), P(o["dist"]),
+                                                          P(o["flats"]), dp, 0, sp),
+            lambda: lib.tt_cuda_flow_accumulation_dev(P(o["acc"]), P(o["direction"]), None, dp, sp),
+            lambda: lib.tt_cuda_hillshade_fused_dev(P(o["hillshade"]), P(d_dem), HS_AZ, HS_ALT,
+                                                    cs, dp, sp),
+        ]
+        for k, c in enumerate(calls):
+            if events is not None:
+                events[k].record(stream)
+            N.check(c(), stages[k])
+        if events is not None:
+            events[-1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    stage_ms = {s: [] for s in stages}
+    step_ms = []
+    lib.tt_cuda_launch_count(1)
+    with ClockSampler(local) as clk:
+        barrier()
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # L2 flush outside the timed events
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)]
+            step(ev)
+            torch.cuda.synchronize()
+            for k, s in enumerate(stages):
+                stage_ms[s].append(ev[k].elapsed_time(ev[k + 1]))
+            step_ms.append(ev[0].elapsed_time(ev[-1]))
+        barrier()
+    launches = int(lib.tt_cuda_launch_count(1)) / args.steps
+    ms = float(np.mean(step_ms))
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * world / (ms * 1e-3) / 1e9
+
+    # End-to-end through the host-pointer C ABI: pinned host buffers, copies
+    # inside the timed region.
+    def pinned(shape, dtype):
+        t = torch.empty(shape, dtype=dtype, pin_memory=True)
+        return t.numpy()
+
+    h_dem = pinned((n, m), torch.float32)
+    h_dem[:] = dem.T
+    h_bc = pinned((n, m), torch.uint8)
+    h_bc[:] = bc.T
+    h_out = {k: pinned((n, m), t.dtype) for k, t in o.items()
+             if k in ("filled", "flats", "dist", "node", "direction", "acc", "hillshade")}
+    hp = lambda a: N.C.c_void_p(a.ctypes.data)  # noqa: E731
+
+    def e2e_step():
+        lib.tt_cuda_d8_pipeline(hp(h_out["filled"]), hp(h_out["flats"]), hp(h_out["dist"]),
+                                hp(h_out["node"]), hp(h_out["direction"]), hp(h_out["acc"]),
+                                hp(h_dem), hp(h_bc), None, dp)
+        N.check(N.last_status(), "d8_pipeline")
+        lib.tt_cuda_hillshade_fused(hp(h_out["hillshade"]), hp(h_dem), HS_AZ, HS_ALT, cs, dp)
+        N.check(N.last_status(), "hillshade_fused")
+
+    e2e_step()
+    e2e_ms = []
+    for _ in range(max(2, min(args.steps, 5))):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    h2d = cells * (4 + 1) + cells * 4  # dem + bc for the pipeline, dem for hillshade
+    d2h = cells * (4 + 4 + 4 + 8 + 1 + 4 + 4)
+    e2e_val = cells * world / (float(np.mean(e2e_ms)) * 1e-3) / 1e9
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    hbm, peak_kind = peaks()
+    # Dominant stage by time.
+    mean_stage = {s: float(np.mean(v)) for s, v in stage_ms.items()}
+    dom = max(mean_stage, key=mean_stage.get)
+    dom_bytes = BYTES[dom] * cells
+    achieved = dom_bytes / (mean_stage[dom] * 1e-3) / 1e9
+    traffic = load_traffic().get(f"{args.workload}:{dom}")
+    pipe_ms = sum(mean_stage[s] for s in stages if s != "hillshade_fused")
+    pipe_gbs = PIPELINE_BYTES * cells / (pipe_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "dem": f"{m}x{n} float32 column-major",
+                   "weights": "unit", "hillshade": "azimuth 315, altitude 60",
+                   "l2": "flushed (512 MiB write) between timed steps",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_cell": BYTES[dom]},
+        "pipeline_roofline": {"bytes_per_cell": PIPELINE_BYTES, "ms": pipe_ms,
+                              "achieved_gbs": pipe_gbs, "frac": pipe_gbs / hbm},
+        "stages_ms": mean_stage,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": float(np.mean(e2e_ms)),
+                "path": "tt_cuda_d8_pipeline + tt_cuda_hillshade_fused (host pointers)"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -541,6 +541,9 @@ __global__ void __launch_bounds__(32) forest_down_kernel(DownArgs a) {
       cur ^= 1;
       __syncwarp();
     }
+    int cyc = 0;
+    for (int jj = 0; jj < kTile; jj++) cyc |= t.nx[cur][jj * kTile + ii] >= 0;
+    if (cyc) atomicOr(a.err, ERR_CYCLE);  // a path longer than the tile: a cycle
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       if (i >= a.m || j >= a.n) continue;
@@ -859,6 +862,7 @@ tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
   TT_CHECK(cudaGetLastError());
   TT_CHECK(cudaMemcpyAsync(hcnt, counters + 4, 4, cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
+  if (*hcnt & ERR_CYCLE) return TT_CUDA_ERR_CYCLE;
   if (*hcnt & ERR_BADDIR) return TT_CUDA_ERR_INVALID_ARGUMENT;
   return TT_CUDA_SUCCESS;
 }

@@ -23,6 +23,7 @@
 // until four consecutive sweeps change nothing.  Changed cells are written
 // back; a changed edge or corner enqueues the neighbouring tile for the next
 // round.  The host launches rounds until the queue is empty.
+#include <algorithm>
 #include <cmath>
 
 #include "tt_internal.cuh"
@@ -363,7 +364,12 @@ tt_cuda_status run_rounds(float *state, const float *aux, const int32_t *flats,
   int64_t round = 1;  // the initial list is round 1, stored in slot 1
   const int batch = 8;
   for (;;) {
-    for (int b = 0; b < batch; b++) {
+    const int nb = (int)std::min<int64_t>(batch, cap - round + 1);
+    if (nb <= 0) {
+      set_last_rounds(round - 1);
+      return TT_CUDA_ERR_NOT_CONVERGED;
+    }
+    for (int b = 0; b < nb; b++) {
       int in = (int)(round & 1), out = (int)((round + 1) & 1);
       TT_CHECK(cudaMemsetAsync(counts + out, 0, sizeof(int), st));
       RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, lists[in],
@@ -376,10 +382,6 @@ tt_cuda_status run_rounds(float *state, const float *aux, const int32_t *flats,
                              cudaMemcpyDeviceToHost, st));
     TT_CHECK(cudaStreamSynchronize(st));
     if (*hcount == 0) break;
-    if (round > cap) {
-      set_last_rounds(round - 1);
-      return TT_CUDA_ERR_NOT_CONVERGED;
-    }
   }
   set_last_rounds(round - 1);
   return TT_CUDA_SUCCESS;

@@ -197,13 +197,100 @@ __device__ __forceinline__ float shade(float dx, float dy, float sx, float sy,
   return (-dx * inv) * sx + (-dy * inv) * sy + inv * sz;
 }
 
+// ------------------------------------------------------------------
+// Float-float (unevaluated sum hi + lo) arithmetic for the shading.  The
+// cancellation in -dx*sx - dy*sy + sz would otherwise cost up to ~1e-5 of
+// relative accuracy where the shade is near zero on steep terrain; carrying
+// ~44 bits keeps the result within a few float32 ulps of the FP64 formula.
+// Error-free transformations: TwoSum (Knuth) and TwoProduct via FMA.
+// ------------------------------------------------------------------
+struct F2 {
+  float hi, lo;
+};
+
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ F2 two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ F2 f2_norm(float hi, float lo) {
+  float s = __fadd_rn(hi, lo);
+  return {s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  F2 s = two_sum(a.hi, b.hi);
+  return f2_norm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  F2 p = two_prod(a.hi, b.hi);
+  float t = __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
+  return f2_norm(p.hi, __fadd_rn(p.lo, t));
+}
+__device__ __forceinline__ F2 f2_mulf(F2 a, float b) {
+  F2 p = two_prod(a.hi, b);
+  return f2_norm(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+// a / b for float b.
+__device__ __forceinline__ F2 f2_divf(F2 a, float b) {
+  float q = __fdiv_rn(a.hi, b);
+  float r = __fadd_rn(__fmaf_rn(-q, b, a.hi), a.lo);
+  return f2_norm(q, __fdiv_rn(r, b));
+}
+__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
+  float q = __fdiv_rn(a.hi, b.hi);
+  F2 qb = f2_mulf(b, q);
+  F2 r = f2_add(a, F2{-qb.hi, -qb.lo});
+  return f2_norm(q, __fdiv_rn(r.hi, b.hi));
+}
+__device__ __forceinline__ F2 f2_sqrt(F2 a) {
+  float s = __fsqrt_rn(a.hi);
+  F2 ss = two_prod(s, s);
+  float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, ss.hi), ss.lo), a.lo);
+  return f2_norm(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
+}
+
+// Exact stencil sums: the one-sided [-3 4 -1] / [1 -4 3] and central
+// [-1 0 1] combinations of float32 samples, as float-float.
+__device__ __forceinline__ F2 axis_diff_f2(float zm2, float zm1, float z0,
+                                           float zp1, float zp2, int64_t k,
+                                           int64_t len) {
+  if (k == 0) {
+    F2 t = f2_add(two_prod(4.0f, zp1), two_prod(-3.0f, z0));
+    return f2_add(t, F2{-zp2, 0.0f});
+  }
+  if (k == len - 1) {
+    F2 t = f2_add(two_prod(-4.0f, zm1), two_prod(3.0f, z0));
+    return f2_add(t, F2{zm2, 0.0f});
+  }
+  return two_sum(zp1, -zm1);
+}
+
+struct Sun2 {
+  float sxh, sxl, syh, syl, szh, szl;
+};
+
+// H = (-dx*sx - dy*sy + sz) / sqrt(dx^2 + dy^2 + 1), in float-float.
+__device__ __forceinline__ float shade_f2(F2 dx, F2 dy, const Sun2 &s) {
+  F2 num = f2_add(f2_add(f2_mul(dx, F2{-s.sxh, -s.sxl}), f2_mul(dy, F2{-s.syh, -s.syl})),
+                  F2{s.szh, s.szl});
+  F2 q = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), F2{1.0f, 0.0f});
+  F2 h = f2_div(num, f2_sqrt(q));
+  return __fadd_rn(h.hi, h.lo);
+}
+
 constexpr int kHS = kTile + 4;  // 2-pixel halo for one-sided borders
 
 template <int MODE>  // 0: hillshade, 1: gradients, 2: hillshade backward
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
                  const float *__restrict__ dem, const float *__restrict__ gout,
-                 int64_t m, int64_t n, float twoh, float sx, float sy, float sz) {
+                 int64_t m, int64_t n, float twoh, float sx, float sy, float sz,
+                 Sun2 s2) {
   __shared__ float z[kHS][kHS + 1];
   __shared__ float hx[MODE == 2 ? kHS : 1][kHS + 1];
   __shared__ float hy[MODE == 2 ? kHS : 1][kHS + 1];
@@ -266,7 +353,15 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
       float dy = axis_grad(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
                            z[cc + 2][r], j, n, twoh);
       if (MODE == 0) {
-        out0[p] = shade(dx, dy, sx, sy, sz);
+        float h = shade(dx, dy, sx, sy, sz);
+        if (isfinite(dx) && isfinite(dy) && isfinite(h)) {
+          F2 ex = f2_divf(axis_diff_f2(z[cc][r - 2], z[cc][r - 1], z[cc][r], z[cc][r + 1],
+                                       z[cc][r + 2], i, m), twoh);
+          F2 ey = f2_divf(axis_diff_f2(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
+                                       z[cc + 2][r], j, n), twoh);
+          h = shade_f2(ex, ey, s2);
+        }
+        out0[p] = h;
       } else {
         out0[p] = dx;
         out1[p] = dy;
@@ -347,7 +442,7 @@ tt_cuda_status gradient2_dev(float *p0, float *p1, const float *dem,
                              float cellsize, const GridDims &g,
                              cudaStream_t st) {
   TT_LAUNCH(hillshade_kernel<1>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            p0, p1, dem, nullptr, g.m, g.n, 2 * cellsize, 0.f, 0.f, 0.f);
+            p0, p1, dem, nullptr, g.m, g.n, 2 * cellsize, 0.f, 0.f, 0.f, Sun2{});
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
@@ -357,8 +452,14 @@ tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
                              cudaStream_t st) {
   float sx, sy, sz;
   sun_vector(azimuth, altitude, &sx, &sy, &sz);
+  double zen = 1.57079632679489661923132169163975 - (double)altitude;
+  double dsx = std::sin(zen) * std::cos((double)azimuth);
+  double dsy = std::sin(zen) * std::sin((double)azimuth);
+  double dsz = std::cos(zen);
+  Sun2 s2{sx, (float)(dsx - (double)sx), sy, (float)(dsy - (double)sy),
+          sz, (float)(dsz - (double)sz)};
   TT_LAUNCH(hillshade_kernel<0>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz);
+            out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz, s2);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
@@ -370,7 +471,7 @@ tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,
   float sx, sy, sz;
   sun_vector(azimuth, altitude, &sx, &sy, &sz);
   TT_LAUNCH(hillshade_kernel<2>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            grad_dem, nullptr, dem, grad_out, g.m, g.n, 2 * cellsize, sx, sy, sz);
+            grad_dem, nullptr, dem, grad_out, g.m, g.n, 2 * cellsize, sx, sy, sz, Sun2{});
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
