@@ -288,9 +288,12 @@ def main():
             if events is not None:
                 events[k].record(stream)
             N.check(c(), stages[k])
+            if stages[k] in ("fillsinks", "gwdt"):
+                rounds[stages[k]] = int(lib.tt_cuda_last_rounds())
         if events is not None:
             events[-1].record(stream)
 
+    rounds = {}
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -386,6 +389,7 @@ def main():
         "pipeline_roofline": {"bytes_per_cell": PIPELINE_BYTES, "ms": pipe_ms,
                               "achieved_gbs": pipe_gbs, "frac": pipe_gbs / hbm},
         "stages_ms": mean_stage,
+        "device_rounds": rounds,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": float(np.mean(e2e_ms)),
                 "path": "tt_cuda_d8_pipeline + tt_cuda_hillshade_fused (host pointers)"},

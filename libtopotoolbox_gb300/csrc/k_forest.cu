@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kUpWarps * 32) forest_up_kernel(UpArgs a) {
       }
     }
     __syncwarp();
-    if (bad && lane == 0) atomicOr(a.err, ERR_BADDIR);
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(a.err, ERR_BADDIR);
     __syncwarp();
 
     // Last-arriver walks.

@@ -88,6 +88,7 @@ class Oracle:
             sig.update({
                 "flow_accumulation_f64": (None, [P, P, P, P, PD]),
                 "flow_accumulation_backward_f64": (None, [P, P, P, P, PD]),
+                "flow_accumulation_f64w": (None, [P, P, P, P, PD]),
                 "hillshade_f64": (None, [P, P, D, D, D, PD]),
                 "hillshade_backward_f64": (None, [P, P, P, D, D, D, PD]),
             })
@@ -172,6 +173,15 @@ class Oracle:
         acc = np.empty(direction.shape, dtype=np.float64, order="F")
         dp, k = _dims(direction.shape)
         self.fn["flow_accumulation_f64"](_ptr(acc), _ptr(node), _ptr(direction), _ptr(w), dp)
+        return acc
+
+    def flow_accumulation_f64w(self, node, direction, weights64):
+        node = np.asfortranarray(node, dtype=np.int64)
+        direction = np.asfortranarray(direction, dtype=np.uint8)
+        w = np.asfortranarray(weights64, dtype=np.float64)
+        acc = np.empty(direction.shape, dtype=np.float64, order="F")
+        dp, k = _dims(direction.shape)
+        self.fn["flow_accumulation_f64w"](_ptr(acc), _ptr(node), _ptr(direction), _ptr(w), dp)
         return acc
 
     def flow_accumulation_backward_f64(self, node, direction, grad_acc):

@@ -493,6 +493,21 @@ void orc_flow_accumulation_f64(double *acc, const ptrdiff_t *source,
   }
 }
 
+void orc_flow_accumulation_f64w(double *acc, const ptrdiff_t *source,
+                                const uint8_t *direction, const double *weights,
+                                const ptrdiff_t dims[2]) {
+  const ptrdiff_t m = dims[0], n = m * dims[1];
+  for (ptrdiff_t p = 0; p < n; p++) acc[p] = weights[p];
+  for (ptrdiff_t k = 0; k < n; k++) {
+    ptrdiff_t u = source[k];
+    uint8_t d = direction[u];
+    if (d == 0) continue;
+    int r = bit_index(d);
+    ptrdiff_t v = (u / m + ACC_DJ[r]) * m + (u % m + ACC_DI[r]);
+    acc[v] += acc[u];
+  }
+}
+
 void orc_flow_accumulation_backward_f64(double *grad_w, const ptrdiff_t *source,
                                         const uint8_t *direction,
                                         const double *grad_acc,

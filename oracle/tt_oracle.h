@@ -52,6 +52,11 @@ void orc_flow_accumulation(float *acc, const ptrdiff_t *source,
 void orc_flow_accumulation_f64(double *acc, const ptrdiff_t *source,
                                const uint8_t *direction, const float *weights,
                                const ptrdiff_t dims[2]);
+/* As orc_flow_accumulation_f64 with float64 weights (for finite
+ * differences of the adjoint). */
+void orc_flow_accumulation_f64w(double *acc, const ptrdiff_t *source,
+                                const uint8_t *direction, const double *weights,
+                                const ptrdiff_t dims[2]);
 /* FP64 adjoint: grad_w[u] = sum of grad_acc over the flow path from u to its
  * outlet (u included).  No counterpart in the reference. */
 void orc_flow_accumulation_backward_f64(double *grad_w, const ptrdiff_t *source,

@@ -63,7 +63,7 @@ def test_flow_accumulation_adjoint(gpu, port):
 
     # central finite differences in FP64 on sampled weights
     def L(wv):
-        a = port.flow_accumulation_f64(node, direction, wv).ravel(order="F")
+        a = port.flow_accumulation_f64w(node, direction, wv).ravel(order="F")
         return float(np.sum((a[sel] - target) ** 2))
 
     h = 1e-3
