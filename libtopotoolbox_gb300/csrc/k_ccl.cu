@@ -15,6 +15,7 @@
 // `conncomps` is the smallest linear index among the component's pixels of
 // maximal depth; the reference picks one of those pixels by its scan-order
 // union-find (src/gwdt.c:141-153), which can differ when depths tie.
+#include <algorithm>
 #include <climits>
 
 #include "tt_internal.cuh"
@@ -56,36 +57,120 @@ __device__ void uf_union(int *L, int a, int b) {
   }
 }
 
-__global__ void ccl_init_kernel(int *__restrict__ L, int *__restrict__ maxkey,
-                                int *__restrict__ argmax,
-                                const int32_t *__restrict__ flats, int64_t N) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    bool f = flats[p] & 1;
-    L[p] = f ? (int)p : -1;
-    if (f) {
-      maxkey[p] = INT_MIN;
-      argmax[p] = INT_MAX;
+// Tile-local labelling: one warp per 32 x 32 tile runs the union-find in
+// shared memory over the tile's internal edges, then writes for every flat
+// pixel the global index of its tile-local root (the smallest index of its
+// tile-local component).  Roots get their max-depth and argmax slots reset.
+constexpr int kCclWarps = 4;
+
+__device__ __forceinline__ int sfind(const int *lab, int x) {
+  int y = ((volatile const int *)lab)[x];
+  while (y != x) {
+    x = y;
+    y = ((volatile const int *)lab)[x];
+  }
+  return x;
+}
+
+__device__ void sunion(int *lab, int a, int b) {
+  for (int it = 0; it < 4096; it++) {
+    a = sfind(lab, a);
+    b = sfind(lab, b);
+    if (a == b) return;
+    if (a < b) {
+      int old = atomicMin(&lab[b], a);
+      if (old == b) return;
+      b = old;
+    } else {
+      int old = atomicMin(&lab[a], b);
+      if (old == a) return;
+      a = old;
     }
   }
 }
 
-__global__ void ccl_merge_kernel(int *__restrict__ L,
-                                 const int32_t *__restrict__ flats, int64_t m,
-                                 int64_t n) {
-  const int64_t N = m * n;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    if (!(flats[p] & 1)) continue;
-    int64_t i = p % m, j = p / m;
-    // Every 8-connected edge once: the four neighbours earlier in scan order.
-    const int di[4] = {-1, -1, 0, 1};
-    const int dj[4] = {0, -1, -1, -1};
+__global__ void __launch_bounds__(kCclWarps * 32)
+ccl_tile_kernel(int *__restrict__ L, int *__restrict__ maxkey,
+                int *__restrict__ argmax, const int32_t *__restrict__ flats,
+                int64_t m, int64_t n, int tm, int tn) {
+  __shared__ int lab[kCclWarps][kTile * kTile];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int *lb = lab[warp];
+  const int T = tm * tn;
+  for (int tile = blockIdx.x * kCclWarps + warp; tile < T; tile += gridDim.x * kCclWarps) {
+    const int ti = tile % tm, tj = tile / tm;
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    const int ii = lane;
+    const int64_t i = i0 + ii;
+    for (int jj = 0; jj < kTile; jj++) {
+      const int64_t j = j0 + jj;
+      bool f = i < m && j < n && (flats[j * m + i] & 1);
+      lb[jj * kTile + ii] = f ? jj * kTile + ii : -1;
+    }
+    __syncwarp();
+    // internal edges to the earlier neighbours (i-1,j), (i-1,j-1), (i,j-1), (i+1,j-1)
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + ii;
+      if (lb[loc] < 0) continue;
+      const int di[4] = {-1, -1, 0, 1};
+      const int dj[4] = {0, -1, -1, -1};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      int64_t ni = i + di[k], nj = j + dj[k];
-      if (ni < 0 || ni >= m || nj < 0) continue;
-      int64_t q = nj * m + ni;
+      for (int k = 0; k < 4; k++) {
+        int qi = ii + di[k], qj = jj + dj[k];
+        if (qi < 0 || qi >= kTile || qj < 0) continue;
+        int q = qj * kTile + qi;
+        if (((volatile int *)lb)[q] >= 0) sunion(lb, loc, q);
+      }
+    }
+    __syncwarp();
+    for (int jj = 0; jj < kTile; jj++) {
+      const int64_t j = j0 + jj;
+      if (i >= m || j >= n) continue;
+      const int loc = jj * kTile + ii;
+      int v = -1;
+      if (lb[loc] >= 0) {
+        int r = sfind(lb, loc);
+        v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
+        if (r == loc) {
+          maxkey[j * m + i] = INT_MIN;
+          argmax[j * m + i] = INT_MAX;
+        }
+      }
+      L[j * m + i] = v;
+    }
+    __syncwarp();
+  }
+}
+
+// Edges that cross tile borders: from the last row, the last column and the
+// first column of every tile to the neighbours (i+1,j), (i,j+1), (i+1,j+1),
+// (i+1,j-1) lying in another tile.
+__global__ void ccl_border_kernel(int *__restrict__ L,
+                                  const int32_t *__restrict__ flats, int64_t m,
+                                  int64_t n, int tm, int tn) {
+  const int T = tm * tn;
+  // 32 last-row + 32 last-column + 32 first-column candidates per tile
+  const int64_t total = (int64_t)T * 96;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    const int tile = (int)(w / 96), k = (int)(w % 96);
+    const int ti = tile % tm, tj = tile / tm;
+    int ii, jj;
+    if (k < 32) { ii = kTile - 1; jj = k; }
+    else if (k < 64) { ii = k - 32; jj = kTile - 1; }
+    else { ii = k - 64; jj = 0; }
+    const int64_t i = (int64_t)ti * kTile + ii, j = (int64_t)tj * kTile + jj;
+    if (i >= m || j >= n) continue;
+    const int64_t p = j * m + i;
+    if (!(flats[p] & 1)) continue;
+    const int di[4] = {1, 0, 1, 1};
+    const int dj[4] = {0, 1, 1, -1};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      int64_t qi = i + di[e], qj = j + dj[e];
+      if (qi >= m || qj < 0 || qj >= n) continue;
+      if (qi / kTile == ti && qj / kTile == tj) continue;  // internal edge
+      int64_t q = qj * m + qi;
       if (flats[q] & 1) uf_union(L, (int)p, (int)q);
     }
   }
@@ -165,8 +250,13 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   int *maxkey = (int *)ws.take((size_t)N * 4);
   int *argmax = (int *)ws.take((size_t)N * 4);
   const int grid = ew_grid(N);
-  TT_LAUNCH(ccl_init_kernel, grid, 256, 0, st, L, maxkey, argmax, flats, N);
-  TT_LAUNCH(ccl_merge_kernel, grid, 256, 0, st, L, flats, g.m, g.n);
+  const int T = g.tiles();
+  const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
+                                           (int64_t)sm_count() * 16);
+  TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, maxkey, argmax, flats,
+            g.m, g.n, g.tm, g.tn);
+  TT_LAUNCH(ccl_border_kernel, ew_grid((int64_t)T * 96), 256, 0, st, L, flats, g.m,
+            g.n, g.tm, g.tn);
   TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, maxkey, flats, orig, filled, N);
   TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, maxkey, argmax, flats, orig, filled, N);
   TT_LAUNCH(costs_kernel, grid, 256, 0, st, costs, conncomps, L, maxkey, argmax,

@@ -21,8 +21,21 @@
 // a one-pixel halo in shared memory and runs directional Gauss-Seidel sweeps
 // (down, up, right, left along the two axes, each lane carrying one line)
 // until four consecutive sweeps change nothing.  Changed cells are written
-// back; a changed edge or corner enqueues the neighbouring tile for the next
-// round.  The host launches rounds until the queue is empty.
+// back with a float atomic minimum; a changed edge or corner pushes the
+// neighbouring tile onto a global work queue.
+//
+// Scheduling: one persistent launch.  Every warp pops a tile from the queue
+// (a ring buffer with monotone head/tail counters), relaxes it and pushes the
+// neighbours it changed, so information crosses tile borders as soon as a
+// tile finishes, with no host round trips.  A per-tile "queued" flag keeps a
+// tile in the queue at most once; it is cleared when the tile is popped,
+// before its halo is read, so later changes re-queue it.  A tile may then be
+// relaxed by two warps at once: both results are valid upper bounds, and
+// because the pointwise minimum of two fixpoints of either update is again a
+// fixpoint, the atomic-minimum write keeps the result exact.  A pending
+// counter (queued + running tiles) detects termination.  Every wait is
+// bounded: a warp that spins too long, or a run that exceeds its visit
+// budget, raises an abort flag and all warps return with an error status.
 #include <algorithm>
 #include <cmath>
 
@@ -44,28 +57,82 @@ struct WarpTile {
   uint32_t dirty[kHalo];   // changed interior rows (bit r-1) of column c
 };
 
+// Queue control block (device memory, zero-initialised except `cap`).
+struct QueueCtl {
+  unsigned long long head;    // next slot to pop
+  unsigned long long tail;    // next slot to push
+  unsigned long long visits;  // tiles relaxed so far
+  int pending;                // queued + running tiles
+  int abort;                  // ABORT_* bits
+};
+
+enum : int { ABORT_SPIN = 1, ABORT_VISITS = 2 };
+
+constexpr long long kSpinLimit = 1LL << 22;  // idle polls before giving up
+
 struct RelaxArgs {
   float *state;
   const float *aux;
   const int32_t *flats;
   int64_t m, n;
   int tm, tn;
-  const int *list_in;
-  const int *count_in;
-  int *list_out;
-  int *count_out;
-  int *mark;
-  int round;
+  QueueCtl *ctl;
+  int *q;       // ring of tile ids, -1 = empty slot
+  int *inq;     // per tile: 1 while queued
+  unsigned long long cap;  // ring capacity (> number of tiles)
+  unsigned long long max_visits;
 };
+
+__device__ __forceinline__ void q_push(const RelaxArgs &a, int t) {
+  if (atomicExch(&a.inq[t], 1) != 0) return;  // already queued
+  atomicAdd(&a.ctl->pending, 1);
+  unsigned long long pos = atomicAdd(&a.ctl->tail, 1ULL);
+  int *slot = &a.q[pos % a.cap];
+  // The slot's previous entry has been claimed by a popper (at most `tiles`
+  // entries are ever queued and cap exceeds that); wait until it took it.
+  for (long long k = 0; atomicCAS(slot, -1, t) != -1; k++) {
+    if (k > kSpinLimit) {
+      atomicOr(&a.ctl->abort, ABORT_SPIN);
+      return;
+    }
+    __nanosleep(64);
+  }
+}
 
 __device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj) {
   if (ti < 0 || tj < 0 || ti >= a.tm || tj >= a.tn) return;
-  int t = tj * a.tm + ti;
-  int next = a.round + 1;
-  if (atomicMax(&a.mark[t], next) < next) {
-    int slot = atomicAdd(a.count_out, 1);
-    a.list_out[slot] = t;
+  q_push(a, tj * a.tm + ti);
+}
+
+// Claims the next queued tile, or returns -1 when the queue is empty.
+__device__ __forceinline__ int q_pop(const RelaxArgs &a) {
+  volatile unsigned long long *vh = &a.ctl->head;
+  volatile unsigned long long *vt = &a.ctl->tail;
+  unsigned long long h = *vh;
+  for (;;) {
+    if (h >= *vt) return -1;
+    unsigned long long old = atomicCAS(&a.ctl->head, h, h + 1);
+    if (old == h) break;
+    h = old;
   }
+  int *slot = &a.q[h % a.cap];
+  int v;
+  for (long long k = 0; (v = atomicExch(slot, -1)) < 0; k++) {
+    if (k > kSpinLimit) {
+      atomicOr(&a.ctl->abort, ABORT_SPIN);
+      return -1;
+    }
+    __nanosleep(32);
+  }
+  return v;
+}
+
+// Float minimum through integer atomics (values are never NaN here).
+__device__ __forceinline__ void atomic_min_float(float *addr, float v) {
+  if (!signbit(v))
+    atomicMin((int *)addr, __float_as_int(v));
+  else
+    atomicMax((unsigned int *)addr, __float_as_uint(v));
 }
 
 template <int KIND>
@@ -140,13 +207,40 @@ __device__ bool sweep_cols(WarpTile &t, int lane, int dir) {
 
 template <int KIND>
 __global__ void __launch_bounds__(kWarps * 32)
-relax_round_kernel(RelaxArgs a) {
+relax_persistent_kernel(RelaxArgs a) {
   __shared__ WarpTile tiles[kWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpTile &t = tiles[warp];
-  const int count = *(volatile const int *)a.count_in;
-  for (int w = blockIdx.x * kWarps + warp; w < count; w += gridDim.x * kWarps) {
-    const int tile = a.list_in[w];
+  long long idle = 0;
+  for (;;) {
+    int tile = -1, stop = 0;
+    if (lane == 0) {
+      if (*(volatile int *)&a.ctl->abort) {
+        stop = 1;
+      } else {
+        tile = q_pop(a);
+        if (tile < 0) {
+          if (*(volatile int *)&a.ctl->pending == 0) {
+            stop = 1;
+          } else if (++idle > kSpinLimit) {
+            atomicOr(&a.ctl->abort, ABORT_SPIN);
+            stop = 1;
+          } else {
+            __nanosleep(idle < 64 ? 100 : 1000);
+          }
+        } else {
+          idle = 0;
+          atomicExch(&a.inq[tile], 0);  // later changes re-queue this tile
+          if (atomicAdd(&a.ctl->visits, 1ULL) >= a.max_visits)
+            atomicOr(&a.ctl->abort, ABORT_VISITS);
+          __threadfence();
+        }
+      }
+    }
+    stop = __shfl_sync(0xffffffffu, stop, 0);
+    if (stop) break;
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile < 0) continue;
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
 
@@ -164,7 +258,7 @@ relax_round_kernel(RelaxArgs a) {
         bool fl = false;
         if (ok) {
           int64_t p = j * a.m + i;
-          sv = a.state[p];
+          sv = __ldcg(&a.state[p]);  // L2: other SMs update it concurrently
           av = a.aux[p];
           if (KIND == GWDT) fl = (a.flats[p] & 1) != 0;
         }
@@ -207,11 +301,13 @@ relax_round_kernel(RelaxArgs a) {
       int64_t j = j0 + c - 1;
       int64_t i = i0 + lane;
       if ((dm >> lane) & 1u) {
-        if (j < a.n && i < a.m) a.state[j * a.m + i] = t.s[c][lane + 1];
+        if (j < a.n && i < a.m) atomic_min_float(&a.state[j * a.m + i], t.s[c][lane + 1]);
       }
       top |= dm & 1u;
       bottom |= (dm >> 31) & 1u;
     }
+    __threadfence();  // publish this lane's writes before any push below
+    __syncwarp();
     if (lane == 0) {
       uint32_t left = t.dirty[1], right = t.dirty[kTile];
       if (top) push_tile(a, ti - 1, tj);
@@ -222,7 +318,9 @@ relax_round_kernel(RelaxArgs a) {
       if ((left >> 31) & 1u) push_tile(a, ti + 1, tj - 1);
       if (right & 1u) push_tile(a, ti - 1, tj + 1);
       if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1);
-      if (quiet < 4) push_tile(a, ti, tj);  // capped: come back next round
+      if (quiet < 4) push_tile(a, ti, tj);  // capped: come back later
+      __threadfence();
+      atomicSub(&a.ctl->pending, 1);
     }
     __syncwarp();
   }
@@ -259,10 +357,25 @@ __global__ void negate_kernel(float *__restrict__ out, const float *__restrict__
     out[p] = -in[p];
 }
 
-__global__ void iota_kernel(int *list, int *mark, int n) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    list[t] = t;
-    mark[t] = 1;
+// Queue every tile (fill starts everywhere).
+__global__ void queue_all_kernel(int *q, int *inq, QueueCtl *ctl, int n,
+                                 unsigned long long cap) {
+  for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+       t < cap; t += (unsigned long long)gridDim.x * blockDim.x) {
+    q[t] = t < (unsigned long long)n ? (int)t : -1;
+    if (t < (unsigned long long)n) inq[t] = 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->tail = n;
+    ctl->pending = n;
+  }
+}
+
+__global__ void queue_clear_kernel(int *q, int *inq, int n, unsigned long long cap) {
+  for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+       t < cap; t += (unsigned long long)gridDim.x * blockDim.x) {
+    q[t] = -1;
+    if (t < (unsigned long long)n) inq[t] = 0;
   }
 }
 
@@ -270,8 +383,7 @@ __global__ void iota_kernel(int *list, int *mark, int n) {
 // whose pixels or halo contain a presill.
 __global__ void gwdt_init_kernel(float *__restrict__ dist,
                                  const int32_t *__restrict__ flats, int64_t m,
-                                 int64_t n, int tm, int tn, int *list, int *count,
-                                 int *mark) {
+                                 int64_t n, RelaxArgs qa) {
   const int64_t N = m * n;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -284,10 +396,7 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
       int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
       int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
       for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) {
-          int t = tj * tm + ti;
-          if (atomicMax(&mark[t], 1) < 1) list[atomicAdd(count, 1)] = t;
-        }
+        for (int ti = ti0; ti <= ti1; ti++) q_push(qa, tj * qa.tm + ti);
     }
   }
 }
@@ -333,57 +442,50 @@ int elementwise_grid(int64_t N) {
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
-// Host driver of the round loop.  `init` fills the initial list.
+// Host driver: set up the queue, run one persistent launch, read the status.
 template <int KIND>
-tt_cuda_status run_rounds(float *state, const float *aux, const int32_t *flats,
-                          const GridDims &g, cudaStream_t st) {
+tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
+                         const GridDims &g, cudaStream_t st) {
   const int T = g.tiles();
+  const unsigned long long cap = 2ULL * (unsigned long long)T + 64;
   Workspace &ws = workspace();
-  size_t need = 3 * align_up((size_t)T * 4) + 256 * 2;
+  size_t need = align_up(sizeof(QueueCtl)) + align_up(cap * 4) + align_up((size_t)T * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
-  int *lists[2] = {(int *)ws.take((size_t)T * 4), (int *)ws.take((size_t)T * 4)};
-  int *mark = (int *)ws.take((size_t)T * 4);
-  int *counts = (int *)ws.take(256);
-  int *hcount = (int *)pinned_scratch();
-  if (!hcount) return TT_CUDA_ERR_ALLOC;
+  QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
+  int *q = (int *)ws.take(cap * 4);
+  int *inq = (int *)ws.take((size_t)T * 4);
+  QueueCtl *hctl = (QueueCtl *)pinned_scratch();
+  if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  TT_CHECK(cudaMemsetAsync(mark, 0, (size_t)T * 4, st));
-  TT_CHECK(cudaMemsetAsync(counts, 0, 2 * sizeof(int) * 2, st));
+  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, q, inq, cap, 0};
+  const int64_t cap_rounds = max_rounds();
+  ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
+  TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
+  const int qgrid = (int)std::min<unsigned long long>((cap + 255) / 256, (unsigned long long)sm_count() * 16);
   if (KIND == FILL) {
-    TT_LAUNCH(iota_kernel, (T + 255) / 256, 256, 0, st, lists[1], mark, T);
-    TT_CHECK(cudaMemcpyAsync(counts + 1, &T, sizeof(int), cudaMemcpyHostToDevice, st));
-    TT_CHECK(cudaStreamSynchronize(st));  // T lives on the host stack
+    TT_LAUNCH(queue_all_kernel, qgrid, 256, 0, st, q, inq, ctl, T, cap);
   } else {
-    TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state,
-              flats, g.m, g.n, g.tm, g.tn, lists[1], counts + 1, mark);
+    TT_LAUNCH(queue_clear_kernel, qgrid, 256, 0, st, q, inq, T, cap);
+    TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats,
+              g.m, g.n, ra);
   }
   TT_CHECK(cudaGetLastError());
-
-  const int grid = sm_count() * 8;
-  const int64_t cap = max_rounds();
-  int64_t round = 1;  // the initial list is round 1, stored in slot 1
-  const int batch = 8;
-  for (;;) {
-    const int nb = (int)std::min<int64_t>(batch, cap - round + 1);
-    if (nb <= 0) {
-      set_last_rounds(round - 1);
-      return TT_CUDA_ERR_NOT_CONVERGED;
-    }
-    for (int b = 0; b < nb; b++) {
-      int in = (int)(round & 1), out = (int)((round + 1) & 1);
-      TT_CHECK(cudaMemsetAsync(counts + out, 0, sizeof(int), st));
-      RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, lists[in],
-                   counts + in, lists[out], counts + out, mark, (int)round};
-      TT_LAUNCH(relax_round_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
-      round++;
-    }
-    TT_CHECK(cudaGetLastError());
-    TT_CHECK(cudaMemcpyAsync(hcount, counts + (round & 1), sizeof(int),
-                             cudaMemcpyDeviceToHost, st));
-    TT_CHECK(cudaStreamSynchronize(st));
-    if (*hcount == 0) break;
+  static int blocks_per_sm[2] = {0, 0};
+  if (!blocks_per_sm[KIND]) {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND>,
+                                                  kWarps * 32, 0);
+    blocks_per_sm[KIND] = b > 0 ? b : 1;
   }
-  set_last_rounds(round - 1);
+  const int grid = sm_count() * blocks_per_sm[KIND];
+  TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
+  TT_CHECK(cudaGetLastError());
+  TT_CHECK(cudaMemcpyAsync(hctl, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaStreamSynchronize(st));
+  // Report tile visits per tile as "rounds" (comparable to a sweep count).
+  set_last_rounds((int64_t)(hctl->visits / (unsigned long long)(T > 0 ? T : 1)));
+  if (hctl->abort & ABORT_VISITS) return TT_CUDA_ERR_NOT_CONVERGED;
+  if (hctl->abort & ABORT_SPIN) return TT_CUDA_ERR_NOT_CONVERGED;
   return TT_CUDA_SUCCESS;
 }
 
@@ -394,7 +496,7 @@ tt_cuda_status fill_dev(float *f, const float *dem, const uint8_t *bc,
   TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem,
             bc, g.cells());
   TT_CHECK(cudaGetLastError());
-  return run_rounds<FILL>(f, dem, nullptr, g, st);
+  return run_queue<FILL>(f, dem, nullptr, g, st);
 }
 
 tt_cuda_status reconstruct_dev(float *marker, const float *mask,
@@ -405,7 +507,7 @@ tt_cuda_status reconstruct_dev(float *marker, const float *mask,
   TT_CHECK(cudaMallocAsync((void **)&buf, (size_t)N * 8, st));
   float *f = buf, *z = buf + N;
   TT_LAUNCH(negate_pair_kernel, elementwise_grid(N), 256, 0, st, f, z, marker, mask, N);
-  tt_cuda_status s = run_rounds<FILL>(f, z, nullptr, g, st);
+  tt_cuda_status s = run_queue<FILL>(f, z, nullptr, g, st);
   if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED)
     TT_LAUNCH(negate_kernel, elementwise_grid(N), 256, 0, st, marker, f, N);
   cudaFreeAsync(buf, st);
@@ -415,7 +517,7 @@ tt_cuda_status reconstruct_dev(float *marker, const float *mask,
 tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
                         const int32_t *flats, const GridDims &g,
                         cudaStream_t st) {
-  tt_cuda_status s = run_rounds<GWDT>(dist, costs, flats, g, st);
+  tt_cuda_status s = run_queue<GWDT>(dist, costs, flats, g, st);
   if ((s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED) && prev) {
     TT_LAUNCH(gwdt_prev_kernel, elementwise_grid(g.cells()), 256, 0, st, prev,
               dist, costs, flats, g.m, g.n);

@@ -1,0 +1,124 @@
+"""Per-stage timing of the D8 pipeline (also the target for ncu captures).
+
+    python -m libtopotoolbox_gb300.stagebench --workload plain_4096 \
+        --stage flow_accumulation --reps 5
+
+Runs the stages before `--stage` once to build its inputs, then times the
+chosen stage `--reps` times with CUDA events on the current stream and prints
+one JSON line (ms per call, Gcells/s, algorithmic GB/s).  `--stage pipeline`
+times the whole sequence.  Inputs stay resident in device memory.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+BYTES = {
+    "fillsinks": 9, "identifyflats": 8, "gwdt_computecosts": 24, "gwdt": 12,
+    "flow_routing_d8_carve": 21, "flow_accumulation": 13,
+    "flow_accumulation_weighted": 17, "flow_accumulation_backward": 9,
+    "hillshade_fused": 8, "hillshade_backward": 12, "pipeline": 87,
+}
+STAGES = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
+          "flow_routing_d8_carve", "flow_accumulation", "flow_accumulation_weighted",
+          "flow_accumulation_backward", "hillshade_fused", "hillshade_backward", "pipeline"]
+
+
+def load(workload, size):
+    from . import dems
+
+    kw = {} if size is None else {"size": size}
+    if workload == "grad_8192":
+        dem, bc, w, cs = dems.grad_8192(**kw)
+        return dem, bc, w, cs
+    dem, bc, cs = getattr(dems, workload)(**kw)
+    if np.isnan(dem).any():
+        dem, bc, _ = dems.nan_to_outlets(dem, bc)
+    rng = np.random.default_rng(0)
+    w = np.asfortranarray(rng.lognormal(0.0, 0.5, size=dem.shape).astype(np.float32))
+    return dem, bc, w, cs
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="plain_4096",
+                    choices=["plain_512", "plain_4096", "plain_16384", "grad_8192"])
+    ap.add_argument("--size", type=int, default=None)
+    ap.add_argument("--stage", default="pipeline", choices=STAGES)
+    ap.add_argument("--reps", type=int, default=5)
+    args = ap.parse_args(argv)
+
+    import torch
+
+    from . import _native as N
+    from .api import dev
+
+    N.lib()
+    dv = torch.device("cuda", 0)
+    dem, bc, w, cs = load(args.workload, args.size)
+    m, n = dem.shape
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dv)  # noqa: E731
+    d_dem, d_bc, d_w = t(dem), t(bc), t(w)
+    st = args.stage
+
+    ctx = {}
+    if st != "pipeline":
+        filled = dev.fillsinks(d_dem, d_bc)
+        flats = dev.identifyflats(filled)
+        costs, _ = dev.gwdt_computecosts(flats, d_dem, filled)
+        dist = dev.gwdt(costs, flats)
+        _, direction = dev.flow_routing_d8_carve(filled, dist, flats, want_node=False)
+        g = torch.rand_like(d_dem) * 2 - 1
+        ctx = dict(filled=filled, flats=flats, costs=costs, dist=dist, direction=direction, g=g)
+    torch.cuda.synchronize()
+
+    def call():
+        c = ctx
+        if st == "fillsinks":
+            dev.fillsinks(d_dem, d_bc, out=c["filled"])
+        elif st == "identifyflats":
+            dev.identifyflats(c["filled"], out=c["flats"])
+        elif st == "gwdt_computecosts":
+            dev.gwdt_computecosts(c["flats"], d_dem, c["filled"])
+        elif st == "gwdt":
+            dev.gwdt(c["costs"], c["flats"])
+        elif st == "flow_routing_d8_carve":
+            dev.flow_routing_d8_carve(c["filled"], c["dist"], c["flats"])
+        elif st == "flow_accumulation":
+            dev.flow_accumulation(c["direction"])
+        elif st == "flow_accumulation_weighted":
+            dev.flow_accumulation(c["direction"], d_w)
+        elif st == "flow_accumulation_backward":
+            dev.flow_accumulation_backward(c["direction"], c["g"])
+        elif st == "hillshade_fused":
+            dev.hillshade_fused(d_dem, 3.9269908, 1.0471976, cs)
+        elif st == "hillshade_backward":
+            dev.hillshade_backward(d_dem, c["g"], 3.9269908, 1.0471976, cs)
+        else:
+            dev.d8_pipeline(d_dem, d_bc)
+
+    call()
+    torch.cuda.synchronize()
+    times = []
+    stream = torch.cuda.current_stream()
+    for _ in range(args.reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        call()
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = float(np.median(times))
+    cells = m * n
+    print(json.dumps({"stage": st, "workload": args.workload, "dims": [m, n], "ms": ms,
+                      "ms_all": times, "gcells_s": cells / (ms * 1e-3) / 1e9,
+                      "alg_gbs": BYTES[st] * cells / (ms * 1e-3) / 1e9,
+                      "last_rounds": int(N.lib().tt_cuda_last_rounds())}))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
