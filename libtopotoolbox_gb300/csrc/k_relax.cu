@@ -24,18 +24,17 @@
 // back with a float atomic minimum; a changed edge or corner pushes the
 // neighbouring tile onto a global work queue.
 //
-// Scheduling: one persistent launch.  Every warp pops a tile from the queue
-// (a ring buffer with monotone head/tail counters), relaxes it and pushes the
-// neighbours it changed, so information crosses tile borders as soon as a
-// tile finishes, with no host round trips.  A per-tile "queued" flag keeps a
-// tile in the queue at most once; it is cleared when the tile is popped,
-// before its halo is read, so later changes re-queue it.  A tile may then be
-// relaxed by two warps at once: both results are valid upper bounds, and
-// because the pointwise minimum of two fixpoints of either update is again a
-// fixpoint, the atomic-minimum write keeps the result exact.  A pending
-// counter (queued + running tiles) detects termination.  Every wait is
-// bounded: a warp that spins too long, or a run that exceeds its visit
-// budget, raises an abort flag and all warps return with an error status.
+// Scheduling: one persistent launch.  Warp w of W owns the tiles
+// w, w + W, w + 2W, ... and keeps scanning their "dirty" flags (32 at a time
+// with a ballot); a warp that relaxes a tile and changes an edge marks the
+// neighbouring tile dirty, so information crosses tile borders as soon as a
+// tile finishes, with no host round trips and no shared queue to contend on.
+// A tile has a single owner, so no two warps relax it at once.  A pending
+// counter (dirty + running tiles) detects termination: it is raised before a
+// flag is set and lowered only after the owner has finished the tile, so it
+// cannot reach zero while work remains.  Every wait is bounded: a warp that
+// idles too long, or a run that exceeds its visit budget, raises an abort
+// flag and all warps return with an error status.
 #include <algorithm>
 #include <cmath>
 
@@ -57,18 +56,16 @@ struct WarpTile {
   uint32_t dirty[kHalo];   // changed interior rows (bit r-1) of column c
 };
 
-// Queue control block (device memory, zero-initialised except `cap`).
+// Control block (device memory, zero-initialised).
 struct QueueCtl {
-  unsigned long long head;    // next slot to pop
-  unsigned long long tail;    // next slot to push
   unsigned long long visits;  // tiles relaxed so far
-  int pending;                // queued + running tiles
+  int pending;                // dirty + running tiles
   int abort;                  // ABORT_* bits
 };
 
 enum : int { ABORT_SPIN = 1, ABORT_VISITS = 2 };
 
-constexpr long long kSpinLimit = 1LL << 22;  // idle polls before giving up
+constexpr long long kSpinLimit = 1LL << 22;  // idle scans before giving up
 
 struct RelaxArgs {
   float *state;
@@ -77,62 +74,18 @@ struct RelaxArgs {
   int64_t m, n;
   int tm, tn;
   QueueCtl *ctl;
-  int *q;       // ring of tile ids, -1 = empty slot
-  int *inq;     // per tile: 1 while queued
-  unsigned long long cap;  // ring capacity (> number of tiles)
+  int *dirty;  // per tile: 1 while waiting to be relaxed
   unsigned long long max_visits;
 };
 
-__device__ __forceinline__ void q_push(const RelaxArgs &a, int t) {
-  if (atomicExch(&a.inq[t], 1) != 0) return;  // already queued
+__device__ __forceinline__ void mark_dirty(const RelaxArgs &a, int t) {
   atomicAdd(&a.ctl->pending, 1);
-  unsigned long long pos = atomicAdd(&a.ctl->tail, 1ULL);
-  int *slot = &a.q[pos % a.cap];
-  // The slot's previous entry has been claimed by a popper (at most `tiles`
-  // entries are ever queued and cap exceeds that); wait until it took it.
-  for (long long k = 0; atomicCAS(slot, -1, t) != -1; k++) {
-    if (k > kSpinLimit) {
-      atomicOr(&a.ctl->abort, ABORT_SPIN);
-      return;
-    }
-    __nanosleep(64);
-  }
+  if (atomicExch(&a.dirty[t], 1) != 0) atomicSub(&a.ctl->pending, 1);
 }
 
 __device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj) {
   if (ti < 0 || tj < 0 || ti >= a.tm || tj >= a.tn) return;
-  q_push(a, tj * a.tm + ti);
-}
-
-// Claims the next queued tile, or returns -1 when the queue is empty.
-__device__ __forceinline__ int q_pop(const RelaxArgs &a) {
-  volatile unsigned long long *vh = &a.ctl->head;
-  volatile unsigned long long *vt = &a.ctl->tail;
-  unsigned long long h = *vh;
-  for (;;) {
-    if (h >= *vt) return -1;
-    unsigned long long old = atomicCAS(&a.ctl->head, h, h + 1);
-    if (old == h) break;
-    h = old;
-  }
-  int *slot = &a.q[h % a.cap];
-  int v;
-  for (long long k = 0; (v = atomicExch(slot, -1)) < 0; k++) {
-    if (k > kSpinLimit) {
-      atomicOr(&a.ctl->abort, ABORT_SPIN);
-      return -1;
-    }
-    __nanosleep(32);
-  }
-  return v;
-}
-
-// Float minimum through integer atomics (values are never NaN here).
-__device__ __forceinline__ void atomic_min_float(float *addr, float v) {
-  if (!signbit(v))
-    atomicMin((int *)addr, __float_as_int(v));
-  else
-    atomicMax((unsigned int *)addr, __float_as_uint(v));
+  mark_dirty(a, tj * a.tm + ti);
 }
 
 template <int KIND>
@@ -206,41 +159,72 @@ __device__ bool sweep_cols(WarpTile &t, int lane, int dir) {
 }
 
 template <int KIND>
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile);
+
+template <int KIND>
 __global__ void __launch_bounds__(kWarps * 32)
 relax_persistent_kernel(RelaxArgs a) {
   __shared__ WarpTile tiles[kWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpTile &t = tiles[warp];
+  const int W = gridDim.x * kWarps;
+  const int wid = blockIdx.x * kWarps + warp;
+  const int T = a.tm * a.tn;
   long long idle = 0;
   for (;;) {
-    int tile = -1, stop = 0;
-    if (lane == 0) {
-      if (*(volatile int *)&a.ctl->abort) {
-        stop = 1;
-      } else {
-        tile = q_pop(a);
-        if (tile < 0) {
-          if (*(volatile int *)&a.ctl->pending == 0) {
-            stop = 1;
-          } else if (++idle > kSpinLimit) {
-            atomicOr(&a.ctl->abort, ABORT_SPIN);
-            stop = 1;
-          } else {
-            __nanosleep(idle < 64 ? 100 : 1000);
+    if (*(volatile int *)&a.ctl->abort) break;
+    bool did = false;
+    for (int base = wid; base < T; base += W * 32) {
+      const int mine = base + lane * W;
+      int f = (mine < T) ? *(volatile int *)&a.dirty[mine] : 0;
+      unsigned mask = __ballot_sync(0xffffffffu, f != 0);
+      while (mask) {
+        const int l = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int tile = base + l * W;
+        int got = 0;
+        if (lane == 0) {
+          got = atomicExch(&a.dirty[tile], 0);
+          if (got) {
+            if (atomicAdd(&a.ctl->visits, 1ULL) >= a.max_visits)
+              atomicOr(&a.ctl->abort, ABORT_VISITS);
+            __threadfence();
           }
-        } else {
-          idle = 0;
-          atomicExch(&a.inq[tile], 0);  // later changes re-queue this tile
-          if (atomicAdd(&a.ctl->visits, 1ULL) >= a.max_visits)
-            atomicOr(&a.ctl->abort, ABORT_VISITS);
-          __threadfence();
         }
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (!got) continue;
+        did = true;
+        relax_tile<KIND>(a, t, lane, tile);
+        if (lane == 0) {
+          __threadfence();
+          atomicSub(&a.ctl->pending, 1);
+        }
+        __syncwarp();
       }
     }
-    stop = __shfl_sync(0xffffffffu, stop, 0);
-    if (stop) break;
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile < 0) continue;
+    if (did) {
+      idle = 0;
+      continue;
+    }
+    int stop = 0;
+    if (lane == 0) {
+      if (*(volatile int *)&a.ctl->pending <= 0) {
+        stop = 1;
+      } else if (++idle > kSpinLimit) {
+        atomicOr(&a.ctl->abort, ABORT_SPIN);
+        stop = 1;
+      } else {
+        __nanosleep(idle < 64 ? 64 : 512);
+      }
+    }
+    if (__shfl_sync(0xffffffffu, stop, 0)) break;
+  }
+}
+
+// Relaxes one tile to its local fixpoint and marks changed neighbours dirty.
+template <int KIND>
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile) {
+  {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
 
@@ -301,7 +285,7 @@ relax_persistent_kernel(RelaxArgs a) {
       int64_t j = j0 + c - 1;
       int64_t i = i0 + lane;
       if ((dm >> lane) & 1u) {
-        if (j < a.n && i < a.m) atomic_min_float(&a.state[j * a.m + i], t.s[c][lane + 1]);
+        if (j < a.n && i < a.m) a.state[j * a.m + i] = t.s[c][lane + 1];
       }
       top |= dm & 1u;
       bottom |= (dm >> 31) & 1u;
@@ -319,8 +303,6 @@ relax_persistent_kernel(RelaxArgs a) {
       if (right & 1u) push_tile(a, ti - 1, tj + 1);
       if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1);
       if (quiet < 4) push_tile(a, ti, tj);  // capped: come back later
-      __threadfence();
-      atomicSub(&a.ctl->pending, 1);
     }
     __syncwarp();
   }
@@ -357,26 +339,11 @@ __global__ void negate_kernel(float *__restrict__ out, const float *__restrict__
     out[p] = -in[p];
 }
 
-// Queue every tile (fill starts everywhere).
-__global__ void queue_all_kernel(int *q, int *inq, QueueCtl *ctl, int n,
-                                 unsigned long long cap) {
-  for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-       t < cap; t += (unsigned long long)gridDim.x * blockDim.x) {
-    q[t] = t < (unsigned long long)n ? (int)t : -1;
-    if (t < (unsigned long long)n) inq[t] = 1;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->tail = n;
-    ctl->pending = n;
-  }
-}
-
-__global__ void queue_clear_kernel(int *q, int *inq, int n, unsigned long long cap) {
-  for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-       t < cap; t += (unsigned long long)gridDim.x * blockDim.x) {
-    q[t] = -1;
-    if (t < (unsigned long long)n) inq[t] = 0;
-  }
+// Mark every tile dirty (fill starts everywhere).
+__global__ void dirty_all_kernel(int *dirty, QueueCtl *ctl, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    dirty[t] = 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = n;
 }
 
 // dist = 1 at presills, +INF at other flats, 0 elsewhere; enqueue every tile
@@ -396,7 +363,7 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
       int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
       int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
       for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) q_push(qa, tj * qa.tm + ti);
+        for (int ti = ti0; ti <= ti1; ti++) mark_dirty(qa, tj * qa.tm + ti);
     }
   }
 }
@@ -442,30 +409,29 @@ int elementwise_grid(int64_t N) {
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
-// Host driver: set up the queue, run one persistent launch, read the status.
+// Host driver: mark the starting tiles, run one persistent launch, read the
+// status.
 template <int KIND>
 tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
                          const GridDims &g, cudaStream_t st) {
   const int T = g.tiles();
-  const unsigned long long cap = 2ULL * (unsigned long long)T + 64;
   Workspace &ws = workspace();
-  size_t need = align_up(sizeof(QueueCtl)) + align_up(cap * 4) + align_up((size_t)T * 4);
+  size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
-  int *q = (int *)ws.take(cap * 4);
-  int *inq = (int *)ws.take((size_t)T * 4);
+  int *dirty = (int *)ws.take((size_t)T * 4);
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
   if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, q, inq, cap, 0};
+  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, dirty, 0};
   const int64_t cap_rounds = max_rounds();
   ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
-  const int qgrid = (int)std::min<unsigned long long>((cap + 255) / 256, (unsigned long long)sm_count() * 16);
+  const int tgrid = (T + 255) / 256;
   if (KIND == FILL) {
-    TT_LAUNCH(queue_all_kernel, qgrid, 256, 0, st, q, inq, ctl, T, cap);
+    TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, ctl, T);
   } else {
-    TT_LAUNCH(queue_clear_kernel, qgrid, 256, 0, st, q, inq, T, cap);
+    TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats,
               g.m, g.n, ra);
   }
@@ -477,15 +443,16 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
                                                   kWarps * 32, 0);
     blocks_per_sm[KIND] = b > 0 ? b : 1;
   }
-  const int grid = sm_count() * blocks_per_sm[KIND];
+  // No more warps than tiles (each warp owns at least one tile).
+  int grid = sm_count() * blocks_per_sm[KIND];
+  grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
   TT_CHECK(cudaGetLastError());
   TT_CHECK(cudaMemcpyAsync(hctl, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
-  // Report tile visits per tile as "rounds" (comparable to a sweep count).
+  // Tile visits per tile, reported as "rounds".
   set_last_rounds((int64_t)(hctl->visits / (unsigned long long)(T > 0 ? T : 1)));
-  if (hctl->abort & ABORT_VISITS) return TT_CUDA_ERR_NOT_CONVERGED;
-  if (hctl->abort & ABORT_SPIN) return TT_CUDA_ERR_NOT_CONVERGED;
+  if (hctl->abort) return TT_CUDA_ERR_NOT_CONVERGED;
   return TT_CUDA_SUCCESS;
 }
 
