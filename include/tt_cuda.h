@@ -232,6 +232,23 @@ TT_CUDA_API tt_cuda_status tt_cuda_hillshade_fused_dev(
 TT_CUDA_API tt_cuda_status tt_cuda_hillshade_backward_dev(
     float *grad_dem, const float *dem, const float *grad_output, float azimuth,
     float altitude, float cellsize, const ptrdiff_t dims[2], void *stream);
+/** fillsinks on device pointers without allocating anything.  No
+ *  counterpart in the reference.  For callers that cannot call cudaMalloc
+ *  while they run -- a framework whose own memory pool already owns the
+ *  device, or a loop that must not pay for cudaMalloc/cudaFree, which can
+ *  synchronise the whole device.  The fill's scratch (a control block and
+ *  one flag per 32 x 32 tile) lives in a static device array sized for
+ *  65536 tiles (for example 8192 x 8192 pixels); each device that loads the
+ *  library keeps it until the process exits.  Larger grids are rejected with
+ *  TT_CUDA_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ *  array's device address (cudaGetSymbolAddress) with that device current;
+ *  make that first call before any stream capture.  All calls share the
+ *  array: each call re-initialises it, and calls that overlap on the GPU
+ *  (other streams, other threads on the same device) race on it.  The call
+ *  synchronises `stream` before it returns. */
+TT_CUDA_API tt_cuda_status tt_cuda_fillsinks_noalloc_dev(
+    float *output, const float *dem, const uint8_t *bc,
+    const ptrdiff_t dims[2], void *stream);
 /** Device form of tt_cuda_d8_pipeline.  `hillshade` (may be NULL) adds the
  *  hillshade of the input DEM with the given angles. */
 TT_CUDA_API tt_cuda_status tt_cuda_d8_pipeline_dev(

@@ -45,6 +45,7 @@ SIGNATURES = {
     "tt_cuda_d8_pipeline": (None, [P, P, P, P, P, P, P, P, P, PD]),
     # device-pointer forms
     "tt_cuda_fillsinks_dev": (ST, [P, P, P, PD, P]),
+    "tt_cuda_fillsinks_noalloc_dev": (ST, [P, P, P, PD, P]),
     "tt_cuda_reconstruct_dev": (ST, [P, P, PD, P]),
     "tt_cuda_identifyflats_dev": (ST, [P, P, PD, P, P]),
     "tt_cuda_gwdt_computecosts_dev": (ST, [P, P, P, P, P, PD, P]),

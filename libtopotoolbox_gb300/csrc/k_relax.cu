@@ -37,6 +37,7 @@
 // flag and all warps return with an error status.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "tt_internal.cuh"
 
@@ -493,4 +494,106 @@ tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
   return s;
 }
 
+// ------------------------------------------------------------------
+// Sink filling that allocates nothing (tt_cuda_fillsinks_noalloc_dev).
+//
+// For callers that cannot allocate device memory once they are running: a
+// framework whose own pool already holds the device's memory, or a loop
+// that must not pay for cudaMalloc/cudaFree (both can synchronise the whole
+// device).  The only scratch of the fill -- the control block and one flag
+// per 32 x 32 tile -- lives in the file-scope array below, sized for
+// kNoAllocMaxTiles tiles; every device that loads this library holds it
+// until the process exits.  All calls share it: each call clears what must
+// start at zero, and calls that overlap on the GPU race on it.
+// ------------------------------------------------------------------
+constexpr int kNoAllocMaxTiles = 65536;  // e.g. 8192 x 8192 pixels
+constexpr int kNoAllocHeaderWords = 64;  // control block, padded to 256 bytes
+static __device__ __align__(256) int g_fill_scratch[kNoAllocHeaderWords + kNoAllocMaxTiles];
+
+namespace {
+void *g_fill_scratch_addr[64];  // device address of g_fill_scratch, per device
+std::mutex g_fill_scratch_mu;
+
+// Set-up, once per device, with that device current.
+tt_cuda_status fill_scratch_address(void **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return TT_CUDA_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= 64) return TT_CUDA_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_fill_scratch_mu);
+  if (!g_fill_scratch_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_fill_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      return TT_CUDA_ERR_CUDA;
+    }
+    g_fill_scratch_addr[dev] = p;
+  }
+  *out = g_fill_scratch_addr[dev];
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
+                            const GridDims &g, cudaStream_t st) {
+  void *base = nullptr;
+  tt_cuda_status s = fill_scratch_address(&base);
+  if (s != TT_CUDA_SUCCESS) return s;
+  QueueCtl *ctl = (QueueCtl *)base;
+  int *dirty = (int *)base + kNoAllocHeaderWords;
+  const int T = g.tiles();
+  TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem, bc,
+            g.cells());
+  TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
+  TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, ctl, T);
+  TT_CHECK(cudaGetLastError());
+  RelaxArgs ra{f, dem, nullptr, g.m, g.n, g.tm, g.tn, ctl, dirty, 0};
+  ra.max_visits = (unsigned long long)T *
+                  (unsigned long long)std::min<int64_t>(max_rounds(), 1LL << 20);
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<FILL>,
+                                                kWarps * 32, 0);
+  int grid = sm_count() * (b > 0 ? b : 1);
+  grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
+  TT_LAUNCH(relax_persistent_kernel<FILL>, grid, kWarps * 32, 0, st, ra);
+  TT_CHECK(cudaGetLastError());
+  QueueCtl h;  // read back into host stack memory: no pinned allocation
+  TT_CHECK(cudaMemcpyAsync(&h, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaStreamSynchronize(st));
+  set_last_rounds((int64_t)(h.visits / (unsigned long long)(T > 0 ? T : 1)));
+  return h.abort ? TT_CUDA_ERR_NOT_CONVERGED : TT_CUDA_SUCCESS;
+}
+}  // namespace
+
 }  // namespace tt
+
+extern "C" tt_cuda_status tt_cuda_fillsinks_noalloc_dev(float *output,
+                                                        const float *dem,
+                                                        const uint8_t *bc,
+                                                        const ptrdiff_t dims[2],
+                                                        void *stream) {
+  using namespace tt;
+  tt_cuda_status s = TT_CUDA_SUCCESS;
+  if (!output || !dem || !bc || !dims || dims[0] <= 0 || dims[1] <= 0 ||
+      dims[0] >= (1LL << 31) || dims[1] >= (1LL << 31) ||
+      dims[0] * dims[1] >= (1LL << 31)) {
+    s = TT_CUDA_ERR_INVALID_ARGUMENT;
+  } else {
+    GridDims g = make_dims(dims);
+    int ndev = 0;
+    if (g.tiles() > kNoAllocMaxTiles) {
+      s = TT_CUDA_ERR_INVALID_ARGUMENT;  // beyond the static scratch
+    } else if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      s = TT_CUDA_ERR_NO_DEVICE;
+    } else {
+      DeviceLock lock;
+      s = fill_noalloc(output, dem, bc, g, (cudaStream_t)stream);
+      if (s == TT_CUDA_ERR_CUDA) cudaGetLastError();
+    }
+  }
+  set_status(s);
+  return s;
+}
