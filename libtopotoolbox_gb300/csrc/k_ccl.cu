@@ -15,6 +15,12 @@
 // `conncomps` is the smallest linear index among the component's pixels of
 // maximal depth; the reference picks one of those pixels by its scan-order
 // union-find (src/gwdt.c:141-153), which can differ when depths tie.
+//
+// Work decomposition: one warp per 32 x 32 tile labels the tile's internal
+// edges in shared memory (with path halving) and reduces each tile-local
+// component to its maximum depth and the smallest pixel attaining it; only
+// edges that cross tile borders touch the global union-find, and the global
+// maximum / argmax take one atomic per (tile, component), not per pixel.
 #include <algorithm>
 #include <climits>
 
@@ -31,11 +37,16 @@ __device__ __forceinline__ float key_to_float(int k) {
   return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff);
 }
 
-__device__ __forceinline__ int uf_find(const int *L, int x) {
-  int y = ((volatile const int *)L)[x];
-  while (y != x) {
-    x = y;
-    y = ((volatile const int *)L)[x];
+// Root of x; labels always point at smaller or equal indices.  Path halving
+// only ever lowers a label (atomicMin), so it is safe under concurrent unions.
+__device__ __forceinline__ int uf_find(int *L, int x) {
+  volatile int *vL = L;
+  int p = vL[x];
+  while (p != x) {
+    int gp = vL[p];
+    if (gp < p) atomicMin(&L[x], gp);
+    x = p;
+    p = gp;
   }
   return x;
 }
@@ -57,61 +68,53 @@ __device__ void uf_union(int *L, int a, int b) {
   }
 }
 
-// Tile-local labelling: one warp per 32 x 32 tile runs the union-find in
-// shared memory over the tile's internal edges, then writes for every flat
-// pixel the global index of its tile-local root (the smallest index of its
-// tile-local component).  Roots get their max-depth and argmax slots reset.
 constexpr int kCclWarps = 4;
 
-__device__ __forceinline__ int sfind(const int *lab, int x) {
-  int y = ((volatile const int *)lab)[x];
-  while (y != x) {
-    x = y;
-    y = ((volatile const int *)lab)[x];
-  }
-  return x;
-}
-
-__device__ void sunion(int *lab, int a, int b) {
-  for (int it = 0; it < 4096; it++) {
-    a = sfind(lab, a);
-    b = sfind(lab, b);
-    if (a == b) return;
-    if (a < b) {
-      int old = atomicMin(&lab[b], a);
-      if (old == b) return;
-      b = old;
-    } else {
-      int old = atomicMin(&lab[a], b);
-      if (old == a) return;
-      a = old;
-    }
-  }
-}
+struct CclTile {
+  int lab[kTile * kTile];
+  int key[kTile * kTile];  // per local root: max depth key, then argmax
+};
 
 __global__ void __launch_bounds__(kCclWarps * 32)
-ccl_tile_kernel(int *__restrict__ L, int *__restrict__ maxkey,
-                int *__restrict__ argmax, const int32_t *__restrict__ flats,
-                int64_t m, int64_t n, int tm, int tn) {
-  __shared__ int lab[kCclWarps][kTile * kTile];
+ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ larg,
+                int *__restrict__ maxkey, int *__restrict__ argmax,
+                const int32_t *__restrict__ flats, const float *__restrict__ orig,
+                const float *__restrict__ filled, int64_t m, int64_t n, int tm, int tn) {
+  __shared__ CclTile tiles[kCclWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int *lb = lab[warp];
+  CclTile &t = tiles[warp];
+  int *lb = t.lab;
   const int T = tm * tn;
   for (int tile = blockIdx.x * kCclWarps + warp; tile < T; tile += gridDim.x * kCclWarps) {
     const int ti = tile % tm, tj = tile / tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
     const int ii = lane;
     const int64_t i = i0 + ii;
+    int keys[kTile];  // depth key of this lane's pixel in each column
+    uint32_t flat_cols = 0;
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
-      bool f = i < m && j < n && (flats[j * m + i] & 1);
-      lb[jj * kTile + ii] = f ? jj * kTile + ii : -1;
+      const int loc = jj * kTile + ii;
+      bool f = false;
+      int k = INT_MIN;
+      if (i < m && j < n) {
+        const int64_t p = j * m + i;
+        f = flats[p] & 1;
+        if (f) {
+          float d = __fsub_rn(filled[p], orig[p]);
+          if (!isnan(d)) k = ordered_key(d);
+        }
+      }
+      keys[jj] = k;
+      if (f) flat_cols |= 1u << jj;
+      lb[loc] = f ? loc : -1;
+      t.key[loc] = INT_MIN;
     }
     __syncwarp();
     // internal edges to the earlier neighbours (i-1,j), (i-1,j-1), (i,j-1), (i+1,j-1)
     for (int jj = 0; jj < kTile; jj++) {
+      if (!((flat_cols >> jj) & 1u)) continue;
       const int loc = jj * kTile + ii;
-      if (lb[loc] < 0) continue;
       const int di[4] = {-1, -1, 0, 1};
       const int dj[4] = {0, -1, -1, -1};
 #pragma unroll
@@ -119,24 +122,54 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ maxkey,
         int qi = ii + di[k], qj = jj + dj[k];
         if (qi < 0 || qi >= kTile || qj < 0) continue;
         int q = qj * kTile + qi;
-        if (((volatile int *)lb)[q] >= 0) sunion(lb, loc, q);
+        if (((volatile int *)lb)[q] >= 0) uf_union(lb, loc, q);
       }
+    }
+    __syncwarp();
+    int roots[kTile];
+    for (int jj = 0; jj < kTile; jj++) {
+      roots[jj] = -1;
+      if (!((flat_cols >> jj) & 1u)) continue;
+      const int r = uf_find(lb, jj * kTile + ii);
+      roots[jj] = r;
+      if (keys[jj] != INT_MIN) atomicMax(&t.key[r], keys[jj]);
+    }
+    __syncwarp();
+    // local maxima of the roots, then the smallest pixel attaining them
+    int rmax[kTile];
+    for (int jj = 0; jj < kTile; jj++) rmax[jj] = roots[jj] >= 0 ? t.key[roots[jj]] : INT_MIN;
+    __syncwarp();
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + ii;
+      if (roots[jj] == loc) t.key[loc] = INT_MAX;
+    }
+    __syncwarp();
+    for (int jj = 0; jj < kTile; jj++) {
+      if (roots[jj] < 0 || keys[jj] == INT_MIN || keys[jj] != rmax[jj]) continue;
+      const int loc = jj * kTile + ii;
+      atomicMin(&t.key[roots[jj]], loc);
     }
     __syncwarp();
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       if (i >= m || j >= n) continue;
+      const int64_t gp = j * m + i;
       const int loc = jj * kTile + ii;
+      const int r = roots[jj];
       int v = -1;
-      if (lb[loc] >= 0) {
-        int r = sfind(lb, loc);
+      if (r >= 0) {
         v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
         if (r == loc) {
-          maxkey[j * m + i] = INT_MIN;
-          argmax[j * m + i] = INT_MAX;
+          lmax[gp] = rmax[jj];
+          const int a = t.key[loc];
+          larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
+          maxkey[gp] = INT_MIN;
+          argmax[gp] = INT_MAX;
+        } else {
+          larg[gp] = -1;  // not a local root
         }
       }
-      L[j * m + i] = v;
+      L[gp] = v;
     }
     __syncwarp();
   }
@@ -149,7 +182,6 @@ __global__ void ccl_border_kernel(int *__restrict__ L,
                                   const int32_t *__restrict__ flats, int64_t m,
                                   int64_t n, int tm, int tn) {
   const int T = tm * tn;
-  // 32 last-row + 32 last-column + 32 first-column candidates per tile
   const int64_t total = (int64_t)T * 96;
   for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
        w += (int64_t)gridDim.x * blockDim.x) {
@@ -176,38 +208,32 @@ __global__ void ccl_border_kernel(int *__restrict__ L,
   }
 }
 
-__global__ void ccl_max_kernel(int *__restrict__ L, int *__restrict__ maxkey,
-                               const int32_t *__restrict__ flats,
-                               const float *__restrict__ orig,
-                               const float *__restrict__ filled, int64_t N) {
+// Local roots fold their maxima into their global root.
+__global__ void ccl_max_kernel(int *__restrict__ L, const int *__restrict__ lmax,
+                               const int *__restrict__ larg, int *__restrict__ maxkey,
+                               const int32_t *__restrict__ flats, int64_t N) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
-    if (!(flats[p] & 1)) continue;
-    int r = uf_find(L, (int)p);
-    L[p] = r;
-    float depth = __fsub_rn(filled[p], orig[p]);
-    if (!isnan(depth)) atomicMax(&maxkey[r], ordered_key(depth));
+    if (!(flats[p] & 1) || larg[p] < 0) continue;
+    const int R = uf_find(L, (int)p);
+    if (lmax[p] != INT_MIN) atomicMax(&maxkey[R], lmax[p]);
   }
 }
 
-__global__ void ccl_argmax_kernel(const int *__restrict__ L,
-                                  const int *__restrict__ maxkey,
-                                  int *__restrict__ argmax,
-                                  const int32_t *__restrict__ flats,
-                                  const float *__restrict__ orig,
-                                  const float *__restrict__ filled, int64_t N) {
+__global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ lmax,
+                                  const int *__restrict__ larg,
+                                  const int *__restrict__ maxkey, int *__restrict__ argmax,
+                                  const int32_t *__restrict__ flats, int64_t N) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
-    if (!(flats[p] & 1)) continue;
-    int r = L[p];
-    float depth = __fsub_rn(filled[p], orig[p]);
-    if (!isnan(depth) && ordered_key(depth) == maxkey[r]) atomicMin(&argmax[r], (int)p);
+    if (!(flats[p] & 1) || larg[p] < 0) continue;
+    const int R = uf_find(L, (int)p);
+    if (lmax[p] != INT_MIN && lmax[p] == maxkey[R]) atomicMin(&argmax[R], larg[p]);
   }
 }
 
 __global__ void costs_kernel(float *__restrict__ costs,
-                             ptrdiff_t *__restrict__ conncomps,
-                             const int *__restrict__ L,
+                             ptrdiff_t *__restrict__ conncomps, int *__restrict__ L,
                              const int *__restrict__ maxkey,
                              const int *__restrict__ argmax,
                              const int32_t *__restrict__ flats,
@@ -218,13 +244,13 @@ __global__ void costs_kernel(float *__restrict__ costs,
     float c = 0.0f;
     ptrdiff_t lab = 0;
     if (flats[p] & 1) {
-      int r = L[p];
-      float maxd = key_to_float(maxkey[r]);
-      float depth = __fsub_rn(filled[p], orig[p]);
-      float diff = __fsub_rn(maxd, depth);
+      const int R = uf_find(L, (int)p);
+      const float maxd = key_to_float(maxkey[R]);
+      const float depth = __fsub_rn(filled[p], orig[p]);
+      const float diff = __fsub_rn(maxd, depth);
       c = __double2float_rn(__dadd_rn((double)diff, 0.1));
-      int a = argmax[r];
-      lab = (a == INT_MAX) ? r : a;
+      const int a = argmax[R];
+      lab = (a == INT_MAX) ? R : a;
     }
     costs[p] = c;
     conncomps[p] = lab;
@@ -245,20 +271,22 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
                          cudaStream_t st) {
   const int64_t N = g.cells();
   Workspace &ws = workspace();
-  if (!ws.reserve(3 * align_up((size_t)N * 4))) return TT_CUDA_ERR_ALLOC;
+  if (!ws.reserve(5 * align_up((size_t)N * 4))) return TT_CUDA_ERR_ALLOC;
   int *L = (int *)ws.take((size_t)N * 4);
+  int *lmax = (int *)ws.take((size_t)N * 4);
+  int *larg = (int *)ws.take((size_t)N * 4);
   int *maxkey = (int *)ws.take((size_t)N * 4);
   int *argmax = (int *)ws.take((size_t)N * 4);
   const int grid = ew_grid(N);
   const int T = g.tiles();
   const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
                                            (int64_t)sm_count() * 16);
-  TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, maxkey, argmax, flats,
-            g.m, g.n, g.tm, g.tn);
+  TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, maxkey, argmax,
+            flats, orig, filled, g.m, g.n, g.tm, g.tn);
   TT_LAUNCH(ccl_border_kernel, ew_grid((int64_t)T * 96), 256, 0, st, L, flats, g.m,
             g.n, g.tm, g.tn);
-  TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, maxkey, flats, orig, filled, N);
-  TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, maxkey, argmax, flats, orig, filled, N);
+  TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, larg, maxkey, flats, N);
+  TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, maxkey, argmax, flats, N);
   TT_LAUNCH(costs_kernel, grid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
             flats, orig, filled, N);
   TT_CHECK(cudaGetLastError());

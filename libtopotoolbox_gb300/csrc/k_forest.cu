@@ -42,13 +42,14 @@
 #include <cmath>
 #include <cstring>
 
+#include <cuda/atomic>
+
 #include "tt_internal.cuh"
 
 namespace tt {
 namespace {
 
 constexpr int kTileCells = kTile * kTile;
-constexpr int kUpWarps = 2;
 
 enum : int {
   RL_NONE = -4,    // outside the grid (partial tile)
@@ -80,17 +81,6 @@ struct UpArgs {
   int *h_out;
   int *hmax;
   int *err;
-};
-
-struct UpTile {
-  uint8_t dir[kHalo][36];  // [c][r], one-pixel halo
-  int16_t rl[kTileCells];  // local receiver or an RL_* code
-  uint8_t ent[kTileCells]; // external donors
-  int pend[kTileCells];
-  long long acc[kTileCells];
-  int h[kTileCells];
-  int16_t list[kTileCells];
-  int nlist;
 };
 
 __device__ __forceinline__ long long to_fixed(float w, int k, int *err) {
@@ -148,145 +138,196 @@ __device__ __forceinline__ int local_receiver(const uint8_t (*dir)[36], int ii,
   return RL_EXIT;
 }
 
-__global__ void __launch_bounds__(kUpWarps * 32) forest_up_kernel(UpArgs a) {
-  __shared__ UpTile tiles[kUpWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  UpTile &t = tiles[warp];
+// One 128-thread block per tile.
+//  1. receivers (local index or RL_* code), external donors, initial values
+//     (weight + inflow from other tiles in the final pass);
+//  2. in-place pointer jumping on packed (next << 16 | depth) words: after
+//     ten rounds every pixel knows its in-tile terminal (exit, outlet or
+//     grid edge) and the number of steps to it;
+//  3. a counting sort by depth;
+//  4. levels from the deepest up: every pixel of level L adds its value into
+//     its receiver (level L-1) with integer atomics, one barrier per level.
+constexpr int kUpThreads = 128;
+
+struct UpTile {
+  uint8_t dir[kHalo][36];      // [c][r], one-pixel halo
+  int16_t rl[kTileCells];      // local receiver or an RL_* code
+  uint32_t pk[kTileCells];     // pointer jumping: next << 16 | depth
+  long long acc[kTileCells];
+  int h[kTileCells];
+  int16_t order[kTileCells];   // pixels sorted by depth
+  int cnt[kTileCells + 1];     // per depth: count, then start offset
+  uint8_t ent[kTileCells];     // pixel has a donor in another tile
+  int maxd;
+  int nvalid;
+  int bad;
+};
+
+__global__ void __launch_bounds__(kUpThreads) forest_up_kernel(UpArgs a) {
+  __shared__ UpTile t;
+  const int tid = threadIdx.x;
   const int T = a.tm * a.tn;
-  for (int tile = blockIdx.x * kUpWarps + warp; tile < T;
-       tile += gridDim.x * kUpWarps) {
+  for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-    load_dir_tile(t.dir, a.dir, a.m, a.n, i0, j0, lane);
-    if (lane == 0) t.nlist = 0;
-    __syncwarp();
+    {  // stage the directions with every load in flight at once
+      constexpr int kL = (kHalo * kHalo + kUpThreads - 1) / kUpThreads;
+      uint8_t v[kL];
+#pragma unroll
+      for (int u = 0; u < kL; u++) {
+        const int e = tid + u * kUpThreads;
+        const int c = e / kHalo, r = e % kHalo;
+        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+        v[u] = (e < kHalo * kHalo && i >= 0 && i < a.m && j >= 0 && j < a.n) ? a.dir[j * a.m + i] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kL; u++) {
+        const int e = tid + u * kUpThreads;
+        if (e < kHalo * kHalo) t.dir[e / kHalo][e % kHalo] = v[u];
+      }
+    }
+    for (int e = tid; e <= kTileCells; e += kUpThreads) t.cnt[e] = 0;
+    if (tid == 0) {
+      t.maxd = 0;
+      t.nvalid = 0;
+      t.bad = 0;
+    }
+    __syncthreads();
 
-    // Receivers, donor counts, initial values.
     int nvalid = 0, bad = 0;
-    const int ii = lane;
-    const int64_t i = i0 + ii;
-    for (int jj = 0; jj < kTile; jj++) {
-      const int64_t j = j0 + jj;
-      const int loc = jj * kTile + ii;
-      int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
-      t.rl[loc] = (int16_t)rl;
-      if (rl == RL_BADDIR) bad = 1;
-      int np = 0, ne = 0;
+    for (int e = tid; e < kTileCells; e += kUpThreads) {
+      const int ii = e % kTile, jj = e / kTile;
+      const int64_t i = i0 + ii, j = j0 + jj;
+      const int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
+      t.rl[e] = (int16_t)rl;
+      bad |= rl == RL_BADDIR;
+      int ne = 0, hin = 0;
       long long inflow = 0;
-      int hin = 0;
       if (rl != RL_NONE) {
         nvalid++;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-          int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
-          int qr = ii + 1 - di, qc = jj + 1 - dj;  // halo coordinates of q
-          unsigned dq = t.dir[qc][qr];
+          const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
+          const int qr = ii + 1 - di, qc = jj + 1 - dj;  // halo coordinates of q
+          if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) continue;
+          const unsigned dq = t.dir[qc][qr];
           if (dq == 0 || d8_bit(dq) != k) continue;
-          if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) {
-            np++;
-          } else {
-            ne++;
-            if (a.phase == 3) {
-              int64_t gq = (j - dj) * a.m + (i - di);
-              if (a.want_acc) inflow += a.cacc[gq];
-              if (a.want_h) hin = max(hin, a.cH[gq] + 1);
-            }
+          ne++;
+          if (a.phase == 3) {
+            const int64_t gq = (j - dj) * a.m + (i - di);
+            if (a.want_acc) inflow += a.cacc[gq];
+            if (a.want_h) hin = max(hin, a.cH[gq] + 1);
           }
         }
       }
-      t.pend[loc] = np;
-      t.ent[loc] = (uint8_t)ne;
+      t.ent[e] = (uint8_t)(ne > 0);
       long long w0 = 0;
       if (a.want_acc && rl != RL_NONE)
         w0 = a.w ? to_fixed(a.w[j * a.m + i], a.wshift, a.err) : 1LL;
-      t.acc[loc] = w0 + inflow;
-      t.h[loc] = hin;
-      if (rl != RL_NONE && np == 0) {
-        int s = atomicAdd(&t.nlist, 1);
-        t.list[s] = (int16_t)loc;
-      }
+      t.acc[e] = w0 + inflow;
+      t.h[e] = hin;
+      t.pk[e] = rl >= 0 ? ((uint32_t)rl << 16) | 1u : ((uint32_t)e << 16);
     }
-    __syncwarp();
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(a.err, ERR_BADDIR);
-    __syncwarp();
+    if (nvalid) atomicAdd(&t.nvalid, nvalid);
+    if (bad) t.bad = 1;
+    __syncthreads();
 
-    // Last-arriver walks.
-    const int nl = *(volatile int *)&t.nlist;
-    int done = 0;
-    volatile long long *vacc = t.acc;
-    volatile int *vh = t.h;
-    for (int idx = lane; idx < nl; idx += 32) {
-      int p = t.list[idx];
-      for (int guard = 0; guard < kTileCells; guard++) {
-        long long v = vacc[p];
-        int hv = vh[p];
-        done++;
-        int q = t.rl[p];
-        if (q < 0) {
-          if (q == RL_EXIT && a.phase == 1) {
-            int64_t gp = (j0 + p / kTile) * a.m + (i0 + p % kTile);
-            if (a.want_acc) a.cacc[gp] = v;
-            if (a.want_h) a.cH[gp] = hv;
-            a.cpend[gp] = 0;
-            a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
-          }
-          break;
-        }
-        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
-        if (a.want_h) atomicMax(&t.h[q], hv + 1);
-        __threadfence_block();
-        if (atomicSub(&t.pend[q], 1) != 1) break;
-        __threadfence_block();
-        p = q;
+    // Pointer jumping (paths inside a tile are shorter than 1024 steps).
+    for (int round = 0; round < 10; round++) {
+      for (int e = tid; e < kTileCells; e += kUpThreads) {
+        const uint32_t v = t.pk[e];
+        const int q = (int)(v >> 16);
+        if (q == e) continue;
+        const uint32_t w = t.pk[q];
+        t.pk[e] = (w & 0xffff0000u) | ((v & 0xffffu) + (w & 0xffffu));
+      }
+      __syncthreads();
+    }
+    int cyc = 0, md = 0;
+    for (int e = tid; e < kTileCells; e += kUpThreads) {
+      if (t.rl[e] == RL_NONE) continue;
+      const uint32_t v = t.pk[e];
+      if (t.rl[v >> 16] >= 0) {  // never reached a terminal: a cycle
+        cyc = 1;
+        continue;
+      }
+      const int d = (int)(v & 0xffffu);
+      atomicAdd(&t.cnt[d], 1);
+      md = max(md, d);
+    }
+    if (cyc) atomicOr(a.err, ERR_CYCLE);
+    if (md) atomicMax(&t.maxd, md);
+    __syncthreads();
+    const int maxd = t.maxd;
+    if (tid == 0) {  // exclusive offsets, deepest level first
+      int run = 0;
+      for (int d = maxd; d >= 0; d--) {
+        const int c = t.cnt[d];
+        t.cnt[d] = run;
+        run += c;
       }
     }
-    __syncwarp();
-    for (int o = 16; o > 0; o >>= 1) {
-      done += __shfl_down_sync(0xffffffffu, done, o);
-      nvalid += __shfl_down_sync(0xffffffffu, nvalid, o);
+    __syncthreads();
+    for (int e = tid; e < kTileCells; e += kUpThreads) {
+      if (t.rl[e] == RL_NONE) continue;
+      const uint32_t v = t.pk[e];
+      if (t.rl[v >> 16] >= 0) continue;
+      t.order[atomicAdd(&t.cnt[v & 0xffffu], 1)] = (int16_t)e;
     }
-    if (lane == 0 && done != nvalid) atomicOr(a.err, ERR_CYCLE);
-    __syncwarp();
+    __syncthreads();
+    // After the scatter cnt[d] is the end of level d = the start of level d-1.
+    for (int d = maxd; d >= 1; d--) {
+      const int beg = d == maxd ? 0 : t.cnt[d + 1], end = t.cnt[d];
+      for (int k = beg + tid; k < end; k += kUpThreads) {
+        const int p = t.order[k];
+        const int q = t.rl[p];
+        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
+        if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
+      }
+      __syncthreads();
+    }
 
     if (a.phase == 1) {
-      // Entry pixels: exit reached in-tile and the number of steps.
-      for (int jj = 0; jj < kTile; jj++) {
-        const int loc = jj * kTile + ii;
-        if (!t.ent[loc]) continue;
-        int p = loc, steps = 0;
-        while (t.rl[p] >= 0 && steps < kTileCells) {
-          p = t.rl[p];
-          steps++;
+      for (int e = tid; e < kTileCells; e += kUpThreads) {
+        const int rl = t.rl[e];
+        const int ii = e % kTile, jj = e / kTile;
+        const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
+        if (rl == RL_EXIT) {
+          if (a.want_acc) a.cacc[gp] = t.acc[e];
+          if (a.want_h) a.cH[gp] = t.h[e];
+          a.cpend[gp] = 0;
+          a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
         }
-        int64_t gr = (j0 + jj) * a.m + i;
-        int x = -1;
-        if (t.rl[p] == RL_EXIT) x = (int)((j0 + p / kTile) * a.m + (i0 + p % kTile));
-        a.xmap[gr] = x;
-        a.xsteps[gr] = steps;
+        if (t.ent[e]) {
+          const uint32_t v = t.pk[e];
+          const int term = (int)(v >> 16);
+          int x = -1;
+          if (t.rl[term] == RL_EXIT)
+            x = (int)((j0 + term / kTile) * a.m + (i0 + term % kTile));
+          a.xmap[gp] = x;
+          a.xsteps[gp] = (int)(v & 0xffffu);
+        }
       }
     } else {
       int hm = 0;
-      for (int jj = 0; jj < kTile; jj++) {
-        const int64_t j = j0 + jj;
+      for (int e = tid; e < kTileCells; e += kUpThreads) {
+        const int ii = e % kTile, jj = e / kTile;
+        const int64_t i = i0 + ii, j = j0 + jj;
         if (i >= a.m || j >= a.n) continue;
-        const int loc = jj * kTile + ii;
-        int64_t gp = j * a.m + i;
+        const int64_t gp = j * a.m + i;
         if (a.want_acc) {
-          float v = __ll2float_rn(t.acc[loc]);
+          const float v = __ll2float_rn(t.acc[e]);
           a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
         }
         if (a.want_h) {
-          int hv = t.h[loc];
-          a.h_out[gp] = hv;
-          hm = max(hm, hv);
+          a.h_out[gp] = t.h[e];
+          hm = max(hm, t.h[e]);
         }
       }
-      if (a.want_h) {
-        for (int o = 16; o > 0; o >>= 1) hm = max(hm, __shfl_down_sync(0xffffffffu, hm, o));
-        if (lane == 0) atomicMax(a.hmax, hm);
-      }
+      if (a.want_h && hm) atomicMax(a.hmax, hm);
     }
-    __syncwarp();
+    if (tid == 0 && t.bad) atomicOr(a.err, ERR_BADDIR);
+    __syncthreads();
   }
 }
 
@@ -340,22 +381,29 @@ __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < L; a += gridDim.x * blockDim.x) {
     int e = leaves[a];
     int n_done = 0;
+    // The walker owns e: every coarse donor has arrived, so its totals are
+    // final and were published by the acquiring decrement below.
+    long long v = want_acc ? cuda::atomic_ref<long long, cuda::thread_scope_device>(cacc[e])
+                                 .load(cuda::std::memory_order_relaxed)
+                           : 0;
+    int hv = want_h ? cuda::atomic_ref<int, cuda::thread_scope_device>(cH[e])
+                          .load(cuda::std::memory_order_relaxed)
+                    : 0;
     for (int guard = 0; guard < limit; guard++) {
       n_done++;
-      int nx = cnext[e];
+      const int nx = cnext[e];
       if (nx < 0) break;
-      if (want_acc) {
-        long long v = atomicAdd((unsigned long long *)&cacc[e], 0ULL);
-        atomicAdd((unsigned long long *)&cacc[nx], (unsigned long long)v);
-      }
-      if (want_h) {
-        int hv = atomicAdd(&cH[e], 0);
-        atomicMax(&cH[nx], hv + chop[e]);
-      }
-      __threadfence();
-      if (atomicSub(&cpend[nx], 1) != 1) break;
-      __threadfence();
+      if (want_acc) atomicAdd((unsigned long long *)&cacc[nx], (unsigned long long)v);
+      if (want_h) atomicMax(&cH[nx], hv + chop[e]);
+      cuda::atomic_ref<int, cuda::thread_scope_device> pend(cpend[nx]);
+      if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) break;
       e = nx;
+      if (want_acc)
+        v = cuda::atomic_ref<long long, cuda::thread_scope_device>(cacc[e])
+                .load(cuda::std::memory_order_relaxed);
+      if (want_h)
+        hv = cuda::atomic_ref<int, cuda::thread_scope_device>(cH[e])
+                 .load(cuda::std::memory_order_relaxed);
     }
     atomicAdd(processed, n_done);
   }
@@ -704,9 +752,8 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.h_out = w.h;
   a.hmax = w.counters + 3;
   a.err = w.counters + 4;
-  const int tgrid = (int)std::min<int64_t>((T + kUpWarps - 1) / kUpWarps,
-                                           (int64_t)sm_count() * 32);
-  TT_LAUNCH(forest_up_kernel, tgrid, kUpWarps * 32, 0, st, a);
+  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 16);
+  TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
             g.m, order, w.xmap, w.xsteps, w.cnext, w.chop, w.cpend);
@@ -716,7 +763,7 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
             w.cnext, w.chop, w.cacc, w.cH, w.cpend, want_acc, want_h,
             w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
   a.phase = 3;
-  TT_LAUNCH(forest_up_kernel, tgrid, kUpWarps * 32, 0, st, a);
+  TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

@@ -55,6 +55,7 @@ struct WarpTile {
   float a[kHalo][kPitch];  // aux: dem (fill) or costs (gwdt)
   uint64_t flat[kHalo];    // gwdt: flat bit per row of column c (rows 0..33)
   uint32_t dirty[kHalo];   // changed interior rows (bit r-1) of column c
+  uint32_t need[kHalo];    // interior rows of column c to re-evaluate
 };
 
 // Control block (device memory, zero-initialised).
@@ -79,88 +80,131 @@ struct RelaxArgs {
   unsigned long long max_visits;
 };
 
-__device__ __forceinline__ void mark_dirty(const RelaxArgs &a, int t) {
+// Dirty flag values: 1 = a halo pixel changed (re-evaluate the edge ring),
+// 2 = evaluate every pixel (first visit, or a visit that hit its sweep cap).
+enum : int { DIRTY_EDGE = 1, DIRTY_FULL = 2 };
+
+__device__ __forceinline__ void mark_dirty(const RelaxArgs &a, int t, int v) {
   atomicAdd(&a.ctl->pending, 1);
-  if (atomicExch(&a.dirty[t], 1) != 0) atomicSub(&a.ctl->pending, 1);
+  if (atomicMax(&a.dirty[t], v) != 0) atomicSub(&a.ctl->pending, 1);
 }
 
-__device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj) {
+__device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj,
+                                          int v = DIRTY_EDGE) {
   if (ti < 0 || tj < 0 || ti >= a.tm || tj >= a.tn) return;
-  mark_dirty(a, tj * a.tm + ti);
+  mark_dirty(a, tj * a.tm + ti, v);
 }
 
+// The update at pixel (c, r) from all eight neighbours.  Neighbour values may
+// be old or new: every value is an upper bound of the fixpoint, so any mix
+// gives a valid (and never higher) result.
 template <int KIND>
-__device__ __forceinline__ float relax_one(const WarpTile &t, int c, int r,
-                                           int c0, int r0, int c1, int r1,
-                                           int c2, int r2, float cur) {
+__device__ __forceinline__ float relax8(const WarpTile &t, int c, int r, float cur) {
   if (KIND == FILL) {
-    float lo = fminf(fminf(fminf(cur, t.s[c0][r0]), t.s[c1][r1]), t.s[c2][r2]);
-    float z = t.a[c][r];
+    float lo = cur;
+#pragma unroll
+    for (int dc = -1; dc <= 1; dc++)
+#pragma unroll
+      for (int dr = -1; dr <= 1; dr++)
+        if (dc || dr) lo = fminf(lo, t.s[c + dc][r + dr]);
+    const float z = t.a[c][r];
     return (lo > z) ? lo : z;
   } else {
     if (!((t.flat[c] >> r) & 1)) return cur;
-    float cs = t.a[c][r];
+    const float cs = t.a[c][r];
     float best = cur;
-    const int cc[3] = {c0, c1, c2}, rr[3] = {r0, r1, r2};
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-      if (!((t.flat[cc[k]] >> rr[k]) & 1)) continue;
-      float ch = (cc[k] != c && rr[k] != r) ? kSqrt2 : 1.0f;
-      float w = __fmul_rn(__fmul_rn(ch, __fadd_rn(cs, t.a[cc[k]][rr[k]])), 0.5f);
-      float prop = __fadd_rn(t.s[cc[k]][rr[k]], w);
-      if (prop < best) best = prop;
+    for (int dc = -1; dc <= 1; dc++) {
+      const uint64_t fc = t.flat[c + dc];
+#pragma unroll
+      for (int dr = -1; dr <= 1; dr++) {
+        if (!(dc || dr)) continue;
+        if (!((fc >> (r + dr)) & 1)) continue;
+        const float ch = (dc && dr) ? kSqrt2 : 1.0f;
+        const float w = __fmul_rn(__fmul_rn(ch, __fadd_rn(cs, t.a[c + dc][r + dr])), 0.5f);
+        const float prop = __fadd_rn(t.s[c + dc][r + dr], w);
+        if (prop < best) best = prop;
+      }
     }
     return best;
   }
 }
 
-// Sweep along r (lane = column).  dir = +1 down, -1 up.
+// Work-proportional Gauss-Seidel sweeps.  need[c] marks the interior pixels
+// of column c whose neighbourhood changed since they were last evaluated
+// against all eight neighbours; only those are evaluated, a step with no
+// marked pixel is skipped by the whole warp, and a pixel that changes marks
+// its eight neighbours.  An unmarked pixel therefore cannot be lowered by any
+// neighbour, and the tile is at its local fixpoint exactly when no pixel is
+// marked.
+
+// Sweep along r (lane = column c).  dir = +1 down, -1 up.
 template <int KIND>
-__device__ bool sweep_rows(WarpTile &t, int lane, int dir) {
+__device__ void sweep_rows(WarpTile &t, int lane, int dir) {
   const int c = lane + 1;
-  bool changed = false;
+  uint32_t nd = t.need[c];
   uint32_t dmask = 0;
   for (int s = 0; s < kTile; s++) {
-    int r = dir > 0 ? 1 + s : kTile - s;
-    int rp = r - dir;
-    float cur = t.s[c][r];
-    float nv = relax_one<KIND>(t, c, r, c - 1, rp, c, rp, c + 1, rp, cur);
-    if (nv < cur) {
-      t.s[c][r] = nv;
-      dmask |= 1u << (r - 1);
-      changed = true;
+    const int r = dir > 0 ? 1 + s : kTile - s;
+    const uint32_t bit = 1u << (r - 1);
+    const bool act = (nd & bit) != 0;
+    if (!__any_sync(0xffffffffu, act)) continue;
+    uint32_t mark = 0;
+    if (act) {
+      nd &= ~bit;
+      const float cur = t.s[c][r];
+      const float nv = relax8<KIND>(t, c, r, cur);
+      if (nv < cur) {
+        t.s[c][r] = nv;
+        dmask |= bit;
+        mark = bit | (bit << 1) | (bit >> 1);
+      }
     }
+    // neighbours in this column and in the two adjacent columns
+    const uint32_t from_left = __shfl_up_sync(0xffffffffu, mark, 1);
+    const uint32_t from_right = __shfl_down_sync(0xffffffffu, mark, 1);
+    nd |= (mark & ~bit) | (lane > 0 ? from_left : 0u) | (lane < 31 ? from_right : 0u);
     __syncwarp();
   }
+  t.need[c] = nd;
   t.dirty[c] |= dmask;
   __syncwarp();
-  return __any_sync(0xffffffffu, changed);
 }
 
-// Sweep along c (lane = row).  dir = +1 right, -1 left.
+// Sweep along c (lane = row r).  dir = +1 right, -1 left.
 template <int KIND>
-__device__ bool sweep_cols(WarpTile &t, int lane, int dir) {
+__device__ void sweep_cols(WarpTile &t, int lane, int dir) {
   const int r = lane + 1;
-  bool any = false;
   for (int s = 0; s < kTile; s++) {
-    int c = dir > 0 ? 1 + s : kTile - s;
-    int cp = c - dir;
-    float cur = t.s[c][r];
-    float nv = relax_one<KIND>(t, c, r, cp, r - 1, cp, r, cp, r + 1, cur);
-    bool ch = nv < cur;
-    if (ch) t.s[c][r] = nv;
-    unsigned b = __ballot_sync(0xffffffffu, ch);
-    if (b) {
-      any = true;
-      if (lane == 0) t.dirty[c] |= b;
+    const int c = dir > 0 ? 1 + s : kTile - s;
+    const uint32_t w = t.need[c];
+    if (w == 0) continue;  // warp-uniform (shared word)
+    const bool act = (w >> lane) & 1u;
+    bool ch = false;
+    if (act) {
+      const float cur = t.s[c][r];
+      const float nv = relax8<KIND>(t, c, r, cur);
+      ch = nv < cur;
+      if (ch) t.s[c][r] = nv;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, ch);
+    __syncwarp();
+    if (lane == 0) {
+      // every marked pixel of column c was evaluated in this step; pixels next
+      // to one that changed (in this column and the two adjacent ones) must
+      // be evaluated again
+      const uint32_t d3 = b | (b << 1) | (b >> 1);
+      t.need[c] = (b << 1) | (b >> 1);
+      if (c > 1) t.need[c - 1] |= d3;
+      if (c < kTile) t.need[c + 1] |= d3;
+      t.dirty[c] |= b;
     }
     __syncwarp();
   }
-  return any;
 }
 
 template <int KIND>
-__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile);
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
 
 template <int KIND>
 __global__ void __launch_bounds__(kWarps * 32)
@@ -195,7 +239,7 @@ relax_persistent_kernel(RelaxArgs a) {
         got = __shfl_sync(0xffffffffu, got, 0);
         if (!got) continue;
         did = true;
-        relax_tile<KIND>(a, t, lane, tile);
+        relax_tile<KIND>(a, t, lane, tile, got);
         if (lane == 0) {
           __threadfence();
           atomicSub(&a.ctl->pending, 1);
@@ -224,55 +268,86 @@ relax_persistent_kernel(RelaxArgs a) {
 
 // Relaxes one tile to its local fixpoint and marks changed neighbours dirty.
 template <int KIND>
-__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile) {
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
   {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
 
-    // Stage tile + halo.  Lane r loads row r (and lanes 0,1 rows 32,33).
-    for (int c = 0; c < kHalo; c++) {
-      int64_t j = j0 - 1 + c;
-      bool jok = j >= 0 && j < a.n;
-      uint32_t flo = 0, fhi = 0;
-      for (int half = 0; half < 2; half++) {
-        int r = lane + half * 32;
-        bool act = r < kHalo;
-        int64_t i = i0 - 1 + r;
-        bool ok = act && jok && i >= 0 && i < a.m;
-        float sv = INFINITY, av = (KIND == FILL) ? INFINITY : 0.0f;
-        bool fl = false;
-        if (ok) {
-          int64_t p = j * a.m + i;
-          sv = __ldcg(&a.state[p]);  // L2: other SMs update it concurrently
-          av = a.aux[p];
-          if (KIND == GWDT) fl = (a.flats[p] & 1) != 0;
+    // Stage tile + halo.  Lane r loads row r (and lanes 0, 1 rows 32, 33).
+    // Loads are issued a chunk of columns at a time into registers before
+    // any of them is consumed, so one visit waits for a few memory latencies
+    // instead of one per column.
+    constexpr int kChunk = 9;  // 34 columns = 9 + 9 + 9 + 7
+    const int r_lo = lane, r_hi = lane + 32;
+    const int64_t i_lo = i0 - 1 + r_lo, i_hi = i0 - 1 + r_hi;
+    const bool ilo_ok = i_lo >= 0 && i_lo < a.m;
+    const bool ihi_ok = r_hi < kHalo && i_hi < a.m;
+    for (int c0 = 0; c0 < kHalo; c0 += kChunk) {
+      float s_lo[kChunk], a_lo[kChunk], s_hi[kChunk], a_hi[kChunk];
+      int f_lo[kChunk], f_hi[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; u++) {
+        const int c = c0 + u;
+        const int64_t j = j0 - 1 + c;
+        const bool jok = c < kHalo && j >= 0 && j < a.n;
+        s_lo[u] = INFINITY;
+        a_lo[u] = (KIND == FILL) ? INFINITY : 0.0f;
+        s_hi[u] = INFINITY;
+        a_hi[u] = (KIND == FILL) ? INFINITY : 0.0f;
+        f_lo[u] = 0;
+        f_hi[u] = 0;
+        if (jok && ilo_ok) {
+          const int64_t p = j * a.m + i_lo;
+          s_lo[u] = __ldcg(&a.state[p]);  // L2: other SMs update it concurrently
+          a_lo[u] = a.aux[p];
+          if (KIND == GWDT) f_lo[u] = a.flats[p];
         }
-        if (act) {
-          t.s[c][r] = sv;
-          t.a[c][r] = av;
-        }
-        if (KIND == GWDT) {
-          unsigned b = __ballot_sync(0xffffffffu, fl);
-          if (half == 0) flo = b; else fhi = b;
+        if (jok && ihi_ok) {
+          const int64_t p = j * a.m + i_hi;
+          s_hi[u] = __ldcg(&a.state[p]);
+          a_hi[u] = a.aux[p];
+          if (KIND == GWDT) f_hi[u] = a.flats[p];
         }
       }
-      if (lane == 0) {
-        t.dirty[c] = 0;
-        if (KIND == GWDT) t.flat[c] = (uint64_t)flo | ((uint64_t)(fhi & 3u) << 32);
+#pragma unroll
+      for (int u = 0; u < kChunk; u++) {
+        const int c = c0 + u;
+        if (c >= kHalo) break;
+        t.s[c][r_lo] = s_lo[u];
+        t.a[c][r_lo] = a_lo[u];
+        if (r_hi < kHalo) {
+          t.s[c][r_hi] = s_hi[u];
+          t.a[c][r_hi] = a_hi[u];
+        }
+        uint32_t flo = 0, fhi = 0;
+        if (KIND == GWDT) {
+          flo = __ballot_sync(0xffffffffu, f_lo[u] & 1);
+          fhi = __ballot_sync(0xffffffffu, f_hi[u] & 1);
+        }
+        if (lane == 0) {
+          t.dirty[c] = 0;
+          t.need[c] = (mode == DIRTY_FULL || c == 1 || c == kTile) ? 0xffffffffu
+                                                                    : 0x80000001u;
+          if (KIND == GWDT) t.flat[c] = (uint64_t)flo | ((uint64_t)(fhi & 3u) << 32);
+        }
       }
     }
     __syncwarp();
 
-    int quiet = 0, sweeps = 0, k = 0;
-    while (quiet < 4 && sweeps < kMaxSweeps) {
-      bool ch;
-      switch (k) {
-        case 0: ch = sweep_rows<KIND>(t, lane, +1); break;
-        case 1: ch = sweep_rows<KIND>(t, lane, -1); break;
-        case 2: ch = sweep_cols<KIND>(t, lane, +1); break;
-        default: ch = sweep_cols<KIND>(t, lane, -1); break;
+    // Sweep until no pixel is marked for re-evaluation: the local fixpoint.
+    bool done = false;
+    int sweeps = 0, k = 0;
+    while (sweeps < kMaxSweeps) {
+      if (!__any_sync(0xffffffffu, t.need[lane + 1] != 0)) {
+        done = true;
+        break;
       }
-      quiet = ch ? 0 : quiet + 1;
+      switch (k) {
+        case 0: sweep_rows<KIND>(t, lane, +1); break;
+        case 1: sweep_rows<KIND>(t, lane, -1); break;
+        case 2: sweep_cols<KIND>(t, lane, +1); break;
+        default: sweep_cols<KIND>(t, lane, -1); break;
+      }
       k = (k + 1) & 3;
       sweeps++;
     }
@@ -303,7 +378,7 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile) 
       if ((left >> 31) & 1u) push_tile(a, ti + 1, tj - 1);
       if (right & 1u) push_tile(a, ti - 1, tj + 1);
       if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1);
-      if (quiet < 4) push_tile(a, ti, tj);  // capped: come back later
+      if (!done) push_tile(a, ti, tj, DIRTY_FULL);  // capped: come back later
     }
     __syncwarp();
   }
@@ -343,12 +418,12 @@ __global__ void negate_kernel(float *__restrict__ out, const float *__restrict__
 // Mark every tile dirty (fill starts everywhere).
 __global__ void dirty_all_kernel(int *dirty, QueueCtl *ctl, int n) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-    dirty[t] = 1;
+    dirty[t] = DIRTY_FULL;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = n;
 }
 
-// dist = 1 at presills, +INF at other flats, 0 elsewhere; enqueue every tile
-// whose pixels or halo contain a presill.
+// dist = 1 at presills, +INF at other flats, 0 elsewhere; flag every tile
+// whose pixels or halo contain a presill (plain stores: idempotent).
 __global__ void gwdt_init_kernel(float *__restrict__ dist,
                                  const int32_t *__restrict__ flats, int64_t m,
                                  int64_t n, RelaxArgs qa) {
@@ -364,9 +439,21 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
       int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
       int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
       for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) mark_dirty(qa, tj * qa.tm + ti);
+        for (int ti = ti0; ti <= ti1; ti++) {
+          int *fl = &qa.dirty[tj * qa.tm + ti];
+          if (*fl == 0) *fl = DIRTY_FULL;
+        }
     }
   }
+}
+
+// pending = number of flagged tiles (the persistent launch starts after).
+__global__ void count_dirty_kernel(const int *__restrict__ dirty, int n, QueueCtl *ctl) {
+  int c = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    c += dirty[t] != 0;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctl->pending, c);
 }
 
 // A valid back-link for every reached flat: the first flat neighbour u (in
@@ -435,6 +522,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats,
               g.m, g.n, ra);
+    TT_LAUNCH(count_dirty_kernel, std::min(tgrid, sm_count() * 4), 256, 0, st, dirty, T, ctl);
   }
   TT_CHECK(cudaGetLastError());
   static int blocks_per_sm[2] = {0, 0};

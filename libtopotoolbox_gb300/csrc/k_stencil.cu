@@ -35,14 +35,24 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
 
-  for (int c = ty; c < kFH; c += kBlockY) {
-    int64_t j = j0 - 2 + c;
-    for (int r = tx; r < kFH; r += kBlockX) {
-      int64_t i = i0 - 2 + r;
-      float v = NAN;
-      if (i >= 0 && i < m && j >= 0 && j < n) v = dem[j * m + i];
-      z[c][r] = v;
-    }
+  {  // stage the DEM: all loads in flight before the first shared store
+    constexpr int kC = (kFH + kBlockY - 1) / kBlockY;
+    float v[kC][2];
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
+        v[k][h] = (c < kFH && r < kFH && i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : NAN;
+      }
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        if (c < kFH && r < kFH) z[c][r] = v[k][h];
+      }
   }
   __syncthreads();
 
@@ -127,22 +137,38 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
-  for (int c = ty; c < kTile + 2; c += kBlockY) {
-    int64_t j = j0 - 1 + c;
-    for (int r = tx; r < kTile + 2; r += kBlockX) {
-      int64_t i = i0 - 1 + r;
-      float a = NAN, b = NAN;
-      uint8_t f = 0;
-      if (i >= 0 && i < m && j >= 0 && j < n) {
-        int64_t p = j * m + i;
-        a = dem[p];
-        b = dist[p];
-        f = (uint8_t)(flats[p] & 1);
+  {  // stage dem, dist and flats with every load in flight at once
+    constexpr int kH = kTile + 2;
+    constexpr int kC = (kH + kBlockY - 1) / kBlockY;
+    float va[kC][2], vb[kC][2];
+    int vf[kC][2];
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+        va[k][h] = NAN;
+        vb[k][h] = NAN;
+        vf[k][h] = 0;
+        if (c < kH && r < kH && i >= 0 && i < m && j >= 0 && j < n) {
+          const int64_t p = j * m + i;
+          va[k][h] = dem[p];
+          vb[k][h] = dist[p];
+          vf[k][h] = flats[p];
+        }
       }
-      zs[c][r] = a;
-      ds[c][r] = b;
-      fs[c][r] = f;
-    }
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        if (c < kH && r < kH) {
+          zs[c][r] = va[k][h];
+          ds[c][r] = vb[k][h];
+          fs[c][r] = (uint8_t)(vf[k][h] & 1);
+        }
+      }
   }
   __syncthreads();
   const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
@@ -297,12 +323,24 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
-  for (int c = ty; c < kHS; c += kBlockY) {
-    int64_t j = j0 - 2 + c;
-    for (int r = tx; r < kHS; r += kBlockX) {
-      int64_t i = i0 - 2 + r;
-      z[c][r] = (i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : 0.0f;
-    }
+  {  // stage the DEM with every load in flight at once
+    constexpr int kC = (kHS + kBlockY - 1) / kBlockY;
+    float v[kC][2];
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
+        v[k][h] = (c < kHS && r < kHS && i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : 0.0f;
+      }
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        if (c < kHS && r < kHS) z[c][r] = v[k][h];
+      }
   }
   __syncthreads();
   if (MODE == 2) {
