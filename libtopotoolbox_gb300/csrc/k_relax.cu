@@ -218,6 +218,8 @@ relax_persistent_kernel(RelaxArgs a) {
   long long idle = 0;
   for (;;) {
     if (*(volatile int *)&a.ctl->abort) break;
+    if (lane == 0 && *(volatile unsigned long long *)&a.ctl->visits >= a.max_visits)
+      atomicOr(&a.ctl->abort, ABORT_VISITS);
     bool did = false;
     for (int base = wid; base < T; base += W * 32) {
       const int mine = base + lane * W;
@@ -231,8 +233,7 @@ relax_persistent_kernel(RelaxArgs a) {
         if (lane == 0) {
           got = atomicExch(&a.dirty[tile], 0);
           if (got) {
-            if (atomicAdd(&a.ctl->visits, 1ULL) >= a.max_visits)
-              atomicOr(&a.ctl->abort, ABORT_VISITS);
+            atomicAdd(&a.ctl->visits, 1ULL);  // no return: no round trip
             __threadfence();
           }
         }
@@ -368,17 +369,21 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
     }
     __threadfence();  // publish this lane's writes before any push below
     __syncwarp();
-    if (lane == 0) {
-      uint32_t left = t.dirty[1], right = t.dirty[kTile];
-      if (top) push_tile(a, ti - 1, tj);
-      if (bottom) push_tile(a, ti + 1, tj);
-      if (left) push_tile(a, ti, tj - 1);
-      if (right) push_tile(a, ti, tj + 1);
-      if (left & 1u) push_tile(a, ti - 1, tj - 1);
-      if ((left >> 31) & 1u) push_tile(a, ti + 1, tj - 1);
-      if (right & 1u) push_tile(a, ti - 1, tj + 1);
-      if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1);
-      if (!done) push_tile(a, ti, tj, DIRTY_FULL);  // capped: come back later
+    {  // lanes 0..8 mark one neighbour each, concurrently
+      const uint32_t left = t.dirty[1], right = t.dirty[kTile];
+      switch (lane) {
+        case 0: if (top) push_tile(a, ti - 1, tj); break;
+        case 1: if (bottom) push_tile(a, ti + 1, tj); break;
+        case 2: if (left) push_tile(a, ti, tj - 1); break;
+        case 3: if (right) push_tile(a, ti, tj + 1); break;
+        case 4: if (left & 1u) push_tile(a, ti - 1, tj - 1); break;
+        case 5: if ((left >> 31) & 1u) push_tile(a, ti + 1, tj - 1); break;
+        case 6: if (right & 1u) push_tile(a, ti - 1, tj + 1); break;
+        case 7: if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1); break;
+        case 8: if (!done) push_tile(a, ti, tj, DIRTY_FULL); break;  // capped
+        default: break;
+      }
+      __threadfence();  // the pending increments land before the owner's decrement
     }
     __syncwarp();
   }

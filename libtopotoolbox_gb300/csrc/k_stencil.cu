@@ -63,17 +63,19 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
       int64_t i = i0 - 1 + r;
       uint8_t f = 0;
       if (i >= 1 && i < m - 1 && j >= 1 && j < n - 1) {
-        float zc = z[c + 1][r + 1];
-        float lo = zc;
+        // flat: no neighbour lower, NaN neighbours counting as -INF
+        const float zc = z[c + 1][r + 1];
+        bool lower = false;
 #pragma unroll
         for (int dc = -1; dc <= 1; dc++)
 #pragma unroll
           for (int dr = -1; dr <= 1; dr++) {
             if (dc == 0 && dr == 0) continue;
-            float zn = z[c + 1 + dc][r + 1 + dr];
-            lo = fminf(lo, isnan(zn) ? -INFINITY : zn);
+            const float zn = z[c + 1 + dc][r + 1 + dr];
+            // a NaN neighbour counts as -INF (src/identifyflats.c:64)
+            lower |= (zn < zc) | ((zn != zn) & (zc != -INFINITY));
           }
-        f = (zc == lo) ? 1 : 0;
+        f = (!lower && zc == zc) ? 1 : 0;
       }
       flat[c][r] = f;
     }
@@ -81,28 +83,24 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
   __syncthreads();
 
   unsigned local = 0;
+  // Pixels outside the grid hold NaN, which never compares equal, so the
+  // gather needs no bounds checks.
   for (int c = ty; c < kTile; c += kBlockY) {
-    int64_t j = j0 + c;
-    if (j >= n) break;
-    int r = tx;
-    int64_t i = i0 + r;
-    if (i >= m) continue;
-    float zc = z[c + 2][r + 2];
-    int fc = flat[c + 1][r + 1];
-    int32_t v = fc;
+    const int64_t j = j0 + c;
+    const int r = tx;
+    const int64_t i = i0 + r;
+    if (j >= n || i >= m) continue;
+    const float zc = z[c + 2][r + 2];
+    const int fc = flat[c + 1][r + 1];
     bool hit = false;
 #pragma unroll
     for (int dc = -1; dc <= 1; dc++)
 #pragma unroll
       for (int dr = -1; dr <= 1; dr++) {
         if (dc == 0 && dr == 0) continue;
-        int64_t ni = i + dr, nj = j + dc;
-        if (ni < 0 || ni >= m || nj < 0 || nj >= n) continue;
-        int fn = flat[c + 1 + dc][r + 1 + dr];
-        if (fn != fc && z[c + 2 + dc][r + 2 + dr] == zc) hit = true;
+        hit |= (flat[c + 1 + dc][r + 1 + dr] != fc) & (z[c + 2 + dc][r + 2 + dr] == zc);
       }
-    if (hit) v |= fc ? 4 : 2;
-    out[j * m + i] = v;
+    out[j * m + i] = fc | (hit ? (fc ? 4 : 2) : 0);
     local += fc;
   }
   // Block reduction of the flat count.
@@ -298,16 +296,9 @@ __device__ __forceinline__ F2 axis_diff_f2(float zm2, float zm1, float z0,
 
 struct Sun2 {
   float sxh, sxl, syh, syl, szh, szl;
+  float rh, rl;  // 1 / (2 * cellsize) as float-float
 };
 
-// H = (-dx*sx - dy*sy + sz) / sqrt(dx^2 + dy^2 + 1), in float-float.
-__device__ __forceinline__ float shade_f2(F2 dx, F2 dy, const Sun2 &s) {
-  F2 num = f2_add(f2_add(f2_mul(dx, F2{-s.sxh, -s.sxl}), f2_mul(dy, F2{-s.syh, -s.syl})),
-                  F2{s.szh, s.szl});
-  F2 q = f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), F2{1.0f, 0.0f});
-  F2 h = f2_div(num, f2_sqrt(q));
-  return __fadd_rn(h.hi, h.lo);
-}
 
 constexpr int kHS = kTile + 4;  // 2-pixel halo for one-sided borders
 
@@ -391,13 +382,24 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
       float dy = axis_grad(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
                            z[cc + 2][r], j, n, twoh);
       if (MODE == 0) {
-        float h = shade(dx, dy, sx, sy, sz);
-        if (isfinite(dx) && isfinite(dy) && isfinite(h)) {
-          F2 ex = f2_divf(axis_diff_f2(z[cc][r - 2], z[cc][r - 1], z[cc][r], z[cc][r + 1],
-                                       z[cc][r + 2], i, m), twoh);
-          F2 ey = f2_divf(axis_diff_f2(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
-                                       z[cc + 2][r], j, n), twoh);
-          h = shade_f2(ex, ey, s2);
+        float h;
+        if (isfinite(dx) && isfinite(dy)) {
+          // Only the numerator -dx*sx - dy*sy + sz cancels; it is carried in
+          // float-float from the exact stencil differences.  The rest is one
+          // rounded square root and one division (a few ulps, no
+          // cancellation).
+          const F2 ex = f2_mul(axis_diff_f2(z[cc][r - 2], z[cc][r - 1], z[cc][r], z[cc][r + 1],
+                                            z[cc][r + 2], i, m), F2{s2.rh, s2.rl});
+          const F2 ey = f2_mul(axis_diff_f2(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
+                                            z[cc + 2][r], j, n), F2{s2.rh, s2.rl});
+          const F2 num = f2_add(f2_add(f2_mul(ex, F2{-s2.sxh, -s2.sxl}),
+                                       f2_mul(ey, F2{-s2.syh, -s2.syl})),
+                                F2{s2.szh, s2.szl});
+          const float q = __fmaf_rn(ex.hi, ex.hi, __fmaf_rn(ey.hi, ey.hi, 1.0f));
+          h = __fdiv_rn(__fadd_rn(num.hi, num.lo), __fsqrt_rn(q));
+          if (!isfinite(h)) h = shade(dx, dy, sx, sy, sz);
+        } else {
+          h = shade(dx, dy, sx, sy, sz);  // NaN / INF exactly as the reference
         }
         out0[p] = h;
       } else {
@@ -494,8 +496,10 @@ tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
   double dsx = std::sin(zen) * std::cos((double)azimuth);
   double dsy = std::sin(zen) * std::sin((double)azimuth);
   double dsz = std::cos(zen);
+  const double rinv = 1.0 / (2.0 * (double)cellsize);
+  const float rh = (float)rinv;
   Sun2 s2{sx, (float)(dsx - (double)sx), sy, (float)(dsy - (double)sy),
-          sz, (float)(dsz - (double)sz)};
+          sz, (float)(dsz - (double)sz), rh, (float)(rinv - (double)rh)};
   TT_LAUNCH(hillshade_kernel<0>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
             out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz, s2);
   TT_CHECK(cudaGetLastError());
