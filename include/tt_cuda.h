@@ -257,6 +257,36 @@ TT_CUDA_API tt_cuda_status tt_cuda_d8_pipeline_dev(
     const uint8_t *bc, const float *weights, float azimuth, float altitude,
     float cellsize, const ptrdiff_t dims[2], void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Batched form (no counterpart in the reference)                       */
+/* ------------------------------------------------------------------ */
+
+/** A batch of independent DEMs run through fillsinks -> identifyflats ->
+ *  gwdt_computecosts -> gwdt -> flow_routing_d8_carve (directions) ->
+ *  flow_accumulation (unit weights) with one launch per stage over the whole
+ *  batch.  The DEMs are packed into one mosaic with NaN gutters, which every
+ *  stage treats exactly like the grid edge, so each DEM's results equal a
+ *  separate call (finite DEMs).  The first run with a given set of pointers
+ *  executes the sequence and captures it in a CUDA graph; later runs with
+ *  the same pointers replay the graph. */
+typedef struct tt_cuda_batch tt_cuda_batch;
+/** `dims` holds count pairs {nrows, ncols}.  `canvas_cols` is the mosaic
+ *  width in columns (0 picks one from the total area). */
+TT_CUDA_API tt_cuda_status tt_cuda_batch_create(int count, const ptrdiff_t *dims,
+                                                int64_t canvas_cols,
+                                                tt_cuda_batch **out);
+/** info[0..3] = canvas rows, canvas columns, DEM pixels, graph nodes. */
+TT_CUDA_API tt_cuda_status tt_cuda_batch_info(const tt_cuda_batch *batch,
+                                              int64_t *info);
+/** Device pointers, one per DEM, in host arrays of length count; an output
+ *  array may be NULL to skip that output.  Runs on an internal stream
+ *  ordered after `stream` and returns when the results are written. */
+TT_CUDA_API tt_cuda_status tt_cuda_batch_run(
+    tt_cuda_batch *batch, const float *const *dem, const uint8_t *const *bc,
+    float *const *filled, int32_t *const *flats, float *const *dist,
+    uint8_t *const *direction, float *const *acc, void *stream);
+TT_CUDA_API void tt_cuda_batch_destroy(tt_cuda_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,11 @@ SIGNATURES = {
     "tt_cuda_hillshade_fused_dev": (ST, [P, P, F, F, F, PD, P]),
     "tt_cuda_hillshade_backward_dev": (ST, [P, P, P, F, F, F, PD, P]),
     "tt_cuda_d8_pipeline_dev": (ST, [P, P, P, P, P, P, P, P, P, P, F, F, F, PD, P]),
+    # batched form
+    "tt_cuda_batch_create": (ST, [C.c_int, PD, I64, C.POINTER(P)]),
+    "tt_cuda_batch_info": (ST, [P, C.POINTER(I64)]),
+    "tt_cuda_batch_run": (ST, [P, P, P, P, P, P, P, P, P]),
+    "tt_cuda_batch_destroy": (None, [P]),
 }
 
 STATUS = {

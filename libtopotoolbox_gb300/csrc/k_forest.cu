@@ -163,7 +163,7 @@ struct UpTile {
   int bad;
 };
 
-__global__ void __launch_bounds__(kUpThreads) forest_up_kernel(UpArgs a) {
+__global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
   __shared__ UpTile t;
   const int tid = threadIdx.x;
   const int T = a.tm * a.tn;
@@ -232,16 +232,20 @@ __global__ void __launch_bounds__(kUpThreads) forest_up_kernel(UpArgs a) {
     if (bad) t.bad = 1;
     __syncthreads();
 
-    // Pointer jumping (paths inside a tile are shorter than 1024 steps).
+    // Pointer jumping (paths inside a tile are shorter than 1024 steps);
+    // stops as soon as every pixel points at its terminal.
     for (int round = 0; round < 10; round++) {
+      int moved = 0;
       for (int e = tid; e < kTileCells; e += kUpThreads) {
         const uint32_t v = t.pk[e];
         const int q = (int)(v >> 16);
         if (q == e) continue;
         const uint32_t w = t.pk[q];
+        if ((int)(w >> 16) == q) continue;  // q is the terminal already
         t.pk[e] = (w & 0xffff0000u) | ((v & 0xffffu) + (w & 0xffffu));
+        moved = 1;
       }
-      __syncthreads();
+      if (!__syncthreads_or(moved)) break;
     }
     int cyc = 0, md = 0;
     for (int e = tid; e < kTileCells; e += kUpThreads) {
@@ -276,13 +280,40 @@ __global__ void __launch_bounds__(kUpThreads) forest_up_kernel(UpArgs a) {
     }
     __syncthreads();
     // After the scatter cnt[d] is the end of level d = the start of level d-1.
-    for (int d = maxd; d >= 1; d--) {
-      const int beg = d == maxd ? 0 : t.cnt[d + 1], end = t.cnt[d];
-      for (int k = beg + tid; k < end; k += kUpThreads) {
-        const int p = t.order[k];
-        const int q = t.rl[p];
-        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
-        if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
+    // Levels of at most 32 pixels (the long, thin chains of carved flats) run
+    // on warp 0 alone with warp barriers; wider levels use the whole block.
+    {
+      bool warp_mode = false;
+      for (int d = maxd; d >= 1; d--) {
+        const int beg = d == maxd ? 0 : t.cnt[d + 1], end = t.cnt[d];
+        const bool narrow = end - beg <= 32;
+        if (!narrow && warp_mode) {
+          __syncthreads();  // the warp-0 levels are visible to every thread
+          warp_mode = false;
+        }
+        if (narrow) {
+          warp_mode = true;
+          if (tid < 32) {
+            const int k = beg + tid;
+            if (k < end) {
+              const int p = t.order[k];
+              const int q = t.rl[p];
+              if (a.want_acc)
+                atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
+              if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
+            }
+            __syncwarp();
+          }
+        } else {
+          for (int k = beg + tid; k < end; k += kUpThreads) {
+            const int p = t.order[k];
+            const int q = t.rl[p];
+            if (a.want_acc)
+              atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
+            if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
+          }
+          __syncthreads();
+        }
       }
       __syncthreads();
     }
@@ -770,6 +801,16 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
 
 // Reads the counters back and maps error bits to a status.
 tt_cuda_status up_status(UpWork &w, cudaStream_t st, int *host6) {
+  if (status_sink()) {  // deferred: ecount, processed, error bits
+    int *rec = sink_record(REC_FOREST, st);
+    if (rec) {
+      TT_CHECK(cudaMemcpyAsync(rec + 1, w.counters + 0, sizeof(int), cudaMemcpyDeviceToDevice, st));
+      TT_CHECK(cudaMemcpyAsync(rec + 2, w.counters + 2, sizeof(int), cudaMemcpyDeviceToDevice, st));
+      TT_CHECK(cudaMemcpyAsync(rec + 3, w.counters + 4, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    }
+    for (int k = 0; k < 6; k++) host6[k] = 0;
+    return TT_CUDA_SUCCESS;
+  }
   int *h = (int *)pinned_scratch();
   if (!h) return TT_CUDA_ERR_ALLOC;
   TT_CHECK(cudaMemcpyAsync(h, w.counters, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -542,6 +542,12 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
   TT_CHECK(cudaGetLastError());
+  if (status_sink()) {  // deferred: record the abort word, no round trip
+    int *rec = sink_record(REC_RELAX, st);
+    if (rec) TT_CHECK(cudaMemcpyAsync(rec + 1, &ctl->abort, sizeof(int),
+                                      cudaMemcpyDeviceToDevice, st));
+    return TT_CUDA_SUCCESS;
+  }
   TT_CHECK(cudaMemcpyAsync(hctl, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
   // Tile visits per tile, reported as "rounds".

@@ -43,15 +43,15 @@ inline GridDims make_dims(const ptrdiff_t dims[2]) {
 // D8 neighbour offsets in the bit order of include/topotoolbox.h:807-816,
 // for column-major (order 0) arrays: bit k points to (i + di[k], j + dj[k]).
 // Row-major (order 1) swaps the two tables (src/flow_routing.c:39-49).
-__host__ __device__ inline int d8_di(int k, unsigned order) {
-  const int a[8] = {0, 1, 1, 1, 0, -1, -1, -1};
-  const int b[8] = {1, 1, 0, -1, -1, -1, 0, 1};
-  return (order & 1) ? b[k] : a[k];
+// The two offset tables {0,1,1,1,0,-1,-1,-1} and {1,1,0,-1,-1,-1,0,1}, stored
+// as 2-bit fields (offset + 1) so a data-dependent k needs no memory lookup.
+constexpr unsigned kD8A = 0x1A9u;   // {0,1,1,1,0,-1,-1,-1} + 1
+constexpr unsigned kD8B = 0x901Au;  // {1,1,0,-1,-1,-1,0,1} + 1
+__host__ __device__ __forceinline__ int d8_di(int k, unsigned order) {
+  return (int)((((order & 1) ? kD8B : kD8A) >> (2 * k)) & 3u) - 1;
 }
-__host__ __device__ inline int d8_dj(int k, unsigned order) {
-  const int a[8] = {0, 1, 1, 1, 0, -1, -1, -1};
-  const int b[8] = {1, 1, 0, -1, -1, -1, 0, 1};
-  return (order & 1) ? a[k] : b[k];
+__host__ __device__ __forceinline__ int d8_dj(int k, unsigned order) {
+  return (int)((((order & 1) ? kD8A : kD8B) >> (2 * k)) & 3u) - 1;
 }
 
 // Index of the highest set bit, as the reference decodes a direction byte
@@ -98,7 +98,26 @@ class Workspace {
   size_t used_ = 0;
 };
 
-Workspace &workspace();          // of the current device
+// Deferred status (used while a batch is captured into a CUDA graph): when a
+// sink is set, stages record their status words into it with device copies
+// instead of reading them back and synchronising the stream.  Each record is
+// kRecordInts ints: {kind, a, b, c}.
+constexpr int kRecordInts = 4;
+enum : int { REC_RELAX = 1, REC_FOREST = 2 };
+struct StatusSink {
+  int *dev;      // device array of records
+  int capacity;  // records
+  int next;      // next free record
+};
+StatusSink *status_sink();               // nullptr unless deferring
+void set_status_sink(StatusSink *sink);  // per thread
+// Reserves a record and returns its device address, or nullptr when full.
+int *sink_record(int kind, cudaStream_t st);
+
+Workspace &workspace();          // of the current device (or the override)
+// While set, workspace() returns `ws` on this thread (a batch keeps its own
+// workspace so that addresses captured in its CUDA graph stay valid).
+void set_workspace_override(Workspace *ws);
 void *pinned_scratch();          // 4 KiB of pinned host memory per device
 int64_t max_rounds();
 void set_last_rounds(int64_t r);

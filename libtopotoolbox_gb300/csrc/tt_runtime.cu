@@ -16,6 +16,8 @@ namespace {
 thread_local tt_cuda_status g_status = TT_CUDA_SUCCESS;
 thread_local int64_t g_launches = 0;
 thread_local int64_t g_last_rounds = 0;
+thread_local StatusSink *g_sink = nullptr;
+thread_local Workspace *g_ws_override = nullptr;
 int64_t g_max_rounds_override = 0;
 
 constexpr int kMaxDevices = 64;
@@ -41,6 +43,20 @@ void set_status(tt_cuda_status s) { g_status = s; }
 tt_cuda_status get_status() { return g_status; }
 void note_launch(int count) { g_launches += count; }
 void set_last_rounds(int64_t r) { g_last_rounds = r; }
+
+StatusSink *status_sink() { return g_sink; }
+void set_status_sink(StatusSink *sink) { g_sink = sink; }
+
+int *sink_record(int kind, cudaStream_t st) {
+  StatusSink *s = g_sink;
+  if (!s || s->next >= s->capacity) return nullptr;
+  int *rec = s->dev + (size_t)s->next * kRecordInts;
+  s->next++;
+  // the kind word is written by a kernel-free memset of its low byte
+  cudaMemsetAsync(rec, 0, kRecordInts * sizeof(int), st);
+  cudaMemsetAsync(rec, kind, 1, st);
+  return rec;
+}
 
 bool cuda_ok(cudaError_t e, const char *what) {
   if (e == cudaSuccess) return true;
@@ -89,7 +105,10 @@ void Workspace::release() {
   cap_ = used_ = 0;
 }
 
-Workspace &workspace() { return g_dev[current_device()].scratch; }
+Workspace &workspace() {
+  return g_ws_override ? *g_ws_override : g_dev[current_device()].scratch;
+}
+void set_workspace_override(Workspace *ws) { g_ws_override = ws; }
 static Workspace &io_workspace() { return g_dev[current_device()].io; }
 
 void *pinned_scratch() {

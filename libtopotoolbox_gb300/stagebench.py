@@ -24,7 +24,8 @@ BYTES = {
 }
 STAGES = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
           "flow_routing_d8_carve", "flow_accumulation", "flow_accumulation_weighted",
-          "flow_accumulation_backward", "hillshade_fused", "hillshade_backward", "pipeline"]
+          "flow_accumulation_backward", "hillshade_fused", "hillshade_backward", "pipeline",
+          "batch"]
 
 
 def load(workload, size):
@@ -42,6 +43,69 @@ def load(workload, size):
     return dem, bc, w, cs
 
 
+def batch_main(args):
+    """Batched workload: `--tiles` DEMs (sides log-uniform 128..2048, aspect
+    0.5..2, quantised to 0.1 m) through one tuned mosaic and a CUDA graph,
+    against the same DEMs through per-DEM device calls."""
+    import time
+
+    import torch
+
+    from . import dems as D
+    from .api import dev
+    from .batch import Batch, tune
+
+    t0 = time.perf_counter()
+    tiles = D.batch_tiles(count=args.tiles)
+    gen_s = time.perf_counter() - t0
+    dv = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dv)  # noqa: E731
+    dems = [t(d) for d, _ in tiles]
+    bcs = [t(b) for _, b in tiles]
+    shapes = [d.shape for d, _ in tiles]
+    cells = sum(a * b for a, b in shapes)
+    best, cands = tune(shapes, dems, bcs, reps=2)
+    bt = Batch(shapes)
+    out = bt.run(dems, bcs)
+    torch.cuda.synchronize()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            a, b = ev(), ev()
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    batched_ms = timed(lambda: bt.run(dems, bcs, outputs=out), args.reps)
+
+    def per_dem():
+        for d, b in zip(dems, bcs):
+            filled = dev.fillsinks(d, b)
+            flats = dev.identifyflats(filled)
+            costs, _ = dev.gwdt_computecosts(flats, d, filled)
+            dist = dev.gwdt(costs, flats)
+            _, direction = dev.flow_routing_d8_carve(filled, dist, flats, want_node=False)
+            dev.flow_accumulation(direction)
+
+    per_dem()
+    torch.cuda.synchronize()
+    per_ms = timed(per_dem, max(1, args.reps // 2))
+    info = bt.info()
+    print(json.dumps({"stage": "batch", "tiles": len(tiles), "pixels": cells,
+                      "canvas": [info["canvas_rows"], info["canvas_cols"]],
+                      "graph_nodes": info["graph_nodes"], "batched_ms": batched_ms,
+                      "per_dem_ms": per_ms, "speedup": per_ms / batched_ms,
+                      "batched_gcells_s": cells / (batched_ms * 1e-3) / 1e9,
+                      "per_dem_gcells_s": cells / (per_ms * 1e-3) / 1e9,
+                      "tuning": cands, "generate_s": gen_s}))
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="plain_4096",
@@ -49,7 +113,10 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--stage", default="pipeline", choices=STAGES)
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--tiles", type=int, default=512, help="DEMs for --stage batch")
     args = ap.parse_args(argv)
+    if args.stage == "batch":
+        return batch_main(args)
 
     import torch
 
