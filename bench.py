@@ -159,6 +159,125 @@ def cpu_baseline_sample(dem, bc, seconds_target=20.0):
                       f"{el:.1f} s"}
 
 
+def adjoint_leg(dev, reps=5):
+    """Forward vs forward + adjoint of weighted accumulation (and hillshade) on
+    the 8192 x 8192 differentiation workload, with the gradient's relative
+    error against the FP64 adjoint oracle."""
+    import torch
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    from libtopotoolbox_gb300 import dems
+    from libtopotoolbox_gb300.api import dev as D
+
+    dem, bc, w, cs = dems.grad_8192()
+    m, n = dem.shape
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)  # noqa: E731
+    d_dem, d_bc, d_w = t(dem), t(bc), t(w)
+    o = D.d8_pipeline(d_dem, d_bc)
+    direction, node = o["direction"], o["node"]
+    acc = D.flow_accumulation(direction, d_w)
+    torch.cuda.synchronize()
+    acc_h = acc.cpu().numpy().T
+    dir_h = direction.cpu().numpy().T
+    rng = np.random.default_rng(64)
+    outl = np.nonzero((dir_h.ravel(order="F") == 0) &
+                      (acc_h.ravel(order="F") > np.median(acc_h)))[0]
+    sel = rng.choice(outl, size=min(64, outl.size), replace=False)
+    target = acc_h.ravel(order="F")[sel].astype(np.float64) * rng.uniform(0.5, 1.5, sel.size)
+    g = np.zeros(m * n, np.float32)
+    g[sel] = (2.0 * (acc_h.ravel(order="F")[sel] - target)).astype(np.float32)
+    d_g = torch.from_numpy(g.reshape(n, m)).to(dev)
+    gbar = torch.rand_like(d_dem) * 2 - 1
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    fwd = timed(lambda: D.flow_accumulation(direction, d_w, out=acc))
+    gw = torch.empty_like(acc)
+    adj = timed(lambda: D.flow_accumulation_backward(direction, d_g, out=gw))
+    hs = torch.empty_like(d_dem)
+    hfwd = timed(lambda: D.hillshade_fused(d_dem, HS_AZ, HS_ALT, cs, out=hs))
+    hg = torch.empty_like(d_dem)
+    hadj = timed(lambda: D.hillshade_backward(d_dem, gbar, HS_AZ, HS_ALT, cs, out=hg))
+    # FP64 adjoint oracle along the same receivers
+    orc = pyoracle.Oracle("port")
+    node_h = node.cpu().numpy().T
+    g64 = orc.flow_accumulation_backward_f64(node_h, dir_h, g.reshape(m, n, order="F"))
+    got = gw.cpu().numpy().T
+    nrm = float(np.linalg.norm(got - g64) / max(np.linalg.norm(g64), 1e-300))
+    mx = float(np.max(np.abs(got - g64)) / max(np.max(np.abs(g64)), 1e-300))
+    a64 = orc.flow_accumulation_f64(node_h, dir_h, w)
+    fwd_err = float(np.max(np.abs(acc_h - a64) / np.abs(a64)))
+    return {"workload": f"grad_8192 ({m}x{n}, lognormal(0,0.5) weights, 64 outlets)",
+            "acc_fwd_ms": fwd, "acc_adj_ms": adj, "acc_ratio": (fwd + adj) / fwd,
+            "acc_grad_rel_err_norm": nrm, "acc_grad_rel_err_max": mx,
+            "acc_fwd_rel_err_max": fwd_err,
+            "hillshade_fwd_ms": hfwd, "hillshade_adj_ms": hadj,
+            "hillshade_ratio": (hfwd + hadj) / hfwd}
+
+
+def batch_leg(dev, reps=3):
+    """512 uneven DEMs: one tuned mosaic replayed from a CUDA graph against
+    per-DEM device calls."""
+    import torch
+
+    from libtopotoolbox_gb300 import dems
+    from libtopotoolbox_gb300.api import dev as D
+    from libtopotoolbox_gb300.batch import Batch, tune
+
+    tiles = dems.batch_tiles()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)  # noqa: E731
+    dm = [t(d) for d, _ in tiles]
+    bc = [t(b) for _, b in tiles]
+    shapes = [d.shape for d, _ in tiles]
+    cells = sum(a * b for a, b in shapes)
+    best, cands = tune(shapes, dm, bc, reps=1)
+    bt = Batch(shapes)
+    out = bt.run(dm, bc)
+    torch.cuda.synchronize()
+
+    def timed(fn, k):
+        ts = []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    batched = timed(lambda: bt.run(dm, bc, outputs=out), reps)
+
+    def per_dem():
+        for d, b in zip(dm, bc):
+            f = D.fillsinks(d, b)
+            fl = D.identifyflats(f)
+            c, _ = D.gwdt_computecosts(fl, d, f)
+            ds = D.gwdt(c, fl)
+            _, dr = D.flow_routing_d8_carve(f, ds, fl, want_node=False)
+            D.flow_accumulation(dr)
+
+    per_dem()
+    per = timed(per_dem, 1)
+    info = bt.info()
+    bt.close()
+    return {"workload": f"{len(tiles)} DEMs, sides log-uniform 128..2048, {cells} pixels",
+            "batched_ms": batched, "per_dem_ms": per, "speedup": per / batched,
+            "batched_gcells_s": cells / (batched * 1e-3) / 1e9,
+            "canvas": [info["canvas_rows"], info["canvas_cols"]],
+            "graph_nodes": info["graph_nodes"], "tuned_canvas_cols": best["canvas_cols"]}
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -221,6 +340,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="plain_4096_hillshade", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -396,6 +517,10 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(dev)
+    if not args.no_batch:
+        line["batched"] = batch_leg(dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
     print(json.dumps(line), flush=True)

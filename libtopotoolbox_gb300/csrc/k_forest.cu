@@ -575,65 +575,82 @@ struct DownTile {
   int16_t last[2][kTileCells];
 };
 
-__global__ void __launch_bounds__(32) forest_down_kernel(DownArgs a) {
+constexpr int kDownThreads = 128;
+
+__global__ void __launch_bounds__(kDownThreads) forest_down_kernel(DownArgs a) {
   __shared__ DownTile t;
-  const int lane = threadIdx.x;
+  const int tid = threadIdx.x;
   const int T = a.tm * a.tn;
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-    load_dir_tile(t.dir, a.dir, a.m, a.n, i0, j0, lane);
-    __syncwarp();
-    const int ii = lane;
-    const int64_t i = i0 + ii;
-    int bad = 0;
-    for (int jj = 0; jj < kTile; jj++) {
-      const int64_t j = j0 + jj;
-      const int loc = jj * kTile + ii;
-      int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
-      if (rl == RL_BADDIR) bad = 1;
-      t.rl[loc] = (int16_t)rl;
-      t.hi[0][loc] = (rl != RL_NONE) ? a.g[j * a.m + i] : 0.0f;
-      t.lo[0][loc] = 0.0f;
-      t.nx[0][loc] = (int16_t)(rl >= 0 ? rl : -1);
-      t.last[0][loc] = (int16_t)loc;
+    {  // stage the directions with every load in flight at once
+      constexpr int kL = (kHalo * kHalo + kDownThreads - 1) / kDownThreads;
+      uint8_t v[kL];
+#pragma unroll
+      for (int u = 0; u < kL; u++) {
+        const int e = tid + u * kDownThreads;
+        const int c = e / kHalo, r = e % kHalo;
+        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+        v[u] = (e < kHalo * kHalo && i >= 0 && i < a.m && j >= 0 && j < a.n) ? a.dir[j * a.m + i] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kL; u++) {
+        const int e = tid + u * kDownThreads;
+        if (e < kHalo * kHalo) t.dir[e / kHalo][e % kHalo] = v[u];
+      }
     }
-    if (bad) atomicOr(a.err, ERR_BADDIR);
-    __syncwarp();
+    __syncthreads();
+    int bad = 0;
+    for (int e = tid; e < kTileCells; e += kDownThreads) {
+      const int ii = e % kTile, jj = e / kTile;
+      const int64_t i = i0 + ii, j = j0 + jj;
+      const int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
+      bad |= rl == RL_BADDIR;
+      t.rl[e] = (int16_t)rl;
+      t.hi[0][e] = (rl != RL_NONE) ? a.g[j * a.m + i] : 0.0f;
+      t.lo[0][e] = 0.0f;
+      t.nx[0][e] = (int16_t)(rl >= 0 ? rl : -1);
+      t.last[0][e] = (int16_t)e;
+    }
+    if (__syncthreads_or(bad) && tid == 0) atomicOr(a.err, ERR_BADDIR);
+    // Synchronous pointer jumping (double buffered): sum of g from each pixel
+    // to the end of its in-tile path, and that end pixel.
     int cur = 0;
     for (int round = 0; round < 10; round++) {
-      for (int jj = 0; jj < kTile; jj++) {
-        const int loc = jj * kTile + ii;
-        int q = t.nx[cur][loc];
-        FF v{t.hi[cur][loc], t.lo[cur][loc]};
-        int nq = -1, lq = t.last[cur][loc];
+      int moved = 0;
+      for (int e = tid; e < kTileCells; e += kDownThreads) {
+        const int q = t.nx[cur][e];
+        FF v{t.hi[cur][e], t.lo[cur][e]};
+        int nq = -1, lq = t.last[cur][e];
         if (q >= 0) {
           v = ff_add(v, FF{t.hi[cur][q], t.lo[cur][q]});
           nq = t.nx[cur][q];
           lq = t.last[cur][q];
+          moved |= nq >= 0;
         }
-        t.hi[cur ^ 1][loc] = v.hi;
-        t.lo[cur ^ 1][loc] = v.lo;
-        t.nx[cur ^ 1][loc] = (int16_t)nq;
-        t.last[cur ^ 1][loc] = (int16_t)lq;
+        t.hi[cur ^ 1][e] = v.hi;
+        t.lo[cur ^ 1][e] = v.lo;
+        t.nx[cur ^ 1][e] = (int16_t)nq;
+        t.last[cur ^ 1][e] = (int16_t)lq;
       }
       cur ^= 1;
-      __syncwarp();
+      if (!__syncthreads_or(moved)) break;
     }
     int cyc = 0;
-    for (int jj = 0; jj < kTile; jj++) cyc |= t.nx[cur][jj * kTile + ii] >= 0;
-    if (cyc) atomicOr(a.err, ERR_CYCLE);  // a path longer than the tile: a cycle
-    for (int jj = 0; jj < kTile; jj++) {
-      const int64_t j = j0 + jj;
+    for (int e = tid; e < kTileCells; e += kDownThreads) cyc |= t.nx[cur][e] >= 0;
+    if (__syncthreads_or(cyc) && tid == 0) atomicOr(a.err, ERR_CYCLE);
+    for (int e = tid; e < kTileCells; e += kDownThreads) {
+      const int ii = e % kTile, jj = e / kTile;
+      const int64_t i = i0 + ii, j = j0 + jj;
       if (i >= a.m || j >= a.n) continue;
-      const int loc = jj * kTile + ii;
       const int64_t gp = j * a.m + i;
-      int e = t.last[cur][loc];
+      const int x = t.last[cur][e];
       int64_t ge = -1;
-      if (t.rl[e] == RL_EXIT) ge = (j0 + e / kTile) * a.m + (i0 + e % kTile);
+      if (t.rl[x] == RL_EXIT) ge = (j0 + x / kTile) * a.m + (i0 + x % kTile);
       if (a.phase == 1) {
-        if (t.rl[loc] == RL_EXIT) {
-          int slot = atomicAdd(a.ecount, 1);
+        if (t.rl[e] == RL_EXIT) {
+          const int slot = atomicAdd(a.ecount, 1);
           a.eidx[gp] = slot;
           a.elist[slot] = (int)gp;
         }
@@ -641,27 +658,27 @@ __global__ void __launch_bounds__(32) forest_down_kernel(DownArgs a) {
         bool entry = false;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-          int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
-          int qr = ii + 1 - di, qc = jj + 1 - dj;
-          unsigned dq = t.dir[qc][qr];
-          if (dq && d8_bit(dq) == k && !(qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile))
-            entry = true;
+          const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
+          const int qr = ii + 1 - di, qc = jj + 1 - dj;
+          if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) continue;
+          const unsigned dq = t.dir[qc][qr];
+          if (dq && d8_bit(dq) == k) entry = true;
         }
         if (entry) {
-          a.clhi[gp] = t.hi[cur][loc];
-          a.cllo[gp] = t.lo[cur][loc];
+          a.clhi[gp] = t.hi[cur][e];
+          a.cllo[gp] = t.lo[cur][e];
           a.cx[gp] = (int)ge;
         }
       } else {
-        FF v{t.hi[cur][loc], t.lo[cur][loc]};
+        FF v{t.hi[cur][e], t.lo[cur][e]};
         if (ge >= 0) {
-          int ex = a.eidx[ge];
+          const int ex = a.eidx[ge];
           v = ff_add(v, FF{a.Dhi[ex], a.Dlo[ex]});
         }
         a.out[gp] = __fadd_rn(v.hi, v.lo);
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
 }
 
@@ -923,8 +940,8 @@ tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
   a.out = grad_w;
   a.err = counters + 4;
   const int T = g.tiles();
-  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 64);
-  TT_LAUNCH(forest_down_kernel, tgrid, 32, 0, st, a);
+  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 16);
+  TT_LAUNCH(forest_down_kernel, tgrid, kDownThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(down_init_kernel, lg, 256, 0, st, elist, counters + 0, dir, g.m, 0u,
             clhi, cllo, cx, eidx, D[0][0], D[0][1], nx[0]);
@@ -946,7 +963,7 @@ tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
   a.phase = 3;
   a.Dhi = D[cur][0];
   a.Dlo = D[cur][1];
-  TT_LAUNCH(forest_down_kernel, tgrid, 32, 0, st, a);
+  TT_LAUNCH(forest_down_kernel, tgrid, kDownThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
   TT_CHECK(cudaMemcpyAsync(hcnt, counters + 4, 4, cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
