@@ -70,11 +70,61 @@ __device__ void uf_union(int *L, int a, int b) {
 
 constexpr int kCclWarps = 4;
 
+// Shared-memory union-find over run ids (see ccl_tile_kernel).
+__device__ __forceinline__ int sfind(int *lab, int x) {
+  volatile int *v = lab;
+  int p = v[x];
+  while (p != x) {
+    const int gp = v[p];
+    if (gp < p) atomicMin(&lab[x], gp);
+    x = p;
+    p = gp;
+  }
+  return x;
+}
+
+__device__ void sunion(int *lab, int a, int b) {
+  for (int it = 0; it < 4096; it++) {
+    a = sfind(lab, a);
+    b = sfind(lab, b);
+    if (a == b) return;
+    if (a < b) {
+      const int old = atomicMin(&lab[b], a);
+      if (old == b) return;
+      b = old;
+    } else {
+      const int old = atomicMin(&lab[a], b);
+      if (old == a) return;
+      a = old;
+    }
+  }
+}
+
+// Bits s.. of the run of set bits that starts at bit s of m.
+__device__ __forceinline__ uint32_t run_mask(uint32_t m, int s) {
+  const uint32_t tail = ~(m >> s);
+  const int len = tail ? __ffs(tail) - 1 : 32 - s;
+  return len >= 32 ? 0xffffffffu : (((1u << len) - 1u) << s);
+}
+
+// Start bit of the run containing bit b (b set in m, starts = run starts).
+__device__ __forceinline__ int run_start(uint32_t starts, int b) {
+  const uint32_t below = starts & (b == 31 ? 0xffffffffu : ((2u << b) - 1u));
+  return 31 - __clz(below);
+}
+
 struct CclTile {
-  int lab[kTile * kTile];
-  int key[kTile * kTile];  // per local root: max depth key, then argmax
+  int lab[kTile * kTile];  // union-find over run ids (column * 32 + first row)
+  int red[kTile * kTile];  // per local root: max depth key, then argmin
+  uint32_t starts[kTile];  // run starts of each column
 };
 
+// One warp per tile.  Each lane owns one column's flat mask (32 bits): a
+// vertical run of flats is connected by construction, so the union-find only
+// runs over runs, uniting each run with the runs of the next column that
+// touch it (8-connectivity = its extent grown by one row).  Every pixel then
+// takes the root of its run; each tile-local component is reduced to its
+// maximum depth and the smallest pixel attaining it.
 __global__ void __launch_bounds__(kCclWarps * 32)
 ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ larg,
                 int *__restrict__ maxkey, int *__restrict__ argmax,
@@ -83,85 +133,100 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
   __shared__ CclTile tiles[kCclWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   CclTile &t = tiles[warp];
-  int *lb = t.lab;
   const int T = tm * tn;
   for (int tile = blockIdx.x * kCclWarps + warp; tile < T; tile += gridDim.x * kCclWarps) {
     const int ti = tile % tm, tj = tile / tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-    const int ii = lane;
-    const int64_t i = i0 + ii;
-    int keys[kTile];  // depth key of this lane's pixel in each column
-    uint32_t flat_cols = 0;
+    const int64_t i = i0 + lane;  // lane = row for the per-pixel phases
+    int keys[kTile];
+    uint32_t my_mask = 0, flat_cols = 0;
+#pragma unroll 8
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
-      const int loc = jj * kTile + ii;
       bool f = false;
       int k = INT_MIN;
       if (i < m && j < n) {
         const int64_t p = j * m + i;
         f = flats[p] & 1;
         if (f) {
-          float d = __fsub_rn(filled[p], orig[p]);
+          const float d = __fsub_rn(filled[p], orig[p]);
           if (!isnan(d)) k = ordered_key(d);
         }
       }
       keys[jj] = k;
-      if (f) flat_cols |= 1u << jj;
-      lb[loc] = f ? loc : -1;
-      t.key[loc] = INT_MIN;
+      flat_cols |= (uint32_t)f << jj;
+      const uint32_t b = __ballot_sync(0xffffffffu, f);
+      if (lane == jj) my_mask = b;
+    }
+    // lane = column c from here to the unions
+    const uint32_t M = my_mask, S = M & ~(M << 1);
+    t.starts[lane] = S;
+    for (uint32_t s = S; s; s &= s - 1) {
+      const int r = __ffs(s) - 1;
+      t.lab[lane * kTile + r] = lane * kTile + r;
     }
     __syncwarp();
-    // internal edges to the earlier neighbours (i-1,j), (i-1,j-1), (i,j-1), (i+1,j-1)
-    for (int jj = 0; jj < kTile; jj++) {
-      if (!((flat_cols >> jj) & 1u)) continue;
-      const int loc = jj * kTile + ii;
-      const int di[4] = {-1, -1, 0, 1};
-      const int dj[4] = {0, -1, -1, -1};
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        int qi = ii + di[k], qj = jj + dj[k];
-        if (qi < 0 || qi >= kTile || qj < 0) continue;
-        int q = qj * kTile + qi;
-        if (((volatile int *)lb)[q] >= 0) uf_union(lb, loc, q);
+    const uint32_t M1 = __shfl_down_sync(0xffffffffu, M, 1);
+    const uint32_t S1 = __shfl_down_sync(0xffffffffu, S, 1);
+    if (lane < kTile - 1) {
+      for (uint32_t rs = S1; rs; rs &= rs - 1) {
+        const int s1 = __ffs(rs) - 1;
+        const uint32_t rm = run_mask(M1, s1);
+        uint32_t ov = M & (rm | (rm << 1) | (rm >> 1));
+        while (ov) {
+          const int s0 = run_start(S, __ffs(ov) - 1);
+          sunion(t.lab, lane * kTile + s0, (lane + 1) * kTile + s1);
+          ov &= ~run_mask(M, s0);
+        }
       }
     }
     __syncwarp();
+    // lane = row again: each flat pixel takes its run's root
     int roots[kTile];
+#pragma unroll
     for (int jj = 0; jj < kTile; jj++) {
       roots[jj] = -1;
-      if (!((flat_cols >> jj) & 1u)) continue;
-      const int r = uf_find(lb, jj * kTile + ii);
-      roots[jj] = r;
-      if (keys[jj] != INT_MIN) atomicMax(&t.key[r], keys[jj]);
+      if ((flat_cols >> jj) & 1u) {
+        const int run = jj * kTile + run_start(t.starts[jj], lane);
+        roots[jj] = sfind(t.lab, run);
+      }
     }
     __syncwarp();
-    // local maxima of the roots, then the smallest pixel attaining them
+    // per-root maximum depth key, then the smallest pixel attaining it
+#pragma unroll
+    for (int jj = 0; jj < kTile; jj++)
+      if (roots[jj] >= 0 && roots[jj] == jj * kTile + lane) t.red[roots[jj]] = INT_MIN;
+    __syncwarp();
+#pragma unroll
+    for (int jj = 0; jj < kTile; jj++)
+      if (roots[jj] >= 0 && keys[jj] != INT_MIN) atomicMax(&t.red[roots[jj]], keys[jj]);
+    __syncwarp();
     int rmax[kTile];
-    for (int jj = 0; jj < kTile; jj++) rmax[jj] = roots[jj] >= 0 ? t.key[roots[jj]] : INT_MIN;
+#pragma unroll
+    for (int jj = 0; jj < kTile; jj++) rmax[jj] = roots[jj] >= 0 ? t.red[roots[jj]] : INT_MIN;
     __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {
-      const int loc = jj * kTile + ii;
-      if (roots[jj] == loc) t.key[loc] = INT_MAX;
-    }
+#pragma unroll
+    for (int jj = 0; jj < kTile; jj++)
+      if (roots[jj] >= 0 && roots[jj] == jj * kTile + lane) t.red[roots[jj]] = INT_MAX;
     __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {
-      if (roots[jj] < 0 || keys[jj] == INT_MIN || keys[jj] != rmax[jj]) continue;
-      const int loc = jj * kTile + ii;
-      atomicMin(&t.key[roots[jj]], loc);
-    }
+#pragma unroll
+    for (int jj = 0; jj < kTile; jj++)
+      if (roots[jj] >= 0 && keys[jj] != INT_MIN && keys[jj] == rmax[jj])
+        atomicMin(&t.red[roots[jj]], jj * kTile + lane);
     __syncwarp();
+#pragma unroll
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       if (i >= m || j >= n) continue;
       const int64_t gp = j * m + i;
-      const int loc = jj * kTile + ii;
+      const int loc = jj * kTile + lane;
       const int r = roots[jj];
       int v = -1;
       if (r >= 0) {
         v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
         if (r == loc) {
           lmax[gp] = rmax[jj];
-          const int a = t.key[loc];
+          const int a = t.red[loc];
           larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
           maxkey[gp] = INT_MIN;
           argmax[gp] = INT_MAX;
