@@ -114,9 +114,13 @@ __device__ __forceinline__ int run_start(uint32_t starts, int b) {
 }
 
 struct CclTile {
-  int lab[kTile * kTile];  // union-find over run ids (column * 32 + first row)
-  int red[kTile * kTile];  // per local root: max depth key, then argmin
-  uint32_t starts[kTile];  // run starts of each column
+  // Union-find over run ids (column * 32 + first row); once every run knows
+  // its root, the same slots hold per-root reductions: the maximum depth
+  // key, then the smallest pixel attaining it.
+  int lab[kTile * kTile];
+  int key[kTile * kTile];    // per pixel: depth key (INT_MIN: none)
+  int16_t root[kTile * kTile];  // per pixel: local root, -1 for non-flats
+  uint32_t starts[kTile];    // run starts of each column
 };
 
 // One warp per tile.  Each lane owns one column's flat mask (32 bits): a
@@ -138,8 +142,7 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
     const int ti = tile % tm, tj = tile / tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
     const int64_t i = i0 + lane;  // lane = row for the per-pixel phases
-    int keys[kTile];
-    uint32_t my_mask = 0, flat_cols = 0;
+    uint32_t my_mask = 0;
 #pragma unroll 8
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
@@ -153,8 +156,8 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
           if (!isnan(d)) k = ordered_key(d);
         }
       }
-      keys[jj] = k;
-      flat_cols |= (uint32_t)f << jj;
+      t.key[jj * kTile + lane] = k;
+      t.root[jj * kTile + lane] = -1;
       const uint32_t b = __ballot_sync(0xffffffffu, f);
       if (lane == jj) my_mask = b;
     }
@@ -181,52 +184,58 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       }
     }
     __syncwarp();
-    // lane = row again: each flat pixel takes its run's root
-    int roots[kTile];
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++) {
-      roots[jj] = -1;
-      if ((flat_cols >> jj) & 1u) {
-        const int run = jj * kTile + run_start(t.starts[jj], lane);
-        roots[jj] = sfind(t.lab, run);
-      }
+    // lane = column: every pixel of a run takes the run's root; roots reset
+    // their reduction slot
+    for (uint32_t s = S; s; s &= s - 1) {
+      const int s0 = __ffs(s) - 1;
+      const int r = sfind(t.lab, lane * kTile + s0);
+      const uint32_t rm = run_mask(M, s0);
+      for (uint32_t b = rm; b; b &= b - 1) t.root[lane * kTile + __ffs(b) - 1] = (int16_t)r;
     }
     __syncwarp();
-    // per-root maximum depth key, then the smallest pixel attaining it
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++)
-      if (roots[jj] >= 0 && roots[jj] == jj * kTile + lane) t.red[roots[jj]] = INT_MIN;
+    for (uint32_t s = S; s; s &= s - 1) {
+      const int loc = lane * kTile + __ffs(s) - 1;
+      if (t.root[loc] == loc) t.lab[loc] = INT_MIN;
+    }
     __syncwarp();
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++)
-      if (roots[jj] >= 0 && keys[jj] != INT_MIN) atomicMax(&t.red[roots[jj]], keys[jj]);
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc], k = t.key[loc];
+      if (r >= 0 && k != INT_MIN) atomicMax(&t.lab[r], k);
+    }
     __syncwarp();
-    int rmax[kTile];
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++) rmax[jj] = roots[jj] >= 0 ? t.red[roots[jj]] : INT_MIN;
+    for (int jj = 0; jj < kTile; jj++) {  // per pixel: its component's maximum
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      if (r >= 0 && t.key[loc] != INT_MIN && t.key[loc] == t.lab[r]) t.key[loc] = INT_MAX;
+    }
     __syncwarp();
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++)
-      if (roots[jj] >= 0 && roots[jj] == jj * kTile + lane) t.red[roots[jj]] = INT_MAX;
+    // roots: keep the maximum aside (in lmax) and turn the slot into an argmin
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      const int64_t j = j0 + jj;
+      if (r == loc && i < m && j < n) lmax[j * m + i] = t.lab[loc];
+    }
     __syncwarp();
-#pragma unroll
-    for (int jj = 0; jj < kTile; jj++)
-      if (roots[jj] >= 0 && keys[jj] != INT_MIN && keys[jj] == rmax[jj])
-        atomicMin(&t.red[roots[jj]], jj * kTile + lane);
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane;
+      if (t.root[loc] == loc) t.lab[loc] = INT_MAX;
+    }
     __syncwarp();
-#pragma unroll
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      if (r >= 0 && t.key[loc] == INT_MAX) atomicMin(&t.lab[r], loc);
+    }
+    __syncwarp();
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       if (i >= m || j >= n) continue;
       const int64_t gp = j * m + i;
       const int loc = jj * kTile + lane;
-      const int r = roots[jj];
+      const int r = t.root[loc];
       int v = -1;
       if (r >= 0) {
         v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
         if (r == loc) {
-          lmax[gp] = rmax[jj];
-          const int a = t.red[loc];
+          const int a = t.lab[loc];
           larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
           maxkey[gp] = INT_MIN;
           argmax[gp] = INT_MAX;

@@ -203,8 +203,9 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
       bad |= rl == RL_BADDIR;
       int ne = 0, hin = 0;
       long long inflow = 0;
-      if (rl != RL_NONE) {
-        nvalid++;
+      const bool ring = ii == 0 || jj == 0 || ii == kTile - 1 || jj == kTile - 1;
+      if (rl != RL_NONE) nvalid++;
+      if (rl != RL_NONE && ring) {  // only ring pixels have donors in other tiles
 #pragma unroll
         for (int k = 0; k < 8; k++) {
           const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
@@ -491,40 +492,52 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int *__restrict__ in,
   }
 }
 
+constexpr int kScatterPer = 8;  // elements per thread per chunk
+
 __global__ void node_scatter_kernel(const int *__restrict__ h, int64_t N,
                                     const int *__restrict__ off,
                                     int *__restrict__ cursor,
                                     ptrdiff_t *__restrict__ node) {
   __shared__ int cnt[kSmallBins];
   __shared__ int base[kSmallBins];
-  // One pass per block-sized chunk so that small bins are reserved once per
-  // block: count, reserve, then place.
-  for (int64_t start = (int64_t)blockIdx.x * blockDim.x; start < N;
-       start += (int64_t)gridDim.x * blockDim.x) {
+  // Chunks of blockDim * kScatterPer pixels: count small bins in shared
+  // memory, reserve each bin's range once per chunk, then place.
+  const int64_t chunk = (int64_t)blockDim.x * kScatterPer;
+  for (int64_t start = (int64_t)blockIdx.x * chunk; start < N;
+       start += (int64_t)gridDim.x * chunk) {
     for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x) cnt[b] = 0;
     __syncthreads();
-    int64_t p = start + threadIdx.x;
-    int v = p < N ? h[p] : -1;
-    int rank = 0;
-    if (v >= 0 && v < kSmallBins) rank = atomicAdd(&cnt[v], 1);
+    int v[kScatterPer], rank[kScatterPer];
+#pragma unroll
+    for (int u = 0; u < kScatterPer; u++) {
+      const int64_t p = start + (int64_t)u * blockDim.x + threadIdx.x;
+      v[u] = p < N ? h[p] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < kScatterPer; u++)
+      rank[u] = (v[u] >= 0 && v[u] < kSmallBins) ? atomicAdd(&cnt[v[u]], 1) : 0;
     __syncthreads();
     for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x)
       base[b] = cnt[b] ? atomicAdd(&cursor[b], cnt[b]) : 0;
     __syncthreads();
-    if (v >= 0) {
+#pragma unroll
+    for (int u = 0; u < kScatterPer; u++) {
+      const int64_t p = start + (int64_t)u * blockDim.x + threadIdx.x;
+      const int hv = v[u];
+      if (hv < 0) continue;
       int slot;
-      if (v < kSmallBins) {
-        slot = base[v] + rank;
+      if (hv < kSmallBins) {
+        slot = base[hv] + rank[u];
       } else {
-        unsigned grp = __match_any_sync(__activemask(), v);
-        int leader = __ffs(grp) - 1;
-        int lane = threadIdx.x & 31;
+        const unsigned grp = __match_any_sync(__activemask(), hv);
+        const int leader = __ffs(grp) - 1;
+        const int lane = threadIdx.x & 31;
         int b0 = 0;
-        if (lane == leader) b0 = atomicAdd(&cursor[v], __popc(grp));
+        if (lane == leader) b0 = atomicAdd(&cursor[hv], __popc(grp));
         b0 = __shfl_sync(grp, b0, leader);
         slot = b0 + __popc(grp & ((1u << lane) - 1));
       }
-      node[off[v] + slot] = (ptrdiff_t)p;
+      node[off[hv] + slot] = (ptrdiff_t)p;
     }
     __syncthreads();
   }

@@ -169,26 +169,29 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
       }
   }
   __syncthreads();
+  // Off-grid neighbours hold NaN: their slope is NaN and never selected,
+  // exactly as the reference skips them, so no bounds checks are needed.
+  // Odd bits divide by sqrtf(2) with IEEE rounding; even bits divide by 1,
+  // which is exact.
   const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
   for (int c = ty; c < kTile; c += kBlockY) {
-    int64_t j = j0 + c;
-    int64_t i = i0 + tx;
+    const int64_t j = j0 + c;
+    const int64_t i = i0 + tx;
     if (j >= n || i >= m) continue;
-    int r = tx;
-    bool fl = fs[c + 1][r + 1] != 0;
-    float zc = zs[c + 1][r + 1];
-    float z = fl ? ds[c + 1][r + 1] : zc;
+    const int r = tx;
+    const bool fl = fs[c + 1][r + 1] != 0;
+    const float zc = zs[c + 1][r + 1];
+    const float z = fl ? ds[c + 1][r + 1] : zc;
     float best = 0.0f;
     uint8_t d = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      int di = d8_di(k, order), dj = d8_dj(k, order);
-      int64_t ni = i + di, nj = j + dj;
-      if (ni < 0 || ni >= m || nj < 0 || nj >= n) continue;
-      float zn = zs[c + 1 + dj][r + 1 + di];
+      const int di = d8_di(k, order), dj = d8_dj(k, order);
+      const float zn = zs[c + 1 + dj][r + 1 + di];
       if (zn > zc) continue;
-      float zz = fl ? ds[c + 1 + dj][r + 1 + di] : zn;
-      float g = __fdiv_rn(__fsub_rn(z, zz), (k & 1) ? sq2 : 1.0f);
+      const float zz = fl ? ds[c + 1 + dj][r + 1 + di] : zn;
+      const float diff = __fsub_rn(z, zz);
+      const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
       if (g > best) {
         best = g;
         d = (uint8_t)(1u << k);
