@@ -17,12 +17,13 @@
 // to the same fixpoint, so tiles can be relaxed concurrently and races
 // between neighbouring tiles are benign.
 //
-// Work decomposition: one warp owns one 32 x 32 tile.  It stages the tile and
-// a one-pixel halo in shared memory and runs directional Gauss-Seidel sweeps
-// (down, up, right, left along the two axes, each lane carrying one line)
-// until four consecutive sweeps change nothing.  Changed cells are written
-// back with a float atomic minimum; a changed edge or corner pushes the
-// neighbouring tile onto a global work queue.
+// Work decomposition: one warp relaxes one 32 x 32 tile at a time.  It stages
+// the tile and a one-pixel halo in shared memory and runs directional
+// Gauss-Seidel sweeps (down, up, right, left, each lane carrying one line)
+// over the pixels marked for re-evaluation until none is marked.  Changed
+// cells are written back with plain stores (a tile has one owner, so no
+// other warp writes them meanwhile); a changed edge or corner marks the
+// neighbouring tile dirty.
 //
 // Scheduling: one persistent launch.  Warp w of W owns the tiles
 // w, w + W, w + 2W, ... and keeps scanning their "dirty" flags (32 at a time
@@ -53,14 +54,11 @@ enum Kind { FILL = 0, GWDT = 1 };
 struct WarpTile {
   float s[kHalo][kPitch];  // state: f (fill) or dist (gwdt); [c][r]
   float a[kHalo][kPitch];  // aux: dem (fill) or costs (gwdt)
-  uint64_t flat[kHalo];    // gwdt: flat bit per row of column c (rows 0..33)
-  uint32_t dirty[kHalo];   // changed interior rows (bit r-1) of column c
-  uint32_t need[kHalo];    // interior rows of column c to re-evaluate
 };
 
 // Control block (device memory, zero-initialised).
 struct QueueCtl {
-  unsigned long long visits;  // tiles relaxed so far
+  unsigned long long visits;  // tiles relaxed so far (flushed in batches)
   int pending;                // dirty + running tiles
   int abort;                  // ABORT_* bits
 };
@@ -76,23 +74,39 @@ struct RelaxArgs {
   int64_t m, n;
   int tm, tn;
   QueueCtl *ctl;
-  int *dirty;  // per tile: 1 while waiting to be relaxed
+  int *dirty;  // per tile: nonzero while waiting to be relaxed
   unsigned long long max_visits;
+  int visit_flush;  // a warp adds its visits to ctl->visits in batches of this
 };
 
 // Dirty flag values: 1 = a halo pixel changed (re-evaluate the edge ring),
 // 2 = evaluate every pixel (first visit, or a visit that hit its sweep cap).
 enum : int { DIRTY_EDGE = 1, DIRTY_FULL = 2 };
 
-__device__ __forceinline__ void mark_dirty(const RelaxArgs &a, int t, int v) {
-  atomicAdd(&a.ctl->pending, 1);
-  if (atomicMax(&a.dirty[t], v) != 0) atomicSub(&a.ctl->pending, 1);
+// Release / acquire at device scope (lighter than a sequentially consistent
+// fence): a writer fences before it sets a flag, a reader after it takes one.
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
-__device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj,
-                                          int v = DIRTY_EDGE) {
-  if (ti < 0 || tj < 0 || ti >= a.tm || tj >= a.tn) return;
-  mark_dirty(a, tj * a.tm + ti, v);
+// 4-byte asynchronous copy global -> shared, cached in L1 (read-only inputs).
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// Transpose of a 32 x 32 bit matrix held one row per lane.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+  uint32_t y = 0;
+#pragma unroll
+  for (int k = 0; k < 32; k++) {
+    const uint32_t b = __ballot_sync(0xffffffffu, (x >> k) & 1u);
+    if (lane == k) y = b;
+  }
+  return y;
 }
 
 // The update at pixel (c, r) from all eight neighbours.  Neighbour values may
@@ -101,54 +115,56 @@ __device__ __forceinline__ void push_tile(const RelaxArgs &a, int ti, int tj,
 template <int KIND>
 __device__ __forceinline__ float relax8(const WarpTile &t, int c, int r, float cur) {
   if (KIND == FILL) {
-    float lo = cur;
-#pragma unroll
-    for (int dc = -1; dc <= 1; dc++)
-#pragma unroll
-      for (int dr = -1; dr <= 1; dr++)
-        if (dc || dr) lo = fminf(lo, t.s[c + dc][r + dr]);
+    const float a0 = fminf(t.s[c - 1][r - 1], t.s[c - 1][r]);
+    const float a1 = fminf(t.s[c - 1][r + 1], t.s[c][r - 1]);
+    const float a2 = fminf(t.s[c][r + 1], t.s[c + 1][r - 1]);
+    const float a3 = fminf(t.s[c + 1][r], t.s[c + 1][r + 1]);
+    const float lo = fminf(cur, fminf(fminf(a0, a1), fminf(a2, a3)));
     const float z = t.a[c][r];
     return (lo > z) ? lo : z;
   } else {
-    if (!((t.flat[c] >> r) & 1)) return cur;
+    // Non-flat and off-grid pixels are staged as state +INF and cost NaN:
+    // every path through them evaluates to +INF or NaN, which never wins
+    // the minimum, and a non-flat centre (cost NaN) keeps its value.
     const float cs = t.a[c][r];
     float best = cur;
 #pragma unroll
     for (int dc = -1; dc <= 1; dc++) {
-      const uint64_t fc = t.flat[c + dc];
 #pragma unroll
       for (int dr = -1; dr <= 1; dr++) {
         if (!(dc || dr)) continue;
-        if (!((fc >> (r + dr)) & 1)) continue;
-        const float ch = (dc && dr) ? kSqrt2 : 1.0f;
-        const float w = __fmul_rn(__fmul_rn(ch, __fadd_rn(cs, t.a[c + dc][r + dr])), 0.5f);
-        const float prop = __fadd_rn(t.s[c + dc][r + dr], w);
-        if (prop < best) best = prop;
+        const float sum = __fadd_rn(cs, t.a[c + dc][r + dr]);
+        // chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
+        const float w = (dc && dr) ? __fmul_rn(__fmul_rn(kSqrt2, sum), 0.5f)
+                                   : __fmul_rn(sum, 0.5f);
+        best = fminf(best, __fadd_rn(t.s[c + dc][r + dr], w));
       }
     }
     return best;
   }
 }
 
-// Work-proportional Gauss-Seidel sweeps.  need[c] marks the interior pixels
-// of column c whose neighbourhood changed since they were last evaluated
-// against all eight neighbours; only those are evaluated, a step with no
-// marked pixel is skipped by the whole warp, and a pixel that changes marks
-// its eight neighbours.  An unmarked pixel therefore cannot be lowered by any
-// neighbour, and the tile is at its local fixpoint exactly when no pixel is
-// marked.
-
-// Sweep along r (lane = column c).  dir = +1 down, -1 up.
-template <int KIND>
-__device__ void sweep_rows(WarpTile &t, int lane, int dir) {
-  const int c = lane + 1;
-  uint32_t nd = t.need[c];
-  uint32_t dmask = 0;
+// One work-proportional Gauss-Seidel sweep.  Each lane carries one line of
+// the tile: a column (ALONG_C false: the sweep walks down or up the rows) or a
+// row (ALONG_C true: it walks right or left along the columns).  `nd` marks
+// the pixels of the lane's line whose neighbourhood changed since they were
+// last evaluated against all eight neighbours, `dm` the pixels that changed;
+// both live in registers, bit k = k-th pixel of the line.  Only marked pixels
+// are evaluated, a step with no marked pixel is skipped by the whole warp,
+// and a pixel that changes marks its eight neighbours (two on its own line,
+// three on each adjacent lane's line).  An unmarked pixel therefore cannot
+// be lowered by any neighbour, and the tile is at its local fixpoint exactly
+// when no pixel is marked.
+template <int KIND, bool ALONG_C>
+__device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &nd,
+                                      uint32_t &dm) {
   for (int s = 0; s < kTile; s++) {
-    const int r = dir > 0 ? 1 + s : kTile - s;
-    const uint32_t bit = 1u << (r - 1);
+    const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
+    const uint32_t bit = 1u << k;
     const bool act = (nd & bit) != 0;
     if (!__any_sync(0xffffffffu, act)) continue;
+    const int c = ALONG_C ? k + 1 : lane + 1;
+    const int r = ALONG_C ? lane + 1 : k + 1;
     uint32_t mark = 0;
     if (act) {
       nd &= ~bit;
@@ -156,55 +172,19 @@ __device__ void sweep_rows(WarpTile &t, int lane, int dir) {
       const float nv = relax8<KIND>(t, c, r, cur);
       if (nv < cur) {
         t.s[c][r] = nv;
-        dmask |= bit;
+        dm |= bit;
         mark = bit | (bit << 1) | (bit >> 1);
       }
     }
-    // neighbours in this column and in the two adjacent columns
-    const uint32_t from_left = __shfl_up_sync(0xffffffffu, mark, 1);
-    const uint32_t from_right = __shfl_down_sync(0xffffffffu, mark, 1);
-    nd |= (mark & ~bit) | (lane > 0 ? from_left : 0u) | (lane < 31 ? from_right : 0u);
-    __syncwarp();
-  }
-  t.need[c] = nd;
-  t.dirty[c] |= dmask;
-  __syncwarp();
-}
-
-// Sweep along c (lane = row r).  dir = +1 right, -1 left.
-template <int KIND>
-__device__ void sweep_cols(WarpTile &t, int lane, int dir) {
-  const int r = lane + 1;
-  for (int s = 0; s < kTile; s++) {
-    const int c = dir > 0 ? 1 + s : kTile - s;
-    const uint32_t w = t.need[c];
-    if (w == 0) continue;  // warp-uniform (shared word)
-    const bool act = (w >> lane) & 1u;
-    bool ch = false;
-    if (act) {
-      const float cur = t.s[c][r];
-      const float nv = relax8<KIND>(t, c, r, cur);
-      ch = nv < cur;
-      if (ch) t.s[c][r] = nv;
-    }
-    const unsigned b = __ballot_sync(0xffffffffu, ch);
-    __syncwarp();
-    if (lane == 0) {
-      // every marked pixel of column c was evaluated in this step; pixels next
-      // to one that changed (in this column and the two adjacent ones) must
-      // be evaluated again
-      const uint32_t d3 = b | (b << 1) | (b >> 1);
-      t.need[c] = (b << 1) | (b >> 1);
-      if (c > 1) t.need[c - 1] |= d3;
-      if (c < kTile) t.need[c + 1] |= d3;
-      t.dirty[c] |= b;
-    }
+    const uint32_t from_prev = __shfl_up_sync(0xffffffffu, mark, 1);
+    const uint32_t from_next = __shfl_down_sync(0xffffffffu, mark, 1);
+    nd |= (mark & ~bit) | (lane > 0 ? from_prev : 0u) | (lane < 31 ? from_next : 0u);
     __syncwarp();
   }
 }
 
 template <int KIND>
-__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
+__device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
 
 template <int KIND>
 __global__ void __launch_bounds__(kWarps * 32)
@@ -216,10 +196,17 @@ relax_persistent_kernel(RelaxArgs a) {
   const int wid = blockIdx.x * kWarps + warp;
   const int T = a.tm * a.tn;
   long long idle = 0;
+  unsigned long long unflushed = 0;  // lane 0: visits not yet added to ctl
   for (;;) {
     if (*(volatile int *)&a.ctl->abort) break;
-    if (lane == 0 && *(volatile unsigned long long *)&a.ctl->visits >= a.max_visits)
-      atomicOr(&a.ctl->abort, ABORT_VISITS);
+    if (lane == 0) {
+      if (unflushed >= (unsigned long long)a.visit_flush) {
+        atomicAdd(&a.ctl->visits, unflushed);
+        unflushed = 0;
+      }
+      if (*(volatile unsigned long long *)&a.ctl->visits >= a.max_visits)
+        atomicOr(&a.ctl->abort, ABORT_VISITS);
+    }
     bool did = false;
     for (int base = wid; base < T; base += W * 32) {
       const int mine = base + lane * W;
@@ -233,18 +220,17 @@ relax_persistent_kernel(RelaxArgs a) {
         if (lane == 0) {
           got = atomicExch(&a.dirty[tile], 0);
           if (got) {
-            atomicAdd(&a.ctl->visits, 1ULL);  // no return: no round trip
-            __threadfence();
+            unflushed++;
+            fence_acq_rel_gpu();  // acquire: the writes published before the flag
           }
         }
         got = __shfl_sync(0xffffffffu, got, 0);
         if (!got) continue;
         did = true;
-        relax_tile<KIND>(a, t, lane, tile, got);
-        if (lane == 0) {
-          __threadfence();
-          atomicSub(&a.ctl->pending, 1);
-        }
+        const int redundant = relax_tile<KIND>(a, t, lane, tile, got);
+        // This tile is done; its pushes were counted before their flags were
+        // set, minus those that found the flag already set.
+        if (lane == 0) atomicSub(&a.ctl->pending, redundant + 1);
         __syncwarp();
       }
     }
@@ -265,128 +251,187 @@ relax_persistent_kernel(RelaxArgs a) {
     }
     if (__shfl_sync(0xffffffffu, stop, 0)) break;
   }
+  if (lane == 0 && unflushed) atomicAdd(&a.ctl->visits, unflushed);
 }
 
 // Relaxes one tile to its local fixpoint and marks changed neighbours dirty.
+// Returns how many of those marks found the flag already set.
 template <int KIND>
-__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
-  {
-    const int ti = tile % a.tm, tj = tile / a.tm;
-    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+__device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
+  const int ti = tile % a.tm, tj = tile / a.tm;
+  const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+  int *const sflat = reinterpret_cast<int *>(&t.s[0][0]);  // flats, before the state
 
-    // Stage tile + halo.  Lane r loads row r (and lanes 0, 1 rows 32, 33).
-    // Loads are issued a chunk of columns at a time into registers before
-    // any of them is consumed, so one visit waits for a few memory latencies
-    // instead of one per column.
-    constexpr int kChunk = 9;  // 34 columns = 9 + 9 + 9 + 7
-    const int r_lo = lane, r_hi = lane + 32;
-    const int64_t i_lo = i0 - 1 + r_lo, i_hi = i0 - 1 + r_hi;
-    const bool ilo_ok = i_lo >= 0 && i_lo < a.m;
-    const bool ihi_ok = r_hi < kHalo && i_hi < a.m;
-    for (int c0 = 0; c0 < kHalo; c0 += kChunk) {
-      float s_lo[kChunk], a_lo[kChunk], s_hi[kChunk], a_hi[kChunk];
-      int f_lo[kChunk], f_hi[kChunk];
+  // Stage tile + halo with every load in flight at once.  Lane l carries
+  // halo row l (pixel row i0 - 1 + l) of all 34 columns; the two last halo
+  // rows (32, 33) are spread over the warp, three columns per lane.  The
+  // state (updated concurrently by other SMs) is read from L2 into
+  // registers; the read-only aux and flats go straight to shared memory by
+  // asynchronous copies.
+  float sv[kHalo], sx[3];
+  const int64_t im = i0 - 1 + lane;
+  const bool im_ok = im >= 0 && im < a.m;
+  const int rx = kTile + (lane & 1);  // halo row 32 or 33
+  const int64_t ix = i0 - 1 + rx;
+  const bool ix_ok = ix < a.m;
 #pragma unroll
-      for (int u = 0; u < kChunk; u++) {
-        const int c = c0 + u;
-        const int64_t j = j0 - 1 + c;
-        const bool jok = c < kHalo && j >= 0 && j < a.n;
-        s_lo[u] = INFINITY;
-        a_lo[u] = (KIND == FILL) ? INFINITY : 0.0f;
-        s_hi[u] = INFINITY;
-        a_hi[u] = (KIND == FILL) ? INFINITY : 0.0f;
-        f_lo[u] = 0;
-        f_hi[u] = 0;
-        if (jok && ilo_ok) {
-          const int64_t p = j * a.m + i_lo;
-          s_lo[u] = __ldcg(&a.state[p]);  // L2: other SMs update it concurrently
-          a_lo[u] = a.aux[p];
-          if (KIND == GWDT) f_lo[u] = a.flats[p];
-        }
-        if (jok && ihi_ok) {
-          const int64_t p = j * a.m + i_hi;
-          s_hi[u] = __ldcg(&a.state[p]);
-          a_hi[u] = a.aux[p];
-          if (KIND == GWDT) f_hi[u] = a.flats[p];
-        }
-      }
+  for (int c = 0; c < kHalo; c++) {
+    const int64_t j = j0 - 1 + c;
+    sv[c] = INFINITY;
+    if (im_ok && j >= 0 && j < a.n) {
+      const int64_t p = j * a.m + im;
+      sv[c] = __ldcg(&a.state[p]);
+      cp_async4(&t.a[c][lane], &a.aux[p]);
+      if (KIND == GWDT) cp_async4(&sflat[c * kPitch + lane], &a.flats[p]);
+    } else if (KIND == GWDT) {
+      sflat[c * kPitch + lane] = 0;  // off-grid: never flat, never evaluated
+    } else {
+      t.a[c][lane] = INFINITY;  // off-grid pixels of the tile stay at +INF
+    }
+  }
 #pragma unroll
-      for (int u = 0; u < kChunk; u++) {
-        const int c = c0 + u;
-        if (c >= kHalo) break;
-        t.s[c][r_lo] = s_lo[u];
-        t.a[c][r_lo] = a_lo[u];
-        if (r_hi < kHalo) {
-          t.s[c][r_hi] = s_hi[u];
-          t.a[c][r_hi] = a_hi[u];
-        }
-        uint32_t flo = 0, fhi = 0;
-        if (KIND == GWDT) {
-          flo = __ballot_sync(0xffffffffu, f_lo[u] & 1);
-          fhi = __ballot_sync(0xffffffffu, f_hi[u] & 1);
-        }
-        if (lane == 0) {
-          t.dirty[c] = 0;
-          t.need[c] = (mode == DIRTY_FULL || c == 1 || c == kTile) ? 0xffffffffu
-                                                                    : 0x80000001u;
-          if (KIND == GWDT) t.flat[c] = (uint64_t)flo | ((uint64_t)(fhi & 3u) << 32);
-        }
+  for (int u = 0; u < 3; u++) {
+    const int c = (lane >> 1) + 16 * u;
+    const int64_t j = j0 - 1 + c;
+    sx[u] = INFINITY;
+    if (c < kHalo) {
+      if (ix_ok && j >= 0 && j < a.n) {
+        const int64_t p = j * a.m + ix;
+        sx[u] = __ldcg(&a.state[p]);
+        cp_async4(&t.a[c][rx], &a.aux[p]);
+        if (KIND == GWDT) cp_async4(&sflat[c * kPitch + rx], &a.flats[p]);
+      } else if (KIND == GWDT) {
+        sflat[c * kPitch + rx] = 0;
+      } else {
+        t.a[c][rx] = INFINITY;
       }
     }
-    __syncwarp();
-
-    // Sweep until no pixel is marked for re-evaluation: the local fixpoint.
-    bool done = false;
-    int sweeps = 0, k = 0;
-    while (sweeps < kMaxSweeps) {
-      if (!__any_sync(0xffffffffu, t.need[lane + 1] != 0)) {
-        done = true;
-        break;
+  }
+  cp_async_wait_all();
+  __syncwarp();
+  if (KIND == GWDT) {  // non-flat (and off-grid) pixels: state +INF, cost NaN
+#pragma unroll
+    for (int c = 0; c < kHalo; c++) {
+      const bool fl = sflat[c * kPitch + lane] & 1;
+      if (!fl) {
+        sv[c] = INFINITY;
+        t.a[c][lane] = NAN;
       }
-      switch (k) {
-        case 0: sweep_rows<KIND>(t, lane, +1); break;
-        case 1: sweep_rows<KIND>(t, lane, -1); break;
-        case 2: sweep_cols<KIND>(t, lane, +1); break;
-        default: sweep_cols<KIND>(t, lane, -1); break;
-      }
-      k = (k + 1) & 3;
-      sweeps++;
     }
-    __syncwarp();
-
-    // Write back changed cells (coalesced per column) and collect edge flags.
-    uint32_t top = 0, bottom = 0;
-    for (int c = 1; c <= kTile; c++) {
-      uint32_t dm = t.dirty[c];
-      if (!dm) continue;
-      int64_t j = j0 + c - 1;
-      int64_t i = i0 + lane;
-      if ((dm >> lane) & 1u) {
-        if (j < a.n && i < a.m) a.state[j * a.m + i] = t.s[c][lane + 1];
+#pragma unroll
+    for (int u = 0; u < 3; u++) {
+      const int c = (lane >> 1) + 16 * u;
+      if (c < kHalo && !(sflat[c * kPitch + rx] & 1)) {
+        sx[u] = INFINITY;
+        t.a[c][rx] = NAN;
       }
-      top |= dm & 1u;
-      bottom |= (dm >> 31) & 1u;
-    }
-    __threadfence();  // publish this lane's writes before any push below
-    __syncwarp();
-    {  // lanes 0..8 mark one neighbour each, concurrently
-      const uint32_t left = t.dirty[1], right = t.dirty[kTile];
-      switch (lane) {
-        case 0: if (top) push_tile(a, ti - 1, tj); break;
-        case 1: if (bottom) push_tile(a, ti + 1, tj); break;
-        case 2: if (left) push_tile(a, ti, tj - 1); break;
-        case 3: if (right) push_tile(a, ti, tj + 1); break;
-        case 4: if (left & 1u) push_tile(a, ti - 1, tj - 1); break;
-        case 5: if ((left >> 31) & 1u) push_tile(a, ti + 1, tj - 1); break;
-        case 6: if (right & 1u) push_tile(a, ti - 1, tj + 1); break;
-        case 7: if ((right >> 31) & 1u) push_tile(a, ti + 1, tj + 1); break;
-        case 8: if (!done) push_tile(a, ti, tj, DIRTY_FULL); break;  // capped
-        default: break;
-      }
-      __threadfence();  // the pending increments land before the owner's decrement
     }
     __syncwarp();
   }
+#pragma unroll
+  for (int c = 0; c < kHalo; c++) t.s[c][lane] = sv[c];
+#pragma unroll
+  for (int u = 0; u < 3; u++) {
+    const int c = (lane >> 1) + 16 * u;
+    if (c < kHalo) t.s[c][rx] = sx[u];
+  }
+  __syncwarp();
+
+  // Marks in the column layout: lane l holds interior column l + 1, bit k =
+  // interior row k + 1.  An edge visit starts from the ring next to the halo.
+  uint32_t nd = (mode == DIRTY_FULL || lane == 0 || lane == kTile - 1) ? 0xffffffffu
+                                                                       : 0x80000001u;
+  uint32_t dm = 0;
+
+  // Sweep until no pixel is marked for re-evaluation: the local fixpoint.
+  // Down and up run in the column layout, right and left in the row layout
+  // (the marks are transposed between the two).
+  bool done = false;
+  int sweeps = 0;
+  while (sweeps < kMaxSweeps) {
+    if (!__any_sync(0xffffffffu, nd != 0)) {
+      done = true;
+      break;
+    }
+    sweep<KIND, false>(t, lane, +1, nd, dm);
+    sweeps++;
+    if (!__any_sync(0xffffffffu, nd != 0)) {
+      done = true;
+      break;
+    }
+    sweep<KIND, false>(t, lane, -1, nd, dm);
+    sweeps++;
+    if (!__any_sync(0xffffffffu, nd != 0)) {
+      done = true;
+      break;
+    }
+    uint32_t ndr = transpose32(nd, lane), dmr = 0;
+    sweep<KIND, true>(t, lane, +1, ndr, dmr);
+    sweeps++;
+    if (__any_sync(0xffffffffu, ndr != 0)) {
+      sweep<KIND, true>(t, lane, -1, ndr, dmr);
+      sweeps++;
+    }
+    nd = transpose32(ndr, lane);
+    dm |= transpose32(dmr, lane);
+  }
+
+  // Write back changed cells (coalesced per column: lane = row).
+#pragma unroll 4
+  for (int c = 0; c < kTile; c++) {
+    const uint32_t d = __shfl_sync(0xffffffffu, dm, c);
+    if (!d) continue;
+    if ((d >> lane) & 1u) {
+      const int64_t j = j0 + c, i = i0 + lane;
+      if (j < a.n && i < a.m) a.state[j * a.m + i] = t.s[c + 1][lane + 1];
+    }
+  }
+  const bool top = __any_sync(0xffffffffu, dm & 1u);
+  const bool bottom = __any_sync(0xffffffffu, (dm >> 31) & 1u);
+  const uint32_t left = __shfl_sync(0xffffffffu, dm, 0);
+  const uint32_t right = __shfl_sync(0xffffffffu, dm, kTile - 1);
+
+  // Lanes 0..8 mark one neighbour each.  The pushes are counted in `pending`
+  // (one returning add, completed before any flag is set), then set with
+  // atomicMax; those that found a flag already set are handed back to the
+  // caller, which removes them with this tile's own count.  A tile whose
+  // edges did not change publishes nothing: only its owner reads its
+  // interior again.
+  int tgt = -1, val = DIRTY_EDGE;
+  switch (lane) {
+    case 0: if (top) { tgt = 0; } break;
+    case 1: if (bottom) { tgt = 1; } break;
+    case 2: if (left) { tgt = 2; } break;
+    case 3: if (right) { tgt = 3; } break;
+    case 4: if (left & 1u) { tgt = 4; } break;
+    case 5: if ((left >> 31) & 1u) { tgt = 5; } break;
+    case 6: if (right & 1u) { tgt = 6; } break;
+    case 7: if ((right >> 31) & 1u) { tgt = 7; } break;
+    case 8: if (!done) { tgt = 8; val = DIRTY_FULL; } break;  // capped: revisit
+    default: break;
+  }
+  if (tgt >= 0) {
+    const int di = (tgt == 0 || tgt == 4 || tgt == 6) ? -1 : (tgt == 1 || tgt == 5 || tgt == 7) ? 1 : 0;
+    const int dj = (tgt == 2 || tgt == 4 || tgt == 5) ? -1 : (tgt == 3 || tgt == 6 || tgt == 7) ? 1 : 0;
+    const int ni = ti + di, nj = tj + dj;
+    tgt = (ni < 0 || nj < 0 || ni >= a.tm || nj >= a.tn) ? -1 : nj * a.tm + ni;
+  }
+  const unsigned pushes = __ballot_sync(0xffffffffu, tgt >= 0);
+  if (!pushes) return 0;
+  fence_acq_rel_gpu();  // release: this lane's writes before any flag below
+  __syncwarp();
+  if (lane == 0) {
+    // the returned value forces the add to complete before the flags
+    const int before = atomicAdd(&a.ctl->pending, __popc(pushes));
+    asm volatile("" ::"r"(before));
+  }
+  __syncwarp();
+  int old = 0;
+  if (tgt >= 0) {
+    fence_acq_rel_gpu();  // cumulative over the warp's writes seen at the barrier
+    old = atomicMax(&a.dirty[tgt], val);
+  }
+  return __popc(__ballot_sync(0xffffffffu, tgt >= 0 && old != 0));
 }
 
 // f = dem where bc == 1 (and where dem is NaN), +INF elsewhere
@@ -496,6 +541,13 @@ __global__ void gwdt_prev_kernel(ptrdiff_t *__restrict__ prev,
   }
 }
 
+// Visits a warp counts locally before adding them to the shared counter: up
+// to 32, fewer when the budget is small enough for the batching to matter.
+int visit_flush(unsigned long long max_visits, int warps) {
+  const unsigned long long f = max_visits / (64ULL * (unsigned long long)std::max(warps, 1));
+  return (int)std::max(1ULL, std::min(32ULL, f));
+}
+
 int elementwise_grid(int64_t N) {
   int64_t b = (N + 255) / 256;
   int64_t cap = (int64_t)sm_count() * 16;
@@ -516,7 +568,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
   if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, dirty, 0};
+  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
   const int64_t cap_rounds = max_rounds();
   ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
@@ -540,6 +592,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   // No more warps than tiles (each warp owns at least one tile).
   int grid = sm_count() * blocks_per_sm[KIND];
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
+  ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
   TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
   TT_CHECK(cudaGetLastError());
   if (status_sink()) {  // deferred: record the abort word, no round trip
@@ -648,7 +701,7 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
   TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, ctl, T);
   TT_CHECK(cudaGetLastError());
-  RelaxArgs ra{f, dem, nullptr, g.m, g.n, g.tm, g.tn, ctl, dirty, 0};
+  RelaxArgs ra{f, dem, nullptr, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
   ra.max_visits = (unsigned long long)T *
                   (unsigned long long)std::min<int64_t>(max_rounds(), 1LL << 20);
   int b = 0;
@@ -656,6 +709,7 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
                                                 kWarps * 32, 0);
   int grid = sm_count() * (b > 0 ? b : 1);
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
+  ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
   TT_LAUNCH(relax_persistent_kernel<FILL>, grid, kWarps * 32, 0, st, ra);
   TT_CHECK(cudaGetLastError());
   QueueCtl h;  // read back into host stack memory: no pinned allocation
