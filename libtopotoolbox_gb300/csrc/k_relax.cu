@@ -144,43 +144,64 @@ __device__ __forceinline__ float relax8(const WarpTile &t, int c, int r, float c
   }
 }
 
-// One work-proportional Gauss-Seidel sweep.  Each lane carries one line of
-// the tile: a column (ALONG_C false: the sweep walks down or up the rows) or a
-// row (ALONG_C true: it walks right or left along the columns).  `nd` marks
-// the pixels of the lane's line whose neighbourhood changed since they were
-// last evaluated against all eight neighbours, `dm` the pixels that changed;
-// both live in registers, bit k = k-th pixel of the line.  Only marked pixels
-// are evaluated, a step with no marked pixel is skipped by the whole warp,
-// and a pixel that changes marks its eight neighbours (two on its own line,
-// three on each adjacent lane's line).  An unmarked pixel therefore cannot
-// be lowered by any neighbour, and the tile is at its local fixpoint exactly
-// when no pixel is marked.
+// One Gauss-Seidel sweep.  Each lane carries one line of the tile: a column
+// (ALONG_C false: the sweep walks down or up the rows) or a row (ALONG_C
+// true: it walks right or left along the columns).  `nd` marks the pixels of
+// the lane's line whose neighbourhood changed since they were last evaluated
+// against all eight neighbours, `dm` collects the pixels that changed; both
+// live in registers, bit k = k-th pixel of the line.
+//
+// A step (one pixel per lane) runs when some lane's pixel is marked or the
+// previous step changed something, and then evaluates every lane's pixel:
+// in SIMT that costs the same as evaluating only the marked ones, and it
+// keeps the per-step dependency chain down to the loads, the minimum and a
+// vote.  After the sweep a pixel is marked again if a neighbour evaluated in
+// the same step or a later one changed (neighbours of earlier steps were
+// already final when it was evaluated), and unevaluated pixels keep their
+// marks.  An unmarked pixel therefore cannot be lowered by any neighbour,
+// and the tile is at its local fixpoint exactly when no pixel is marked.
+//
+// Fill (a cheap update) runs every step from the first marked one to the
+// end of the line with no vote at all; gwdt (a heavier update) votes after
+// each step and skips steps with nothing to do.
 template <int KIND, bool ALONG_C>
 __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &nd,
-                                      uint32_t &dm) {
-  for (int s = 0; s < kTile; s++) {
+                                      uint32_t &dm_all) {
+  constexpr bool kVote = KIND == GWDT;
+  constexpr int kUnroll = KIND == GWDT ? 2 : 4;
+  uint32_t dm = 0, evald = 0;
+  bool prev = false;
+  int first = 0;
+  if (!kVote) {
+    const uint32_t steps = __reduce_or_sync(0xffffffffu, nd);
+    if (!steps) return;
+    first = dir > 0 ? __ffs(steps) - 1 : kTile - 1 - (31 - __clz(steps));
+  }
+#pragma unroll kUnroll
+  for (int s = first; s < kTile; s++) {
     const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
     const uint32_t bit = 1u << k;
-    const bool act = (nd & bit) != 0;
-    if (!__any_sync(0xffffffffu, act)) continue;
+    if (kVote && !prev && !__any_sync(0xffffffffu, nd & bit)) continue;
+    evald |= bit;
     const int c = ALONG_C ? k + 1 : lane + 1;
     const int r = ALONG_C ? lane + 1 : k + 1;
-    uint32_t mark = 0;
-    if (act) {
-      nd &= ~bit;
-      const float cur = t.s[c][r];
-      const float nv = relax8<KIND>(t, c, r, cur);
-      if (nv < cur) {
-        t.s[c][r] = nv;
-        dm |= bit;
-        mark = bit | (bit << 1) | (bit >> 1);
-      }
+    const float cur = t.s[c][r];
+    const float nv = relax8<KIND>(t, c, r, cur);
+    const bool ch = nv < cur;
+    if (ch) {
+      t.s[c][r] = nv;
+      dm |= bit;
     }
-    const uint32_t from_prev = __shfl_up_sync(0xffffffffu, mark, 1);
-    const uint32_t from_next = __shfl_down_sync(0xffffffffu, mark, 1);
-    nd |= (mark & ~bit) | (lane > 0 ? from_prev : 0u) | (lane < 31 ? from_next : 0u);
+    if (kVote) prev = __any_sync(0xffffffffu, ch);
     __syncwarp();
   }
+  const uint32_t from_prev = __shfl_up_sync(0xffffffffu, dm, 1);
+  const uint32_t from_next = __shfl_down_sync(0xffffffffu, dm, 1);
+  const uint32_t side = (lane > 0 ? from_prev : 0u) | (lane < 31 ? from_next : 0u);
+  const uint32_t any3 = dm | side;
+  const uint32_t later = dir > 0 ? (any3 >> 1) : (any3 << 1);
+  nd = (nd & ~evald) | side | later;
+  dm_all |= dm;
 }
 
 template <int KIND>
