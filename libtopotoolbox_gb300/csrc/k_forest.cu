@@ -6,12 +6,13 @@
 // The reference walks it sequentially (a DFS for the order, then one pass in
 // that order for the sums).  Here the forest is contracted in two levels:
 //
-//  1. Tile level (one warp per 32 x 32 tile, shared memory).  Pixels whose
-//     receiver lies outside their tile are the tile's exits E.  Inside a tile
-//     sums are taken with a "last arriver continues" walk: every in-tile leaf
-//     starts a lane that adds its value into its receiver and decrements the
-//     receiver's count of pending in-tile donors; the lane that brings the
-//     count to zero owns the now-complete receiver and continues downstream.
+//  1. Tile level (one 128-thread block per 32 x 32 tile, shared memory).
+//     Pixels whose receiver lies outside their tile are the tile's exits E.
+//     Inside a tile sums are taken with a "last arriver continues" walk:
+//     every in-tile leaf starts a thread that adds its value into its
+//     receiver and decrements the receiver's count of pending in-tile
+//     donors; the thread that brings the count to zero owns the now-complete
+//     receiver and continues downstream.
 //     For each entry pixel (one with a donor in another tile) the walk also
 //     records the exit its in-tile path reaches and the number of steps.
 //  2. Coarse level (global memory).  The exits form a smaller forest
@@ -139,29 +140,39 @@ __device__ __forceinline__ int local_receiver(const uint8_t (*dir)[36], int ii,
 }
 
 // One 128-thread block per tile.
-//  1. receivers (local index or RL_* code), external donors, initial values
-//     (weight + inflow from other tiles in the final pass);
-//  2. in-place pointer jumping on packed (next << 16 | depth) words: after
-//     ten rounds every pixel knows its in-tile terminal (exit, outlet or
-//     grid edge) and the number of steps to it;
-//  3. a counting sort by depth;
-//  4. levels from the deepest up: every pixel of level L adds its value into
-//     its receiver (level L-1) with integer atomics, one barrier per level.
+//  1. receivers (local index or RL_* code), the count of in-tile donors of
+//     every pixel, initial values (weight); the 124 ring pixels, one per
+//     thread, look for donors in other tiles and, in the final pass, add
+//     their inflow;
+//  2. "last arriver continues": every in-tile leaf starts a walk that adds
+//     its value into its receiver and decrements the receiver's count of
+//     pending donors; the walker that brings the count to zero owns the now
+//     complete receiver and continues downstream.  No barriers, and every
+//     pixel is owned exactly once unless it lies on or below a cycle;
+//  3. every entry pixel (ring pixel with a donor in another tile) follows
+//     its receivers to the in-tile terminal and records it with the number
+//     of steps (first pass only).
 constexpr int kUpThreads = 128;
+constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
 
 struct UpTile {
-  uint8_t dir[kHalo][36];      // [c][r], one-pixel halo
-  int16_t rl[kTileCells];      // local receiver or an RL_* code
-  uint32_t pk[kTileCells];     // pointer jumping: next << 16 | depth
+  uint8_t dir[kHalo][36];   // [c][r], one-pixel halo
+  int16_t rl[kTileCells];   // local receiver or an RL_* code
+  int pend[kTileCells];     // in-tile donors not yet arrived
   long long acc[kTileCells];
   int h[kTileCells];
-  int16_t order[kTileCells];   // pixels sorted by depth
-  int cnt[kTileCells + 1];     // per depth: count, then start offset
-  uint8_t ent[kTileCells];     // pixel has a donor in another tile
-  int maxd;
   int nvalid;
+  int owned;
   int bad;
 };
+
+// Pixel index (jj * 32 + ii) of ring pixel k, 0 <= k < 124.
+__device__ __forceinline__ int ring_pixel(int k) {
+  if (k < kTile) return k * kTile;                      // ii = 0
+  if (k < 2 * kTile) return (k - kTile) * kTile + kTile - 1;  // ii = 31
+  if (k < 3 * kTile - 2) return k - 2 * kTile + 1;       // jj = 0, ii = 1..30
+  return (kTile - 1) * kTile + (k - 3 * kTile + 3);     // jj = 31, ii = 1..30
+}
 
 __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
   __shared__ UpTile t;
@@ -186,10 +197,10 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
         if (e < kHalo * kHalo) t.dir[e / kHalo][e % kHalo] = v[u];
       }
     }
-    for (int e = tid; e <= kTileCells; e += kUpThreads) t.cnt[e] = 0;
+    for (int e = tid; e < kTileCells; e += kUpThreads) t.pend[e] = 0;
     if (tid == 0) {
-      t.maxd = 0;
       t.nvalid = 0;
+      t.owned = 0;
       t.bad = 0;
     }
     __syncthreads();
@@ -201,11 +212,29 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
       const int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
       t.rl[e] = (int16_t)rl;
       bad |= rl == RL_BADDIR;
-      int ne = 0, hin = 0;
-      long long inflow = 0;
-      const bool ring = ii == 0 || jj == 0 || ii == kTile - 1 || jj == kTile - 1;
-      if (rl != RL_NONE) nvalid++;
-      if (rl != RL_NONE && ring) {  // only ring pixels have donors in other tiles
+      if (rl >= 0) atomicAdd(&t.pend[rl], 1);
+      long long w0 = 0;
+      if (rl != RL_NONE) {
+        nvalid++;
+        if (a.want_acc) w0 = a.w ? to_fixed(a.w[j * a.m + i], a.wshift, a.err) : 1LL;
+      }
+      t.acc[e] = w0;
+      t.h[e] = 0;
+    }
+    if (nvalid) atomicAdd(&t.nvalid, nvalid);
+    if (bad) t.bad = 1;
+    __syncthreads();
+
+    // Ring pixels: donors in other tiles (and their inflow, final pass).
+    bool entry = false;
+    int re = 0;
+    if (tid < kRing) {
+      re = ring_pixel(tid);
+      const int ii = re % kTile, jj = re / kTile;
+      const int64_t i = i0 + ii, j = j0 + jj;
+      if (t.rl[re] != RL_NONE) {
+        long long inflow = 0;
+        int hin = 0, ne = 0;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
           const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
@@ -220,125 +249,62 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
             if (a.want_h) hin = max(hin, a.cH[gq] + 1);
           }
         }
+        entry = ne > 0;
+        if (inflow) t.acc[re] += inflow;
+        if (hin) t.h[re] = hin;
       }
-      t.ent[e] = (uint8_t)(ne > 0);
-      long long w0 = 0;
-      if (a.want_acc && rl != RL_NONE)
-        w0 = a.w ? to_fixed(a.w[j * a.m + i], a.wshift, a.err) : 1LL;
-      t.acc[e] = w0 + inflow;
-      t.h[e] = hin;
-      t.pk[e] = rl >= 0 ? ((uint32_t)rl << 16) | 1u : ((uint32_t)e << 16);
     }
-    if (nvalid) atomicAdd(&t.nvalid, nvalid);
-    if (bad) t.bad = 1;
+    // Leaves, taken before any walk starts (a walk empties counts).
+    unsigned leaves = 0;
+#pragma unroll
+    for (int u = 0; u < kTileCells / kUpThreads; u++) {
+      const int e = tid + u * kUpThreads;
+      if (t.rl[e] != RL_NONE && t.pend[e] == 0) leaves |= 1u << u;
+    }
     __syncthreads();
 
-    // Pointer jumping (paths inside a tile are shorter than 1024 steps);
-    // stops as soon as every pixel points at its terminal.
-    for (int round = 0; round < 10; round++) {
-      int moved = 0;
-      for (int e = tid; e < kTileCells; e += kUpThreads) {
-        const uint32_t v = t.pk[e];
-        const int q = (int)(v >> 16);
-        if (q == e) continue;
-        const uint32_t w = t.pk[q];
-        if ((int)(w >> 16) == q) continue;  // q is the terminal already
-        t.pk[e] = (w & 0xffff0000u) | ((v & 0xffffu) + (w & 0xffffu));
-        moved = 1;
+    // Last arriver continues.
+    int owned = 0;
+    for (; leaves; leaves &= leaves - 1) {
+      int cur = tid + (__ffs(leaves) - 1) * kUpThreads;
+      long long v = t.acc[cur];
+      int hv = t.h[cur];
+      owned++;
+      for (int guard = 0; guard < kTileCells; guard++) {
+        const int q = t.rl[cur];
+        if (q < 0) break;  // exit, outlet or grid edge: nothing further in-tile
+        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
+        if (a.want_h) atomicMax(&t.h[q], hv + 1);
+        cuda::atomic_ref<int, cuda::thread_scope_block> pend(t.pend[q]);
+        if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) break;
+        cur = q;  // every donor of q has arrived: q is complete
+        owned++;
+        if (a.want_acc) v = t.acc[cur];
+        if (a.want_h) hv = t.h[cur];
       }
-      if (!__syncthreads_or(moved)) break;
     }
-    int cyc = 0, md = 0;
-    for (int e = tid; e < kTileCells; e += kUpThreads) {
-      if (t.rl[e] == RL_NONE) continue;
-      const uint32_t v = t.pk[e];
-      if (t.rl[v >> 16] >= 0) {  // never reached a terminal: a cycle
-        cyc = 1;
-        continue;
-      }
-      const int d = (int)(v & 0xffffu);
-      atomicAdd(&t.cnt[d], 1);
-      md = max(md, d);
-    }
-    if (cyc) atomicOr(a.err, ERR_CYCLE);
-    if (md) atomicMax(&t.maxd, md);
+    if (owned) atomicAdd(&t.owned, owned);
     __syncthreads();
-    const int maxd = t.maxd;
-    if (tid == 0) {  // exclusive offsets, deepest level first
-      int run = 0;
-      for (int d = maxd; d >= 0; d--) {
-        const int c = t.cnt[d];
-        t.cnt[d] = run;
-        run += c;
-      }
-    }
-    __syncthreads();
-    for (int e = tid; e < kTileCells; e += kUpThreads) {
-      if (t.rl[e] == RL_NONE) continue;
-      const uint32_t v = t.pk[e];
-      if (t.rl[v >> 16] >= 0) continue;
-      t.order[atomicAdd(&t.cnt[v & 0xffffu], 1)] = (int16_t)e;
-    }
-    __syncthreads();
-    // After the scatter cnt[d] is the end of level d = the start of level d-1.
-    // Levels of at most 32 pixels (the long, thin chains of carved flats) run
-    // on warp 0 alone with warp barriers; wider levels use the whole block.
-    {
-      bool warp_mode = false;
-      for (int d = maxd; d >= 1; d--) {
-        const int beg = d == maxd ? 0 : t.cnt[d + 1], end = t.cnt[d];
-        const bool narrow = end - beg <= 32;
-        if (!narrow && warp_mode) {
-          __syncthreads();  // the warp-0 levels are visible to every thread
-          warp_mode = false;
-        }
-        if (narrow) {
-          warp_mode = true;
-          if (tid < 32) {
-            const int k = beg + tid;
-            if (k < end) {
-              const int p = t.order[k];
-              const int q = t.rl[p];
-              if (a.want_acc)
-                atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
-              if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
-            }
-            __syncwarp();
-          }
-        } else {
-          for (int k = beg + tid; k < end; k += kUpThreads) {
-            const int p = t.order[k];
-            const int q = t.rl[p];
-            if (a.want_acc)
-              atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)t.acc[p]);
-            if (a.want_h) atomicMax(&t.h[q], t.h[p] + 1);
-          }
-          __syncthreads();
-        }
-      }
-      __syncthreads();
-    }
+    if (tid == 0 && t.owned != t.nvalid) atomicOr(a.err, ERR_CYCLE);
 
     if (a.phase == 1) {
       for (int e = tid; e < kTileCells; e += kUpThreads) {
-        const int rl = t.rl[e];
-        const int ii = e % kTile, jj = e / kTile;
-        const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
-        if (rl == RL_EXIT) {
-          if (a.want_acc) a.cacc[gp] = t.acc[e];
-          if (a.want_h) a.cH[gp] = t.h[e];
-          a.cpend[gp] = 0;
-          a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
-        }
-        if (t.ent[e]) {
-          const uint32_t v = t.pk[e];
-          const int term = (int)(v >> 16);
-          int x = -1;
-          if (t.rl[term] == RL_EXIT)
-            x = (int)((j0 + term / kTile) * a.m + (i0 + term % kTile));
-          a.xmap[gp] = x;
-          a.xsteps[gp] = (int)(v & 0xffffu);
-        }
+        if (t.rl[e] != RL_EXIT) continue;
+        const int64_t gp = (j0 + e / kTile) * a.m + (i0 + e % kTile);
+        if (a.want_acc) a.cacc[gp] = t.acc[e];
+        if (a.want_h) a.cH[gp] = t.h[e];
+        a.cpend[gp] = 0;
+        a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
+      }
+      if (entry) {  // the in-tile terminal of an entry pixel and its distance
+        int cur = re, steps = 0;
+        for (; steps < kTileCells && t.rl[cur] >= 0; steps++) cur = t.rl[cur];
+        int x = -1;
+        if (t.rl[cur] == RL_EXIT)
+          x = (int)((j0 + cur / kTile) * a.m + (i0 + cur % kTile));
+        const int64_t gp = (j0 + re / kTile) * a.m + (i0 + re % kTile);
+        a.xmap[gp] = x;
+        a.xsteps[gp] = steps;
       }
     } else {
       int hm = 0;
