@@ -305,15 +305,13 @@ struct Sun2 {
 
 constexpr int kHS = kTile + 4;  // 2-pixel halo for one-sided borders
 
-template <int MODE>  // 0: hillshade, 1: gradients, 2: hillshade backward
+template <int MODE>  // 0: hillshade, 1: gradients
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
                  const float *__restrict__ dem, const float *__restrict__ gout,
                  int64_t m, int64_t n, float twoh, float sx, float sy, float sz,
                  Sun2 s2) {
   __shared__ float z[kHS][kHS + 1];
-  __shared__ float hx[MODE == 2 ? kHS : 1][kHS + 1];
-  __shared__ float hy[MODE == 2 ? kHS : 1][kHS + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
@@ -337,49 +335,13 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
       }
   }
   __syncthreads();
-  if (MODE == 2) {
-    // dH/d(dx) and dH/d(dy) (times the upstream gradient) for the tile and a
-    // two-pixel ring: every DEM sample of the tile is read by stencils
-    // centred at most two pixels away.
-    for (int c = ty; c < kHS; c += kBlockY) {
-      int64_t j = j0 - 2 + c;
-      for (int r = tx; r < kHS; r += kBlockX) {
-        int64_t i = i0 - 2 + r;
-        float ax = 0.f, ay = 0.f;
-        if (i >= 0 && i < m && j >= 0 && j < n) {
-          auto zz = [&](int dc, int dr) {
-            int cc = c + dc, rr = r + dr;
-            if (cc < 0 || cc >= kHS || rr < 0 || rr >= kHS) {
-              int64_t gi = i + dr, gj = j + dc;
-              return (gi >= 0 && gi < m && gj >= 0 && gj < n) ? dem[gj * m + gi] : 0.0f;
-            }
-            return z[cc][rr];
-          };
-          float dx = axis_grad(zz(0, -2), zz(0, -1), zz(0, 0), zz(0, 1), zz(0, 2), i, m, twoh);
-          float dy = axis_grad(zz(-2, 0), zz(-1, 0), zz(0, 0), zz(1, 0), zz(2, 0), j, n, twoh);
-          float q = dx * dx + dy * dy + 1.0f;
-          float inv = 1.0f / sqrtf(q);
-          float num = -dx * sx - dy * sy + sz;
-          if (!isnan(num * inv)) {
-            float inv3 = inv * inv * inv;
-            float g = gout[j * m + i];
-            ax = g * (-sx * inv - num * dx * inv3);
-            ay = g * (-sy * inv - num * dy * inv3);
-          }
-        }
-        hx[c][r] = ax;
-        hy[c][r] = ay;
-      }
-    }
-    __syncthreads();
-  }
   for (int c = ty; c < kTile; c += kBlockY) {
     int64_t j = j0 + c;
     int64_t i = i0 + tx;
     if (j >= n || i >= m) continue;
     int r = tx + 2, cc = c + 2;
     int64_t p = j * m + i;
-    if (MODE == 0 || MODE == 1) {
+    {
       float dx = axis_grad(z[cc][r - 2], z[cc][r - 1], z[cc][r], z[cc][r + 1],
                            z[cc][r + 2], i, m, twoh);
       float dy = axis_grad(z[cc - 2][r], z[cc - 1][r], z[cc][r], z[cc + 1][r],
@@ -409,45 +371,126 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
         out0[p] = dx;
         out1[p] = dy;
       }
-    } else {
-      // Transposed stencils: sample (i, j) receives from the centres whose
-      // stencil reads it.  Along i: centre i+1 reads i with -1 (central),
-      // centre i-1 reads i with +1; the one-sided border stencils at 0 and
-      // m-1 read i in {0,1,2} and {m-3,m-2,m-1}.
-      float acc = 0.0f;
-      // along i (axis length m)
-      for (int d = -2; d <= 2; d++) {
-        int64_t k = i + d;  // centre position
-        if (k < 0 || k >= m) continue;
-        float a = hx[cc][r + d];
-        float w = 0.0f;
-        int off = (int)(i - k);  // sample offset relative to the centre
-        if (k == 0) {
-          w = (off == 0) ? -3.f : (off == 1) ? 4.f : (off == 2) ? -1.f : 0.f;
-        } else if (k == m - 1) {
-          w = (off == 0) ? 3.f : (off == -1) ? -4.f : (off == -2) ? 1.f : 0.f;
-        } else {
-          w = (off == 1) ? 1.f : (off == -1) ? -1.f : 0.f;
-        }
-        if (w != 0.f) acc += w * a;
-      }
-      for (int d = -2; d <= 2; d++) {
-        int64_t k = j + d;
-        if (k < 0 || k >= n) continue;
-        float a = hy[cc + d][r];
-        float w = 0.0f;
-        int off = (int)(j - k);
-        if (k == 0) {
-          w = (off == 0) ? -3.f : (off == 1) ? 4.f : (off == 2) ? -1.f : 0.f;
-        } else if (k == n - 1) {
-          w = (off == 0) ? 3.f : (off == -1) ? -4.f : (off == -2) ? 1.f : 0.f;
-        } else {
-          w = (off == 1) ? 1.f : (off == -1) ? -1.f : 0.f;
-        }
-        if (w != 0.f) acc += w * a;
-      }
-      out0[p] = acc / twoh;
     }
+  }
+}
+
+// Weight with which the stencil centred at k (axis length len) reads the
+// sample at k + off (src/hillshade.c:23-76: central differences inside,
+// second-order one-sided differences on the first and last sample).
+__device__ __forceinline__ float stencil_weight(int64_t k, int64_t len, int off) {
+  if (k == 0) return (off == 0) ? -3.f : (off == 1) ? 4.f : (off == 2) ? -1.f : 0.f;
+  if (k == len - 1) return (off == 0) ? 3.f : (off == -1) ? -4.f : (off == -2) ? 1.f : 0.f;
+  return (off == 1) ? 1.f : (off == -1) ? -1.f : 0.f;
+}
+
+// Adjoint of hillshade w.r.t. the DEM: grad_dem = S^T (dH/d(dx) * g, dH/d(dy)
+// * g), S the gradient stencils.  A 32 x 32 output tile needs dH/d(dx),
+// dH/d(dy) at centres up to two pixels away, whose stencils read the DEM up
+// to four pixels away: the block stages the DEM with a 4-pixel halo and the
+// upstream gradient with a 2-pixel halo, evaluates the 36 x 36 centres from
+// shared memory, then applies the transposed stencils.
+constexpr int kHB = kTile + 8;  // DEM tile with a 4-pixel halo
+constexpr int kHG = kTile + 4;  // centres with a 2-pixel halo
+
+__global__ void __launch_bounds__(kBlockX * kBlockY)
+hillshade_bwd_kernel(float *__restrict__ gdem, const float *__restrict__ dem,
+                     const float *__restrict__ gout, int64_t m, int64_t n,
+                     float twoh, float sx, float sy, float sz) {
+  __shared__ float z[kHB][kHB + 1];
+  __shared__ float gx[kHG][kHG + 1];  // upstream gradient, then dL/d(dx)
+  __shared__ float gy[kHG][kHG + 1];  // dL/d(dy)
+  constexpr int kThreads = kBlockX * kBlockY;
+  const int tid = threadIdx.y * kBlockX + threadIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.x * kTile;
+  const int64_t j0 = (int64_t)blockIdx.y * kTile;
+  {  // stage the DEM and the upstream gradient, every load in flight at once
+    constexpr int kZ = (kHB * kHB + kThreads - 1) / kThreads;
+    constexpr int kG = (kHG * kHG + kThreads - 1) / kThreads;
+    float vz[kZ], vg[kG];
+#pragma unroll
+    for (int u = 0; u < kZ; u++) {
+      const int e = tid + u * kThreads;
+      const int c = e / kHB, r = e % kHB;
+      const int64_t i = i0 - 4 + r, j = j0 - 4 + c;
+      vz[u] = (e < kHB * kHB && i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < kG; u++) {
+      const int e = tid + u * kThreads;
+      const int c = e / kHG, r = e % kHG;
+      const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
+      vg[u] = (e < kHG * kHG && i >= 0 && i < m && j >= 0 && j < n) ? gout[j * m + i] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < kZ; u++) {
+      const int e = tid + u * kThreads;
+      if (e < kHB * kHB) z[e / kHB][e % kHB] = vz[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kG; u++) {
+      const int e = tid + u * kThreads;
+      if (e < kHG * kHG) gx[e / kHG][e % kHG] = vg[u];
+    }
+  }
+  __syncthreads();
+  // dH/d(dx) * g and dH/d(dy) * g at the 36 x 36 centres.
+  for (int e = tid; e < kHG * kHG; e += kThreads) {
+    const int c = e / kHG, r = e % kHG;
+    const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
+    float ax = 0.f, ay = 0.f;
+    if (i >= 0 && i < m && j >= 0 && j < n) {
+      const int zc = c + 2, zr = r + 2;
+      const float dx = axis_grad(z[zc][zr - 2], z[zc][zr - 1], z[zc][zr], z[zc][zr + 1],
+                                 z[zc][zr + 2], i, m, twoh);
+      const float dy = axis_grad(z[zc - 2][zr], z[zc - 1][zr], z[zc][zr], z[zc + 1][zr],
+                                 z[zc + 2][zr], j, n, twoh);
+      const float q = dx * dx + dy * dy + 1.0f;
+      const float inv = 1.0f / sqrtf(q);
+      const float num = -dx * sx - dy * sy + sz;
+      if (!isnan(num * inv)) {
+        const float inv3 = inv * inv * inv;
+        const float g = gx[c][r];
+        ax = g * (-sx * inv - num * dx * inv3);
+        ay = g * (-sy * inv - num * dy * inv3);
+      }
+    }
+    gx[c][r] = ax;  // this thread alone read gx[c][r]
+    gy[c][r] = ay;
+  }
+  __syncthreads();
+  // Transposed stencils: sample (i, j) receives from the centres whose
+  // stencil reads it.  Away from the borders only the two central neighbours
+  // along each axis contribute.
+  const int tx = threadIdx.x;
+  const int64_t i = i0 + tx;
+  for (int cy = threadIdx.y; cy < kTile; cy += kBlockY) {
+    const int64_t j = j0 + cy;
+    if (j >= n || i >= m) continue;
+    const int r = tx + 2, cc = cy + 2;
+    float acc;
+    if (i >= 3 && i <= m - 4 && j >= 3 && j <= n - 4) {
+      acc = gx[cc][r - 1] - gx[cc][r + 1];
+      acc = acc + gy[cc - 1][r];
+      acc = acc - gy[cc + 1][r];
+    } else {
+      acc = 0.0f;
+#pragma unroll
+      for (int d = -2; d <= 2; d++) {
+        const int64_t k = i + d;  // centre position along i
+        if (k < 0 || k >= m) continue;
+        const float w = stencil_weight(k, m, (int)(i - k));
+        if (w != 0.f) acc += w * gx[cc][r + d];
+      }
+#pragma unroll
+      for (int d = -2; d <= 2; d++) {
+        const int64_t k = j + d;
+        if (k < 0 || k >= n) continue;
+        const float w = stencil_weight(k, n, (int)(j - k));
+        if (w != 0.f) acc += w * gy[cc + d][r];
+      }
+    }
+    gdem[j * m + i] = acc / twoh;
   }
 }
 
@@ -515,8 +558,8 @@ tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,
                                       const GridDims &g, cudaStream_t st) {
   float sx, sy, sz;
   sun_vector(azimuth, altitude, &sx, &sy, &sz);
-  TT_LAUNCH(hillshade_kernel<2>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            grad_dem, nullptr, dem, grad_out, g.m, g.n, 2 * cellsize, sx, sy, sz, Sun2{});
+  TT_LAUNCH(hillshade_bwd_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
+            grad_dem, dem, grad_out, g.m, g.n, 2 * cellsize, sx, sy, sz);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
