@@ -61,6 +61,16 @@ enum : int {
 
 enum : int { ERR_CYCLE = 1, ERR_BADDIR = 2, ERR_WEIGHT = 4 };
 
+// One exit of the coarse forest, updated as a unit by a 128-bit
+// compare-and-swap: a donor adds its total, raises the longest path and
+// counts itself off in one atomic step, so the donor that takes `pend` to
+// zero reads the complete totals from the swap itself.
+struct __align__(16) CoarseCell {
+  long long sum;  // fixed-point total (local, then with all coarse donors)
+  int h;          // longest upstream path
+  int pend;       // coarse donors not yet arrived
+};
+
 struct UpArgs {
   const uint8_t *dir;
   int64_t m, n;
@@ -68,12 +78,13 @@ struct UpArgs {
   unsigned order;
   const float *w;  // nullptr: unit weights
   int wshift;      // fixed-point scale 2^wshift
-  int phase;       // 1: local pass, 3: final pass
+  int phase;       // 1: local pass (forest_up_kernel), 3: final pass (forest_fin_kernel)
   bool want_acc;
   bool want_h;
-  long long *cacc;  // per exit: local (then total) fixed-point sum
-  int *cH;          // per exit: longest upstream path
-  int *cpend;       // per exit: pending coarse donors
+  CoarseCell *cell;  // per exit: sums, longest path, pending coarse donors
+  long long *lacc;   // per pixel: in-tile (local) fixed-point total
+  int16_t *lrl;      // per pixel: local receiver or RL_* code
+  uint8_t *emask;    // per tile and ring pixel: directions of donors in other tiles
   int *xmap;        // per entry pixel: exit reached in-tile, or -1
   int *xsteps;      // per entry pixel: steps to that exit
   int *elist;       // list of exits
@@ -105,21 +116,6 @@ __device__ __forceinline__ long long to_fixed(float w, int k, int *err) {
   else
     v = 0;
   return (bits >> 31) ? -v : v;
-}
-
-__device__ __forceinline__ void load_dir_tile(uint8_t (*dir)[36],
-                                              const uint8_t *__restrict__ g,
-                                              int64_t m, int64_t n, int64_t i0,
-                                              int64_t j0, int lane) {
-  for (int c = 0; c < kHalo; c++) {
-    int64_t j = j0 - 1 + c;
-    for (int r = lane; r < kHalo; r += 32) {
-      int64_t i = i0 - 1 + r;
-      uint8_t v = 0;
-      if (i >= 0 && i < m && j >= 0 && j < n) v = g[j * m + i];
-      dir[c][r] = v;
-    }
-  }
 }
 
 // Receiver code of tile pixel (ii, jj).
@@ -225,16 +221,14 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
     if (bad) t.bad = 1;
     __syncthreads();
 
-    // Ring pixels: donors in other tiles (and their inflow, final pass).
+    // Ring pixels with donors in other tiles (entry pixels).
     bool entry = false;
     int re = 0;
     if (tid < kRing) {
       re = ring_pixel(tid);
       const int ii = re % kTile, jj = re / kTile;
-      const int64_t i = i0 + ii, j = j0 + jj;
+      unsigned ne = 0;
       if (t.rl[re] != RL_NONE) {
-        long long inflow = 0;
-        int hin = 0, ne = 0;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
           const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
@@ -242,17 +236,11 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
           if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) continue;
           const unsigned dq = t.dir[qc][qr];
           if (dq == 0 || d8_bit(dq) != k) continue;
-          ne++;
-          if (a.phase == 3) {
-            const int64_t gq = (j - dj) * a.m + (i - di);
-            if (a.want_acc) inflow += a.cacc[gq];
-            if (a.want_h) hin = max(hin, a.cH[gq] + 1);
-          }
+          ne |= 1u << k;
         }
-        entry = ne > 0;
-        if (inflow) t.acc[re] += inflow;
-        if (hin) t.h[re] = hin;
+        entry = ne != 0;
       }
+      a.emask[(size_t)tile * kRing + tid] = (uint8_t)ne;
     }
     // Leaves, taken before any walk starts (a walk empties counts).
     unsigned leaves = 0;
@@ -287,44 +275,109 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
     __syncthreads();
     if (tid == 0 && t.owned != t.nvalid) atomicOr(a.err, ERR_CYCLE);
 
-    if (a.phase == 1) {
-      for (int e = tid; e < kTileCells; e += kUpThreads) {
-        if (t.rl[e] != RL_EXIT) continue;
-        const int64_t gp = (j0 + e / kTile) * a.m + (i0 + e % kTile);
-        if (a.want_acc) a.cacc[gp] = t.acc[e];
-        if (a.want_h) a.cH[gp] = t.h[e];
-        a.cpend[gp] = 0;
-        a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
-      }
-      if (entry) {  // the in-tile terminal of an entry pixel and its distance
-        int cur = re, steps = 0;
-        for (; steps < kTileCells && t.rl[cur] >= 0; steps++) cur = t.rl[cur];
-        int x = -1;
-        if (t.rl[cur] == RL_EXIT)
-          x = (int)((j0 + cur / kTile) * a.m + (i0 + cur % kTile));
-        const int64_t gp = (j0 + re / kTile) * a.m + (i0 + re % kTile);
-        a.xmap[gp] = x;
-        a.xsteps[gp] = steps;
-      }
-    } else {
-      int hm = 0;
-      for (int e = tid; e < kTileCells; e += kUpThreads) {
-        const int ii = e % kTile, jj = e / kTile;
-        const int64_t i = i0 + ii, j = j0 + jj;
-        if (i >= a.m || j >= a.n) continue;
-        const int64_t gp = j * a.m + i;
-        if (a.want_acc) {
-          const float v = __ll2float_rn(t.acc[e]);
-          a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
-        }
-        if (a.want_h) {
-          a.h_out[gp] = t.h[e];
-          hm = max(hm, t.h[e]);
-        }
-      }
-      if (a.want_h && hm) atomicMax(a.hmax, hm);
+    for (int e = tid; e < kTileCells; e += kUpThreads) {
+      const int ii = e % kTile, jj = e / kTile;
+      const int64_t i = i0 + ii, j = j0 + jj;
+      if (i >= a.m || j >= a.n) continue;
+      const int64_t gp = j * a.m + i;
+      if (a.want_acc) a.lacc[gp] = t.acc[e];  // local totals for the final pass
+      if (a.want_h) a.h_out[gp] = t.h[e];
+      a.lrl[gp] = t.rl[e];
+      if (t.rl[e] != RL_EXIT) continue;
+      a.cell[gp] = CoarseCell{a.want_acc ? t.acc[e] : 0LL, a.want_h ? t.h[e] : 0, 0};
+      a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
+    }
+    if (entry) {  // the in-tile terminal of an entry pixel and its distance
+      int cur = re, steps = 0;
+      for (; steps < kTileCells && t.rl[cur] >= 0; steps++) cur = t.rl[cur];
+      int x = -1;
+      if (t.rl[cur] == RL_EXIT)
+        x = (int)((j0 + cur / kTile) * a.m + (i0 + cur % kTile));
+      const int64_t gp = (j0 + re / kTile) * a.m + (i0 + re % kTile);
+      a.xmap[gp] = x;
+      a.xsteps[gp] = steps;
     }
     if (tid == 0 && t.bad) atomicOr(a.err, ERR_BADDIR);
+    __syncthreads();
+  }
+}
+
+// Final pass: a pixel's total is its local total plus the inflow of every
+// entry pixel whose in-tile path passes through it.  The first pass left the
+// local totals, every pixel's receiver code and, per ring pixel, the
+// directions of its donors in other tiles.  Each entry pixel (one thread per
+// ring pixel) gathers its inflow from the coarse cells of those donors and
+// walks its path to the terminal, adding the inflow and raising h to
+// (longest path into the entry) + (steps walked).
+struct FinTile {
+  long long acc[kTileCells];
+  int h[kTileCells];
+  int16_t rl[kTileCells];
+};
+
+__global__ void __launch_bounds__(kUpThreads, 8) forest_fin_kernel(UpArgs a) {
+  __shared__ FinTile t;
+  const int tid = threadIdx.x;
+  const int T = a.tm * a.tn;
+  constexpr int kP = kTileCells / kUpThreads;
+  for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
+    const int ti = tile % a.tm, tj = tile / a.tm;
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    const int64_t ilim = a.m - i0, jlim = a.n - j0;  // in-grid: ii < ilim, jj < jlim
+#pragma unroll
+    for (int u = 0; u < kP; u++) {  // local totals and receivers
+      const int e = tid + u * kUpThreads;
+      const int ii = e % kTile, jj = e / kTile;
+      const bool in = ii < ilim && jj < jlim;
+      const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
+      if (a.want_acc) t.acc[e] = in ? a.lacc[gp] : 0LL;
+      if (a.want_h) t.h[e] = in ? a.h_out[gp] : 0;
+      t.rl[e] = in ? a.lrl[gp] : (int16_t)RL_NONE;
+    }
+    unsigned mask = 0;
+    if (tid < kRing) mask = a.emask[(size_t)tile * kRing + tid];
+    __syncthreads();
+
+    if (mask) {  // an entry pixel: carry its inflow down its path
+      const int re = ring_pixel(tid);
+      const int64_t i = i0 + re % kTile, j = j0 + re / kTile;
+      long long inflow = 0;
+      int hin = 0;
+      for (unsigned mk = mask; mk; mk &= mk - 1) {
+        const int k = __ffs(mk) - 1;
+        const CoarseCell cq = a.cell[(j - d8_dj(k, a.order)) * a.m + (i - d8_di(k, a.order))];
+        inflow += cq.sum;
+        hin = max(hin, cq.h + 1);
+      }
+      int cur = re;
+      for (int d = 0; d < kTileCells; d++) {
+        if (a.want_acc && inflow)
+          atomicAdd((unsigned long long *)&t.acc[cur], (unsigned long long)inflow);
+        if (a.want_h) atomicMax(&t.h[cur], hin + d);
+        const int q = t.rl[cur];
+        if (q < 0) break;
+        cur = q;
+      }
+    }
+    __syncthreads();
+
+    int hm = 0;
+#pragma unroll
+    for (int u = 0; u < kP; u++) {
+      const int e = tid + u * kUpThreads;
+      const int ii = e % kTile, jj = e / kTile;
+      if (ii >= ilim || jj >= jlim) continue;
+      const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
+      if (a.want_acc) {
+        const float v = __ll2float_rn(t.acc[e]);
+        a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
+      }
+      if (a.want_h) {
+        a.h_out[gp] = t.h[e];
+        hm = max(hm, t.h[e]);
+      }
+    }
+    if (a.want_h && hm) atomicMax(a.hmax, hm);
     __syncthreads();
   }
 }
@@ -344,7 +397,7 @@ __global__ void coarse_link_kernel(const int *__restrict__ elist,
                                    unsigned order, const int *__restrict__ xmap,
                                    const int *__restrict__ xsteps,
                                    int *__restrict__ cnext, int *__restrict__ chop,
-                                   int *__restrict__ cpend) {
+                                   CoarseCell *__restrict__ cell) {
   const int E = *ecount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
     int e = elist[a];
@@ -352,56 +405,72 @@ __global__ void coarse_link_kernel(const int *__restrict__ elist,
     int nx = xmap[r];
     cnext[e] = nx;
     chop[e] = 1 + xsteps[r];
-    if (nx >= 0) atomicAdd(&cpend[nx], 1);
+    if (nx >= 0) atomicAdd(&cell[nx].pend, 1);
   }
 }
 
 __global__ void coarse_leaves_kernel(const int *__restrict__ elist,
                                      const int *__restrict__ ecount,
-                                     const int *__restrict__ cpend,
+                                     const CoarseCell *__restrict__ cell,
                                      int *__restrict__ leaves,
                                      int *__restrict__ lcount) {
   const int E = *ecount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
     int e = elist[a];
-    if (cpend[e] == 0) leaves[atomicAdd(lcount, 1)] = e;
+    if (cell[e].pend == 0) leaves[atomicAdd(lcount, 1)] = e;
   }
 }
 
+// Relaxed 128-bit compare-and-swap: (lo, hi) holds the expected value on
+// entry and the value found on return.
+__device__ __forceinline__ void cas128(CoarseCell *p, unsigned long long &lo,
+                                       unsigned long long &hi, unsigned long long nlo,
+                                       unsigned long long nhi) {
+  asm volatile(
+      "{\n\t.reg .b128 c, v, d;\n\tmov.b128 c, {%0, %1};\n\tmov.b128 v, {%2, %3};\n\t"
+      "atom.global.cas.b128 d, [%4], c, v;\n\tmov.b128 {%0, %1}, d;\n\t}"
+      : "+l"(lo), "+l"(hi)
+      : "l"(nlo), "l"(nhi), "l"(p)
+      : "memory");
+}
+
+// Last-arriver walk over the exits: a walker owns a complete exit, folds its
+// totals into the next exit downstream with one compare-and-swap, and
+// continues only if it was the last donor to arrive.
 __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
                                    const int *__restrict__ lcount,
                                    const int *__restrict__ cnext,
                                    const int *__restrict__ chop,
-                                   long long *cacc, int *cH, int *cpend,
-                                   bool want_acc, bool want_h, int *processed,
-                                   int limit) {
+                                   CoarseCell *cell, int *processed, int limit) {
   const int L = *lcount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < L; a += gridDim.x * blockDim.x) {
     int e = leaves[a];
     int n_done = 0;
-    // The walker owns e: every coarse donor has arrived, so its totals are
-    // final and were published by the acquiring decrement below.
-    long long v = want_acc ? cuda::atomic_ref<long long, cuda::thread_scope_device>(cacc[e])
-                                 .load(cuda::std::memory_order_relaxed)
-                           : 0;
-    int hv = want_h ? cuda::atomic_ref<int, cuda::thread_scope_device>(cH[e])
-                          .load(cuda::std::memory_order_relaxed)
-                    : 0;
+    // A leaf has no coarse donors: its cell was completed by earlier kernels.
+    const longlong2 c0 = __ldcg(reinterpret_cast<const longlong2 *>(&cell[e]));
+    long long v = c0.x;
+    int hv = (int)(unsigned)(unsigned long long)c0.y;
     for (int guard = 0; guard < limit; guard++) {
       n_done++;
       const int nx = cnext[e];
       if (nx < 0) break;
-      if (want_acc) atomicAdd((unsigned long long *)&cacc[nx], (unsigned long long)v);
-      if (want_h) atomicMax(&cH[nx], hv + chop[e]);
-      cuda::atomic_ref<int, cuda::thread_scope_device> pend(cpend[nx]);
-      if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) break;
-      e = nx;
-      if (want_acc)
-        v = cuda::atomic_ref<long long, cuda::thread_scope_device>(cacc[e])
-                .load(cuda::std::memory_order_relaxed);
-      if (want_h)
-        hv = cuda::atomic_ref<int, cuda::thread_scope_device>(cH[e])
-                 .load(cuda::std::memory_order_relaxed);
+      const int hop = chop[e];
+      const longlong2 g = __ldcg(reinterpret_cast<const longlong2 *>(&cell[nx]));
+      unsigned long long lo = (unsigned long long)g.x, hi = (unsigned long long)g.y;
+      unsigned long long nlo, nhi;
+      for (;;) {
+        const int oh = (int)(unsigned)hi, op = (int)(unsigned)(hi >> 32);
+        nlo = lo + (unsigned long long)v;
+        nhi = (unsigned long long)(unsigned)max(oh, hv + hop) |
+              ((unsigned long long)(unsigned)(op - 1) << 32);
+        const unsigned long long elo = lo, ehi = hi;
+        cas128(&cell[nx], lo, hi, nlo, nhi);
+        if (lo == elo && hi == ehi) break;  // swapped
+      }
+      if ((int)(unsigned)(hi >> 32) != 1) break;  // other donors still to come
+      e = nx;  // every donor of nx has arrived: its totals are final
+      v = (long long)nlo;
+      hv = (int)(unsigned)nhi;
     }
     atomicAdd(processed, n_done);
   }
@@ -724,8 +793,11 @@ int list_grid(int64_t n) {
 }
 
 struct UpWork {
-  long long *cacc;
-  int *cH, *cpend, *cnext, *chop, *xmap, *xsteps, *elist, *leaves, *h;
+  CoarseCell *cell;
+  long long *lacc;
+  int16_t *lrl;
+  uint8_t *emask;
+  int *cnext, *chop, *xmap, *xsteps, *elist, *leaves, *h;
   int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err, [5] maxabs
 };
 
@@ -733,14 +805,16 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
                         UpWork &w) {
   const size_t N = (size_t)g.cells();
   Workspace &ws = workspace();
-  size_t need = 256 + 8 * align_up(N * 4) + (want_acc ? align_up(N * 8) : 0) +
-                (want_h ? 2 * align_up(N * 4) : 0) + 4096;
+  size_t need = 256 + align_up(N * sizeof(CoarseCell)) + 6 * align_up(N * 4) +
+                (want_acc ? align_up(N * 8) : 0) + (want_h ? align_up(N * 4) : 0) +
+                align_up(N * 2) + align_up((size_t)g.tiles() * kRing) + 4096;
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   w.counters = (int *)ws.take(256);
-  w.cacc = want_acc ? (long long *)ws.take(N * 8) : nullptr;
-  w.cH = want_h ? (int *)ws.take(N * 4) : nullptr;
+  w.cell = (CoarseCell *)ws.take(N * sizeof(CoarseCell));
+  w.lacc = want_acc ? (long long *)ws.take(N * 8) : nullptr;
+  w.lrl = (int16_t *)ws.take(N * 2);
+  w.emask = (uint8_t *)ws.take((size_t)g.tiles() * kRing);
   w.h = want_h ? (int *)ws.take(N * 4) : nullptr;
-  w.cpend = (int *)ws.take(N * 4);
   w.cnext = (int *)ws.take(N * 4);
   w.chop = (int *)ws.take(N * 4);
   w.xmap = (int *)ws.take(N * 4);
@@ -768,9 +842,10 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.phase = 1;
   a.want_acc = want_acc;
   a.want_h = want_h;
-  a.cacc = w.cacc;
-  a.cH = w.cH;
-  a.cpend = w.cpend;
+  a.cell = w.cell;
+  a.lacc = w.lacc;
+  a.lrl = w.lrl;
+  a.emask = w.emask;
   a.xmap = w.xmap;
   a.xsteps = w.xsteps;
   a.elist = w.elist;
@@ -783,14 +858,14 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
-            g.m, order, w.xmap, w.xsteps, w.cnext, w.chop, w.cpend);
+            g.m, order, w.xmap, w.xsteps, w.cnext, w.chop, w.cell);
   TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.elist, w.counters + 0,
-            w.cpend, w.leaves, w.counters + 1);
+            w.cell, w.leaves, w.counters + 1);
   TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1,
-            w.cnext, w.chop, w.cacc, w.cH, w.cpend, want_acc, want_h,
-            w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
+            w.cnext, w.chop, w.cell, w.counters + 2,
+            (int)std::min<int64_t>(g.cells(), INT_MAX));
   a.phase = 3;
-  TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
+  TT_LAUNCH(forest_fin_kernel, tgrid, kUpThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
@@ -872,7 +947,7 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
   if (s == TT_CUDA_ERR_CYCLE) return s;
   const int H = h6[3] + 1;
   // hist, off and cursor reuse the coarse arrays (no longer needed).
-  int *hist = w.cpend, *off = w.cnext, *cursor = w.chop;
+  int *hist = w.xmap, *off = w.cnext, *cursor = w.chop;
   if ((int64_t)H > g.cells()) return TT_CUDA_ERR_CYCLE;
   TT_CHECK(cudaMemsetAsync(hist, 0, (size_t)H * 4, st));
   TT_CHECK(cudaMemsetAsync(cursor, 0, (size_t)H * 4, st));
