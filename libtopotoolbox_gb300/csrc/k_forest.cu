@@ -81,13 +81,14 @@ struct UpArgs {
   int phase;       // 1: local pass (forest_up_kernel), 3: final pass (forest_fin_kernel)
   bool want_acc;
   bool want_h;
-  CoarseCell *cell;  // per exit: sums, longest path, pending coarse donors
+  CoarseCell *ccell;  // per exit id: sums, longest path, pending coarse donors
+  CoarseCell *cell;   // per exit pixel: final totals, read by the final pass
   long long *lacc;   // per pixel: in-tile (local) fixed-point total
   int16_t *lrl;      // per pixel: local receiver or RL_* code
   uint8_t *emask;    // per tile and ring pixel: directions of donors in other tiles
-  int *xmap;        // per entry pixel: exit reached in-tile, or -1
+  int *xmap;        // per entry pixel: id of the exit reached in-tile, or -1
   int *xsteps;      // per entry pixel: steps to that exit
-  int *elist;       // list of exits
+  int *elist;       // per exit id: the exit's pixel
   int *ecount;
   float *acc_out;
   int *h_out;
@@ -284,15 +285,16 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
       if (a.want_h) a.h_out[gp] = t.h[e];
       a.lrl[gp] = t.rl[e];
       if (t.rl[e] != RL_EXIT) continue;
-      a.cell[gp] = CoarseCell{a.want_acc ? t.acc[e] : 0LL, a.want_h ? t.h[e] : 0, 0};
-      a.elist[atomicAdd(a.ecount, 1)] = (int)gp;
+      const int id = atomicAdd(a.ecount, 1);  // dense exit ids
+      a.ccell[id] = CoarseCell{a.want_acc ? t.acc[e] : 0LL, a.want_h ? t.h[e] : 0, 0};
+      a.elist[id] = (int)gp;
+      t.pend[e] = id;  // the counts are spent: keep the exit's id there
     }
+    __syncthreads();
     if (entry) {  // the in-tile terminal of an entry pixel and its distance
       int cur = re, steps = 0;
       for (; steps < kTileCells && t.rl[cur] >= 0; steps++) cur = t.rl[cur];
-      int x = -1;
-      if (t.rl[cur] == RL_EXIT)
-        x = (int)((j0 + cur / kTile) * a.m + (i0 + cur % kTile));
+      const int x = t.rl[cur] == RL_EXIT ? t.pend[cur] : -1;
       const int64_t gp = (j0 + re / kTile) * a.m + (i0 + re % kTile);
       a.xmap[gp] = x;
       a.xsteps[gp] = steps;
@@ -390,35 +392,31 @@ __device__ __forceinline__ int64_t receiver_of(const uint8_t *dir, int64_t p,
   return (j + d8_dj(k, order)) * m + (i + d8_di(k, order));
 }
 
-// Coarse links: cnext(e) = exit reached from receiver(e), hop = 1 + steps.
+// Coarse links, over exit ids: link(e) = {next exit, hops}, the exit
+// reached in-tile from receiver(e) and 1 + the steps to it.
 __global__ void coarse_link_kernel(const int *__restrict__ elist,
                                    const int *__restrict__ ecount,
                                    const uint8_t *__restrict__ dir, int64_t m,
                                    unsigned order, const int *__restrict__ xmap,
                                    const int *__restrict__ xsteps,
-                                   int *__restrict__ cnext, int *__restrict__ chop,
-                                   CoarseCell *__restrict__ cell) {
+                                   int2 *__restrict__ link,
+                                   CoarseCell *__restrict__ ccell) {
   const int E = *ecount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
-    int e = elist[a];
-    int64_t r = receiver_of(dir, e, m, order);
-    int nx = xmap[r];
-    cnext[e] = nx;
-    chop[e] = 1 + xsteps[r];
-    if (nx >= 0) atomicAdd(&cell[nx].pend, 1);
+    const int64_t r = receiver_of(dir, elist[a], m, order);
+    const int nx = xmap[r];
+    link[a] = make_int2(nx, 1 + xsteps[r]);
+    if (nx >= 0) atomicAdd(&ccell[nx].pend, 1);
   }
 }
 
-__global__ void coarse_leaves_kernel(const int *__restrict__ elist,
-                                     const int *__restrict__ ecount,
-                                     const CoarseCell *__restrict__ cell,
+__global__ void coarse_leaves_kernel(const int *__restrict__ ecount,
+                                     const CoarseCell *__restrict__ ccell,
                                      int *__restrict__ leaves,
                                      int *__restrict__ lcount) {
   const int E = *ecount;
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
-    int e = elist[a];
-    if (cell[e].pend == 0) leaves[atomicAdd(lcount, 1)] = e;
-  }
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x)
+    if (ccell[a].pend == 0) leaves[atomicAdd(lcount, 1)] = a;
 }
 
 // Relaxed 128-bit compare-and-swap: (lo, hi) holds the expected value on
@@ -436,44 +434,55 @@ __device__ __forceinline__ void cas128(CoarseCell *p, unsigned long long &lo,
 
 // Last-arriver walk over the exits: a walker owns a complete exit, folds its
 // totals into the next exit downstream with one compare-and-swap, and
-// continues only if it was the last donor to arrive.
+// continues only if it was the last donor to arrive.  The next exit's link
+// is loaded together with its cell, so a hop costs two dependent accesses.
 __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
                                    const int *__restrict__ lcount,
-                                   const int *__restrict__ cnext,
-                                   const int *__restrict__ chop,
-                                   CoarseCell *cell, int *processed, int limit) {
+                                   const int2 *__restrict__ link,
+                                   CoarseCell *ccell, int *processed, int limit) {
   const int L = *lcount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < L; a += gridDim.x * blockDim.x) {
-    int e = leaves[a];
+    const int e0 = leaves[a];
     int n_done = 0;
     // A leaf has no coarse donors: its cell was completed by earlier kernels.
-    const longlong2 c0 = __ldcg(reinterpret_cast<const longlong2 *>(&cell[e]));
+    const longlong2 c0 = __ldcg(reinterpret_cast<const longlong2 *>(&ccell[e0]));
     long long v = c0.x;
     int hv = (int)(unsigned)(unsigned long long)c0.y;
+    int2 l = link[e0];
     for (int guard = 0; guard < limit; guard++) {
       n_done++;
-      const int nx = cnext[e];
+      const int nx = l.x;
       if (nx < 0) break;
-      const int hop = chop[e];
-      const longlong2 g = __ldcg(reinterpret_cast<const longlong2 *>(&cell[nx]));
+      const longlong2 g = __ldcg(reinterpret_cast<const longlong2 *>(&ccell[nx]));
+      const int2 ln = link[nx];
       unsigned long long lo = (unsigned long long)g.x, hi = (unsigned long long)g.y;
       unsigned long long nlo, nhi;
       for (;;) {
         const int oh = (int)(unsigned)hi, op = (int)(unsigned)(hi >> 32);
         nlo = lo + (unsigned long long)v;
-        nhi = (unsigned long long)(unsigned)max(oh, hv + hop) |
+        nhi = (unsigned long long)(unsigned)max(oh, hv + l.y) |
               ((unsigned long long)(unsigned)(op - 1) << 32);
         const unsigned long long elo = lo, ehi = hi;
-        cas128(&cell[nx], lo, hi, nlo, nhi);
+        cas128(&ccell[nx], lo, hi, nlo, nhi);
         if (lo == elo && hi == ehi) break;  // swapped
       }
       if ((int)(unsigned)(hi >> 32) != 1) break;  // other donors still to come
-      e = nx;  // every donor of nx has arrived: its totals are final
-      v = (long long)nlo;
+      v = (long long)nlo;  // every donor of nx has arrived: its totals are final
       hv = (int)(unsigned)nhi;
+      l = ln;
     }
     atomicAdd(processed, n_done);
   }
+}
+
+// Final exit totals back to pixel-indexed cells for the final tile pass.
+__global__ void coarse_scatter_kernel(const int *__restrict__ ecount,
+                                      const int *__restrict__ elist,
+                                      const CoarseCell *__restrict__ ccell,
+                                      CoarseCell *__restrict__ cell) {
+  const int E = *ecount;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x)
+    cell[elist[a]] = ccell[a];
 }
 
 // ------------------------------------------------------------------
@@ -793,11 +802,12 @@ int list_grid(int64_t n) {
 }
 
 struct UpWork {
-  CoarseCell *cell;
+  CoarseCell *ccell, *cell;
   long long *lacc;
   int16_t *lrl;
   uint8_t *emask;
-  int *cnext, *chop, *xmap, *xsteps, *elist, *leaves, *h;
+  int2 *link;
+  int *xmap, *xsteps, *elist, *leaves, *h;
   int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err, [5] maxabs
 };
 
@@ -805,22 +815,25 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
                         UpWork &w) {
   const size_t N = (size_t)g.cells();
   Workspace &ws = workspace();
-  size_t need = 256 + align_up(N * sizeof(CoarseCell)) + 6 * align_up(N * 4) +
+  // Exits are ring pixels: at most 124 per tile.
+  const size_t E = std::min(N, (size_t)g.tiles() * kRing);
+  size_t need = 256 + align_up(N * sizeof(CoarseCell)) + align_up(E * sizeof(CoarseCell)) +
+                align_up(E * 8) + 2 * align_up(E * 4) + 2 * align_up(N * 4) +
                 (want_acc ? align_up(N * 8) : 0) + (want_h ? align_up(N * 4) : 0) +
                 align_up(N * 2) + align_up((size_t)g.tiles() * kRing) + 4096;
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   w.counters = (int *)ws.take(256);
   w.cell = (CoarseCell *)ws.take(N * sizeof(CoarseCell));
+  w.ccell = (CoarseCell *)ws.take(E * sizeof(CoarseCell));
+  w.link = (int2 *)ws.take(E * 8);
   w.lacc = want_acc ? (long long *)ws.take(N * 8) : nullptr;
   w.lrl = (int16_t *)ws.take(N * 2);
   w.emask = (uint8_t *)ws.take((size_t)g.tiles() * kRing);
   w.h = want_h ? (int *)ws.take(N * 4) : nullptr;
-  w.cnext = (int *)ws.take(N * 4);
-  w.chop = (int *)ws.take(N * 4);
   w.xmap = (int *)ws.take(N * 4);
   w.xsteps = (int *)ws.take(N * 4);
-  w.elist = (int *)ws.take(N * 4);
-  w.leaves = (int *)ws.take(N * 4);
+  w.elist = (int *)ws.take(E * 4);
+  w.leaves = (int *)ws.take(E * 4);
   return TT_CUDA_SUCCESS;
 }
 
@@ -842,6 +855,7 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.phase = 1;
   a.want_acc = want_acc;
   a.want_h = want_h;
+  a.ccell = w.ccell;
   a.cell = w.cell;
   a.lacc = w.lacc;
   a.lrl = w.lrl;
@@ -858,12 +872,13 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
-            g.m, order, w.xmap, w.xsteps, w.cnext, w.chop, w.cell);
-  TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.elist, w.counters + 0,
-            w.cell, w.leaves, w.counters + 1);
-  TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1,
-            w.cnext, w.chop, w.cell, w.counters + 2,
-            (int)std::min<int64_t>(g.cells(), INT_MAX));
+            g.m, order, w.xmap, w.xsteps, w.link, w.ccell);
+  TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.counters + 0, w.ccell, w.leaves,
+            w.counters + 1);
+  TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1, w.link,
+            w.ccell, w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
+  TT_LAUNCH(coarse_scatter_kernel, lg, 256, 0, st, w.counters + 0, w.elist, w.ccell,
+            w.cell);
   a.phase = 3;
   TT_LAUNCH(forest_fin_kernel, tgrid, kUpThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
@@ -947,7 +962,7 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
   if (s == TT_CUDA_ERR_CYCLE) return s;
   const int H = h6[3] + 1;
   // hist, off and cursor reuse the coarse arrays (no longer needed).
-  int *hist = w.xmap, *off = w.cnext, *cursor = w.chop;
+  int *hist = w.xmap, *off = w.xsteps, *cursor = reinterpret_cast<int *>(w.cell);
   if ((int64_t)H > g.cells()) return TT_CUDA_ERR_CYCLE;
   TT_CHECK(cudaMemsetAsync(hist, 0, (size_t)H * 4, st));
   TT_CHECK(cudaMemsetAsync(cursor, 0, (size_t)H * 4, st));
