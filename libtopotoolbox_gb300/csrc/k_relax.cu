@@ -30,12 +30,18 @@
 // with a ballot); a warp that relaxes a tile and changes an edge marks the
 // neighbouring tile dirty, so information crosses tile borders as soon as a
 // tile finishes, with no host round trips and no shared queue to contend on.
-// A tile has a single owner, so no two warps relax it at once.  A pending
-// counter (dirty + running tiles) detects termination: it is raised before a
-// flag is set and lowered only after the owner has finished the tile, so it
-// cannot reach zero while work remains.  Every wait is bounded: a warp that
-// idles too long, or a run that exceeds its visit budget, raises an abort
-// flag and all warps return with an error status.
+// A tile has a single owner, so no two warps relax it at once.
+//
+// Termination: only a running warp sets flags.  A warp that finds none of
+// its tiles dirty adds itself to an idle count (after its own flags are
+// visible); a warp that finds a flag again leaves the count, and bumps a
+// wake counter kept in the same 64-bit word, before it takes the flag.  The
+// warp whose arrival makes every warp idle scans all flags and ends the run
+// if none is set and the word is unchanged since its arrival (no warp woke,
+// so none ran and none could set a flag behind the scan); otherwise the
+// owners of the set flags wake up and the last one to go idle scans again.  Every wait is bounded: a warp that idles too
+// long, or a run that exceeds its visit budget, raises an abort flag and all
+// warps return with an error status.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -59,7 +65,8 @@ struct WarpTile {
 // Control block (device memory, zero-initialised).
 struct QueueCtl {
   unsigned long long visits;  // tiles relaxed so far (flushed in batches)
-  int pending;                // dirty + running tiles
+  unsigned long long idle;    // wakes << 32 | warps that found nothing to do
+  int done;                   // set once every warp is idle and no flag is set
   int abort;                  // ABORT_* bits
 };
 
@@ -79,7 +86,7 @@ struct RelaxArgs {
   int visit_flush;  // a warp adds its visits to ctl->visits in batches of this
 };
 
-// Dirty flag values: 1 = a halo pixel changed (re-evaluate the edge ring),
+// Dirty flag bits: 1 = a halo pixel changed (re-evaluate the edge ring),
 // 2 = evaluate every pixel (first visit, or a visit that hit its sweep cap).
 enum : int { DIRTY_EDGE = 1, DIRTY_FULL = 2 };
 
@@ -205,7 +212,17 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
 }
 
 template <int KIND>
-__device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
+
+// The warp that made every warp idle (idle word `seen` after its arrival):
+// finish the run if no flag is set and no warp has woken since.
+__device__ void check_done(const RelaxArgs &a, int lane, int T, unsigned long long seen) {
+  bool any = false;
+  for (int t = lane; t < T; t += 32) any |= *(volatile int *)&a.dirty[t] != 0;
+  if (__any_sync(0xffffffffu, any) || lane != 0) return;
+  fence_acq_rel_gpu();
+  if (*(volatile unsigned long long *)&a.ctl->idle == seen) atomicExch(&a.ctl->done, 1);
+}
 
 template <int KIND>
 __global__ void __launch_bounds__(kWarps * 32)
@@ -216,10 +233,11 @@ relax_persistent_kernel(RelaxArgs a) {
   const int W = gridDim.x * kWarps;
   const int wid = blockIdx.x * kWarps + warp;
   const int T = a.tm * a.tn;
-  long long idle = 0;
+  long long spins = 0;
+  bool idle = false;                 // counted in ctl->idle (warp-uniform)
   unsigned long long unflushed = 0;  // lane 0: visits not yet added to ctl
   for (;;) {
-    if (*(volatile int *)&a.ctl->abort) break;
+    if (*(volatile int *)&a.ctl->abort || *(volatile int *)&a.ctl->done) break;
     if (lane == 0) {
       if (unflushed >= (unsigned long long)a.visit_flush) {
         atomicAdd(&a.ctl->visits, unflushed);
@@ -233,6 +251,16 @@ relax_persistent_kernel(RelaxArgs a) {
       const int mine = base + lane * W;
       int f = (mine < T) ? *(volatile int *)&a.dirty[mine] : 0;
       unsigned mask = __ballot_sync(0xffffffffu, f != 0);
+      if (mask && idle) {  // wake: leave the idle count before taking a flag
+        if (lane == 0) {
+          const unsigned long long before =
+              atomicAdd(&a.ctl->idle, (1ULL << 32) - 1ULL);  // wakes + 1, idle - 1
+          asm volatile("" ::"l"(before));
+          fence_acq_rel_gpu();
+        }
+        idle = false;
+        __syncwarp();
+      }
       while (mask) {
         const int l = __ffs(mask) - 1;
         mask &= mask - 1;
@@ -248,26 +276,33 @@ relax_persistent_kernel(RelaxArgs a) {
         got = __shfl_sync(0xffffffffu, got, 0);
         if (!got) continue;
         did = true;
-        const int redundant = relax_tile<KIND>(a, t, lane, tile, got);
-        // This tile is done; its pushes were counted before their flags were
-        // set, minus those that found the flag already set.
-        if (lane == 0) atomicSub(&a.ctl->pending, redundant + 1);
-        __syncwarp();
+        relax_tile<KIND>(a, t, lane, tile, got);
       }
     }
     if (did) {
-      idle = 0;
+      spins = 0;
+      continue;
+    }
+    if (!idle) {
+      idle = true;
+      fence_acq_rel_gpu();  // every lane: its flags before the idle mark
+      __syncwarp();
+      unsigned long long seen = 0;
+      if (lane == 0) {
+        seen = atomicAdd(&a.ctl->idle, 1ULL) + 1ULL;
+        if ((unsigned)seen == (unsigned)W) fence_acq_rel_gpu();  // all flags visible
+      }
+      seen = __shfl_sync(0xffffffffu, seen, 0);
+      if ((unsigned)seen == (unsigned)W) check_done(a, lane, T, seen);
       continue;
     }
     int stop = 0;
     if (lane == 0) {
-      if (*(volatile int *)&a.ctl->pending <= 0) {
-        stop = 1;
-      } else if (++idle > kSpinLimit) {
+      if (++spins > kSpinLimit) {
         atomicOr(&a.ctl->abort, ABORT_SPIN);
         stop = 1;
       } else {
-        __nanosleep(idle < 64 ? 64 : 512);
+        __nanosleep(spins < 64 ? 64 : 512);
       }
     }
     if (__shfl_sync(0xffffffffu, stop, 0)) break;
@@ -276,9 +311,8 @@ relax_persistent_kernel(RelaxArgs a) {
 }
 
 // Relaxes one tile to its local fixpoint and marks changed neighbours dirty.
-// Returns how many of those marks found the flag already set.
 template <int KIND>
-__device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
+__device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
   const int ti = tile % a.tm, tj = tile / a.tm;
   const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
   int *const sflat = reinterpret_cast<int *>(&t.s[0][0]);  // flats, before the state
@@ -360,7 +394,7 @@ __device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, i
 
   // Marks in the column layout: lane l holds interior column l + 1, bit k =
   // interior row k + 1.  An edge visit starts from the ring next to the halo.
-  uint32_t nd = (mode == DIRTY_FULL || lane == 0 || lane == kTile - 1) ? 0xffffffffu
+  uint32_t nd = ((mode & DIRTY_FULL) || lane == 0 || lane == kTile - 1) ? 0xffffffffu
                                                                        : 0x80000001u;
   uint32_t dm = 0;
 
@@ -412,12 +446,9 @@ __device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, i
   const uint32_t left = __shfl_sync(0xffffffffu, dm, 0);
   const uint32_t right = __shfl_sync(0xffffffffu, dm, kTile - 1);
 
-  // Lanes 0..8 mark one neighbour each.  The pushes are counted in `pending`
-  // (one returning add, completed before any flag is set), then set with
-  // atomicMax; those that found a flag already set are handed back to the
-  // caller, which removes them with this tile's own count.  A tile whose
-  // edges did not change publishes nothing: only its owner reads its
-  // interior again.
+  // Lanes 0..8 mark one neighbour each with an atomic OR, after a release
+  // fence.  A tile whose edges did not change publishes nothing: only its
+  // owner reads its interior again.
   int tgt = -1, val = DIRTY_EDGE;
   switch (lane) {
     case 0: if (top) { tgt = 0; } break;
@@ -437,22 +468,13 @@ __device__ int relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, i
     const int ni = ti + di, nj = tj + dj;
     tgt = (ni < 0 || nj < 0 || ni >= a.tm || nj >= a.tn) ? -1 : nj * a.tm + ni;
   }
-  const unsigned pushes = __ballot_sync(0xffffffffu, tgt >= 0);
-  if (!pushes) return 0;
+  if (!__any_sync(0xffffffffu, tgt >= 0)) return;
   fence_acq_rel_gpu();  // release: this lane's writes before any flag below
   __syncwarp();
-  if (lane == 0) {
-    // the returned value forces the add to complete before the flags
-    const int before = atomicAdd(&a.ctl->pending, __popc(pushes));
-    asm volatile("" ::"r"(before));
-  }
-  __syncwarp();
-  int old = 0;
   if (tgt >= 0) {
     fence_acq_rel_gpu();  // cumulative over the warp's writes seen at the barrier
-    old = atomicMax(&a.dirty[tgt], val);
+    atomicOr(&a.dirty[tgt], val);
   }
-  return __popc(__ballot_sync(0xffffffffu, tgt >= 0 && old != 0));
 }
 
 // f = dem where bc == 1 (and where dem is NaN), +INF elsewhere
@@ -487,10 +509,9 @@ __global__ void negate_kernel(float *__restrict__ out, const float *__restrict__
 }
 
 // Mark every tile dirty (fill starts everywhere).
-__global__ void dirty_all_kernel(int *dirty, QueueCtl *ctl, int n) {
+__global__ void dirty_all_kernel(int *dirty, int n) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
     dirty[t] = DIRTY_FULL;
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = n;
 }
 
 // dist = 1 at presills, +INF at other flats, 0 elsewhere; flag every tile
@@ -516,15 +537,6 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
         }
     }
   }
-}
-
-// pending = number of flagged tiles (the persistent launch starts after).
-__global__ void count_dirty_kernel(const int *__restrict__ dirty, int n, QueueCtl *ctl) {
-  int c = 0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-    c += dirty[t] != 0;
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctl->pending, c);
 }
 
 // A valid back-link for every reached flat: the first flat neighbour u (in
@@ -595,12 +607,11 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
   const int tgrid = (T + 255) / 256;
   if (KIND == FILL) {
-    TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, ctl, T);
+    TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, T);
   } else {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats,
               g.m, g.n, ra);
-    TT_LAUNCH(count_dirty_kernel, std::min(tgrid, sm_count() * 4), 256, 0, st, dirty, T, ctl);
   }
   TT_CHECK(cudaGetLastError());
   static int blocks_per_sm[2] = {0, 0};
@@ -720,7 +731,7 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem, bc,
             g.cells());
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
-  TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, ctl, T);
+  TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, T);
   TT_CHECK(cudaGetLastError());
   RelaxArgs ra{f, dem, nullptr, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
   ra.max_visits = (unsigned long long)T *
