@@ -132,6 +132,7 @@ struct CclTile {
 __global__ void __launch_bounds__(kCclWarps * 32)
 ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ larg,
                 int *__restrict__ maxkey, int *__restrict__ argmax,
+                int *__restrict__ roots, int *__restrict__ nroots,
                 const int32_t *__restrict__ flats, const float *__restrict__ orig,
                 const float *__restrict__ filled, int64_t m, int64_t n, int tm, int tn) {
   __shared__ CclTile tiles[kCclWarps];
@@ -227,10 +228,20 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
     __syncwarp();
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
-      if (i >= m || j >= n) continue;
+      const bool in = i < m && j < n;
       const int64_t gp = j * m + i;
       const int loc = jj * kTile + lane;
       const int r = t.root[loc];
+      const bool is_root = in && r == loc;
+      // local roots go to a compact list (one reservation per column)
+      const unsigned rb = __ballot_sync(0xffffffffu, is_root);
+      if (rb) {
+        int base = 0;
+        if (lane == __ffs(rb) - 1) base = atomicAdd(nroots, __popc(rb));
+        base = __shfl_sync(0xffffffffu, base, __ffs(rb) - 1);
+        if (is_root) roots[base + __popc(rb & ((1u << lane) - 1u))] = (int)gp;
+      }
+      if (!in) continue;
       int v = -1;
       if (r >= 0) {
         v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
@@ -282,27 +293,33 @@ __global__ void ccl_border_kernel(int *__restrict__ L,
   }
 }
 
-// Local roots fold their maxima into their global root.
+// Local roots (a compact list) fold their maxima into their global root.
 __global__ void ccl_max_kernel(int *__restrict__ L, const int *__restrict__ lmax,
-                               const int *__restrict__ larg, int *__restrict__ maxkey,
-                               const int32_t *__restrict__ flats, int64_t N) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    if (!(flats[p] & 1) || larg[p] < 0) continue;
-    const int R = uf_find(L, (int)p);
+                               const int *__restrict__ roots, const int *__restrict__ nroots,
+                               int *__restrict__ rootR, int *__restrict__ maxkey) {
+  const int K = *nroots;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+    const int p = roots[k];
+    const int R = uf_find(L, p);
+    rootR[k] = R;
     if (lmax[p] != INT_MIN) atomicMax(&maxkey[R], lmax[p]);
   }
 }
 
+// The argmax of each component over its local roots; afterwards every local
+// root points straight at its global root, so any flat pixel p reaches its
+// root in two steps: L[L[p]] (every label above a pixel is a local root).
 __global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ lmax,
                                   const int *__restrict__ larg,
-                                  const int *__restrict__ maxkey, int *__restrict__ argmax,
-                                  const int32_t *__restrict__ flats, int64_t N) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    if (!(flats[p] & 1) || larg[p] < 0) continue;
-    const int R = uf_find(L, (int)p);
+                                  const int *__restrict__ roots, const int *__restrict__ nroots,
+                                  const int *__restrict__ rootR,
+                                  const int *__restrict__ maxkey, int *__restrict__ argmax) {
+  const int K = *nroots;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+    const int p = roots[k];
+    const int R = rootR[k];
     if (lmax[p] != INT_MIN && lmax[p] == maxkey[R]) atomicMin(&argmax[R], larg[p]);
+    L[p] = R;
   }
 }
 
@@ -318,7 +335,7 @@ __global__ void costs_kernel(float *__restrict__ costs,
     float c = 0.0f;
     ptrdiff_t lab = 0;
     if (flats[p] & 1) {
-      const int R = uf_find(L, (int)p);
+      const int R = L[L[p]];
       const float maxd = key_to_float(maxkey[R]);
       const float depth = __fsub_rn(filled[p], orig[p]);
       const float diff = __fsub_rn(maxd, depth);
@@ -345,7 +362,10 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
                          cudaStream_t st) {
   const int64_t N = g.cells();
   Workspace &ws = workspace();
-  if (!ws.reserve(5 * align_up((size_t)N * 4))) return TT_CUDA_ERR_ALLOC;
+  if (!ws.reserve(7 * align_up((size_t)N * 4) + 256)) return TT_CUDA_ERR_ALLOC;
+  int *nroots = (int *)ws.take(256);
+  int *roots = (int *)ws.take((size_t)N * 4);
+  int *rootR = (int *)ws.take((size_t)N * 4);
   int *L = (int *)ws.take((size_t)N * 4);
   int *lmax = (int *)ws.take((size_t)N * 4);
   int *larg = (int *)ws.take((size_t)N * 4);
@@ -355,12 +375,14 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   const int T = g.tiles();
   const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
                                            (int64_t)sm_count() * 16);
+  TT_CHECK(cudaMemsetAsync(nroots, 0, sizeof(int), st));
   TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, maxkey, argmax,
-            flats, orig, filled, g.m, g.n, g.tm, g.tn);
+            roots, nroots, flats, orig, filled, g.m, g.n, g.tm, g.tn);
   TT_LAUNCH(ccl_border_kernel, ew_grid((int64_t)T * 96), 256, 0, st, L, flats, g.m,
             g.n, g.tm, g.tn);
-  TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, larg, maxkey, flats, N);
-  TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, maxkey, argmax, flats, N);
+  TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
+  TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
+            maxkey, argmax);
   TT_LAUNCH(costs_kernel, grid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
             flats, orig, filled, N);
   TT_CHECK(cudaGetLastError());
