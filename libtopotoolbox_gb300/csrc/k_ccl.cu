@@ -144,23 +144,34 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
     const int64_t i = i0 + lane;  // lane = row for the per-pixel phases
     uint32_t my_mask = 0;
-#pragma unroll 8
-    for (int jj = 0; jj < kTile; jj++) {
-      const int64_t j = j0 + jj;
-      bool f = false;
-      int k = INT_MIN;
-      if (i < m && j < n) {
-        const int64_t p = j * m + i;
-        f = flats[p] & 1;
+    // Eight columns at a time: every load of the batch is issued (from a
+    // clamped, always valid address) before any result is used.
+    const int64_t icl = i < m ? i : m - 1;
+    for (int j8 = 0; j8 < kTile; j8 += 8) {
+      int fv[8];
+      float fl[8], og[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int64_t j = j0 + j8 + u;
+        const int64_t p = (j < n ? j : n - 1) * m + icl;
+        fv[u] = flats[p];
+        fl[u] = filled[p];
+        og[u] = orig[p];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int jj = j8 + u;
+        const bool f = i < m && j0 + jj < n && (fv[u] & 1);
+        int k = INT_MIN;
         if (f) {
-          const float d = __fsub_rn(filled[p], orig[p]);
+          const float d = __fsub_rn(fl[u], og[u]);
           if (!isnan(d)) k = ordered_key(d);
         }
+        t.key[jj * kTile + lane] = k;
+        t.root[jj * kTile + lane] = -1;
+        const uint32_t b = __ballot_sync(0xffffffffu, f);
+        if (lane == jj) my_mask = b;
       }
-      t.key[jj * kTile + lane] = k;
-      t.root[jj * kTile + lane] = -1;
-      const uint32_t b = __ballot_sync(0xffffffffu, f);
-      if (lane == jj) my_mask = b;
     }
     // lane = column c from here to the unions
     const uint32_t M = my_mask, S = M & ~(M << 1);
@@ -194,9 +205,29 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       for (uint32_t b = rm; b; b &= b - 1) t.root[lane * kTile + __ffs(b) - 1] = (int16_t)r;
     }
     __syncwarp();
-    for (uint32_t s = S; s; s &= s - 1) {
-      const int loc = lane * kTile + __ffs(s) - 1;
-      if (t.root[loc] == loc) t.lab[loc] = INT_MIN;
+    {  // local roots: reset their reduction slot and list them (one
+       // reservation per tile, lane = column)
+      uint32_t rs = 0;
+      for (uint32_t s = S; s; s &= s - 1) {
+        const int loc = lane * kTile + __ffs(s) - 1;
+        if (t.root[loc] == loc) {
+          t.lab[loc] = INT_MIN;
+          rs |= s & (~s + 1u);
+        }
+      }
+      const int mine = __popc(rs);
+      int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      int base = 0;
+      if (lane == 0 && total) base = atomicAdd(nroots, total);
+      base = __shfl_sync(0xffffffffu, base, 0) + incl - mine;
+      for (uint32_t b = rs; b; b &= b - 1)
+        roots[base++] = (int)((j0 + lane) * m + (i0 + __ffs(b) - 1));
     }
     __syncwarp();
     for (int jj = 0; jj < kTile; jj++) {
@@ -232,15 +263,6 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       const int64_t gp = j * m + i;
       const int loc = jj * kTile + lane;
       const int r = t.root[loc];
-      const bool is_root = in && r == loc;
-      // local roots go to a compact list (one reservation per column)
-      const unsigned rb = __ballot_sync(0xffffffffu, is_root);
-      if (rb) {
-        int base = 0;
-        if (lane == __ffs(rb) - 1) base = atomicAdd(nroots, __popc(rb));
-        base = __shfl_sync(0xffffffffu, base, __ffs(rb) - 1);
-        if (is_root) roots[base + __popc(rb & ((1u << lane) - 1u))] = (int)gp;
-      }
       if (!in) continue;
       int v = -1;
       if (r >= 0) {

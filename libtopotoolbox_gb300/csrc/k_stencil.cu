@@ -17,102 +17,104 @@ constexpr int kBlockY = 8;   // along j
 // ------------------------------------------------------------------
 // identifyflats (src/identifyflats.c:33-121)
 //
-// One block handles a 32 x 32 tile.  Shared memory holds the DEM of the tile
-// with a two-pixel halo; flat bits are computed for the tile plus a one-pixel
-// ring, after which sill and presill bits are gathered per pixel:
-//   sill(s)    = !flat(s) && exists flat neighbour f with z_f == z_s
-//   presill(f) =  flat(f) && exists non-flat neighbour s with z_s == z_f
-// which is the scatter at src/identifyflats.c:83-119 restated as a gather.
+// flat(p)    = interior pixel, not NaN, and no neighbour lower, a NaN
+//              neighbour counting as -INF (src/identifyflats.c:64)
+// sill(s)    = !flat(s) && exists flat neighbour f with z_f == z_s
+// presill(f) =  flat(f) && exists non-flat neighbour s with z_s == z_f
+// (the scatter at src/identifyflats.c:83-119 restated as a gather).
+//
+// Streamed by warps: a warp owns a strip of 28 output rows (lane l carries
+// row strip*28 - 2 + l; lanes 0..1 and 30..31 are halo) and walks 128
+// columns.  Each column is loaded once, coalesced; the rows above and below
+// come from the neighbouring lanes by shuffles; a window of four columns
+// lives in registers, and the flat bits of a column are one ballot mask.
+// Flat bits of column j - 1 are known once column j is loaded, and the
+// sill/presill gather of column j - 2 then needs only registers and masks.
+// Loads are issued eight columns ahead.
 // ------------------------------------------------------------------
-constexpr int kFH = kTile + 4;  // 36: tile + 2-pixel halo
+constexpr int kFlatRows = 28;   // output rows per warp
+constexpr int kFlatSeg = 128;   // output columns per warp
+constexpr int kFlatAhead = 8;   // columns loaded per batch
 
-__global__ void __launch_bounds__(kBlockX * kBlockY)
+__device__ __forceinline__ float nan_to_neg_inf(float v) { return v != v ? -INFINITY : v; }
+
+__global__ void __launch_bounds__(128)
 identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
-                     int64_t m, int64_t n, unsigned long long *count) {
-  __shared__ float z[kFH][kFH + 1];           // [c][r], 2-pixel halo
-  __shared__ uint8_t flat[kTile + 2][kTile + 3];  // [c][r], 1-pixel ring
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t i0 = (int64_t)blockIdx.x * kTile;
-  const int64_t j0 = (int64_t)blockIdx.y * kTile;
-
-  {  // stage the DEM: all loads in flight before the first shared store
-    constexpr int kC = (kFH + kBlockY - 1) / kBlockY;
-    float v[kC][2];
+                     int64_t m, int64_t n, int nstrips, int nsegs,
+                     unsigned long long *count) {
+  const int lane = threadIdx.x & 31;
+  const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (wid >= nstrips * nsegs) return;  // whole warps only
+  const int strip = wid % nstrips, seg = wid / nstrips;
+  const int64_t i = (int64_t)strip * kFlatRows - 2 + lane;
+  const bool row_in = i >= 0 && i < m;
+  const bool row_int = i >= 1 && i < m - 1;  // interior rows may be flat
+  const bool row_out = lane >= 2 && lane < 2 + kFlatRows && row_in;
+  const int64_t ic = row_in ? i : (i < 0 ? 0 : m - 1);  // clamped for loads
+  const int64_t js = (int64_t)seg * kFlatSeg;
+  const int64_t je = (js + kFlatSeg < n ? js + kFlatSeg : n) - 1;  // last output column
+  // window of columns jl-3..jl: z, the row above (u) and below (d)
+  float Z[4], U[4], D[4];
 #pragma unroll
-    for (int k = 0; k < kC; k++)
+  for (int w = 0; w < 4; w++) Z[w] = U[w] = D[w] = NAN;
+  unsigned F0 = 0, F1 = 0, F2 = 0;  // flat masks of columns jl-3, jl-2, jl-1
+  unsigned cnt = 0;
+  for (int64_t jb = js - 2; jb <= je + 2; jb += kFlatAhead) {
+    float buf[kFlatAhead];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
-        const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
-        v[k][h] = (c < kFH && r < kFH && i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i] : NAN;
+    for (int u = 0; u < kFlatAhead; u++) {
+      const int64_t j = jb + u;
+      const int64_t jc = j < 0 ? 0 : (j >= n ? n - 1 : j);
+      buf[u] = dem[jc * m + ic];
+    }
+#pragma unroll
+    for (int u = 0; u < kFlatAhead; u++) {
+      const int64_t jl = jb + u;
+      if (jl > je + 2) break;
+      const float zn = (row_in && jl >= 0 && jl < n) ? buf[u] : NAN;
+      const float un = __shfl_up_sync(0xffffffffu, zn, 1);
+      const float dn = __shfl_down_sync(0xffffffffu, zn, 1);
+#pragma unroll
+      for (int w = 0; w < 3; w++) {
+        Z[w] = Z[w + 1];
+        U[w] = U[w + 1];
+        D[w] = D[w + 1];
       }
-#pragma unroll
-    for (int k = 0; k < kC; k++)
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
-        if (c < kFH && r < kFH) z[c][r] = v[k][h];
+      Z[3] = zn;
+      U[3] = un;
+      D[3] = dn;
+      // flat bit of column jl - 1 (window column 2)
+      const float zc = Z[2];
+      const float lo = fminf(
+          fminf(fminf(nan_to_neg_inf(U[1]), nan_to_neg_inf(Z[1])),
+                fminf(nan_to_neg_inf(D[1]), nan_to_neg_inf(U[2]))),
+          fminf(fminf(nan_to_neg_inf(D[2]), nan_to_neg_inf(U[3])),
+                fminf(nan_to_neg_inf(Z[3]), nan_to_neg_inf(D[3]))));
+      const bool col_int = jl - 1 >= 1 && jl - 1 < n - 1;
+      const bool f = row_int && col_int && zc == zc && !(lo < zc);
+      F0 = F1;
+      F1 = F2;
+      F2 = __ballot_sync(0xffffffffu, f);
+      // sill / presill of column jl - 2 (window column 1)
+      const int64_t jo = jl - 2;
+      if (jo >= js && jo <= je) {
+        const float z1 = Z[1];
+        const unsigned fc = (F1 >> lane) & 1u;
+        const unsigned lm = (lane + 31) & 31, lp = (lane + 1) & 31;  // rows above, below
+        const bool hit =
+            ((((F0 >> lm) & 1u) != fc) & (U[0] == z1)) | ((((F0 >> lane) & 1u) != fc) & (Z[0] == z1)) |
+            ((((F0 >> lp) & 1u) != fc) & (D[0] == z1)) | ((((F1 >> lm) & 1u) != fc) & (U[1] == z1)) |
+            ((((F1 >> lp) & 1u) != fc) & (D[1] == z1)) | ((((F2 >> lm) & 1u) != fc) & (U[2] == z1)) |
+            ((((F2 >> lane) & 1u) != fc) & (Z[2] == z1)) | ((((F2 >> lp) & 1u) != fc) & (D[2] == z1));
+        if (row_out) {
+          out[jo * m + i] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
+          cnt += fc;
+        }
       }
-  }
-  __syncthreads();
-
-  // Flat bits for the tile and its one-pixel ring.
-  for (int c = ty; c < kTile + 2; c += kBlockY) {
-    int64_t j = j0 - 1 + c;
-    for (int r = tx; r < kTile + 2; r += kBlockX) {
-      int64_t i = i0 - 1 + r;
-      uint8_t f = 0;
-      if (i >= 1 && i < m - 1 && j >= 1 && j < n - 1) {
-        // flat: no neighbour lower, NaN neighbours counting as -INF
-        const float zc = z[c + 1][r + 1];
-        bool lower = false;
-#pragma unroll
-        for (int dc = -1; dc <= 1; dc++)
-#pragma unroll
-          for (int dr = -1; dr <= 1; dr++) {
-            if (dc == 0 && dr == 0) continue;
-            const float zn = z[c + 1 + dc][r + 1 + dr];
-            // a NaN neighbour counts as -INF (src/identifyflats.c:64)
-            lower |= (zn < zc) | ((zn != zn) & (zc != -INFINITY));
-          }
-        f = (!lower && zc == zc) ? 1 : 0;
-      }
-      flat[c][r] = f;
     }
   }
-  __syncthreads();
-
-  unsigned local = 0;
-  // Pixels outside the grid hold NaN, which never compares equal, so the
-  // gather needs no bounds checks.
-  for (int c = ty; c < kTile; c += kBlockY) {
-    const int64_t j = j0 + c;
-    const int r = tx;
-    const int64_t i = i0 + r;
-    if (j >= n || i >= m) continue;
-    const float zc = z[c + 2][r + 2];
-    const int fc = flat[c + 1][r + 1];
-    bool hit = false;
-#pragma unroll
-    for (int dc = -1; dc <= 1; dc++)
-#pragma unroll
-      for (int dr = -1; dr <= 1; dr++) {
-        if (dc == 0 && dr == 0) continue;
-        hit |= (flat[c + 1 + dc][r + 1 + dr] != fc) & (z[c + 2 + dc][r + 2 + dr] == zc);
-      }
-    out[j * m + i] = fc | (hit ? (fc ? 4 : 2) : 0);
-    local += fc;
-  }
-  // Block reduction of the flat count.
-  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-  __shared__ unsigned warp_sum[kBlockY];
-  if (tx == 0) warp_sum[ty] = local;
-  __syncthreads();
-  if (ty == 0 && tx == 0) {
-    unsigned s = 0;
-    for (int w = 0; w < kBlockY; w++) s += warp_sum[w];
-    if (s) atomicAdd(count, (unsigned long long)s);
-  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if (lane == 0 && cnt) atomicAdd(count, (unsigned long long)cnt);
 }
 
 // ------------------------------------------------------------------
@@ -509,8 +511,11 @@ tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
     cnt = (unsigned long long *)ws.take(8);
   }
   TT_CHECK(cudaMemsetAsync(cnt, 0, 8, st));
-  TT_LAUNCH(identifyflats_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            flags, dem, g.m, g.n, cnt);
+  const int nstrips = (int)((g.m + kFlatRows - 1) / kFlatRows);
+  const int nsegs = (int)((g.n + kFlatSeg - 1) / kFlatSeg);
+  const int64_t warps = (int64_t)nstrips * nsegs;
+  TT_LAUNCH(identifyflats_kernel, (int)((warps + 3) / 4), 128, 0, st, flags, dem, g.m, g.n,
+            nstrips, nsegs, cnt);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
