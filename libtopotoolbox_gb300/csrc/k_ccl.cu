@@ -405,8 +405,10 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
   TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
             maxkey, argmax);
-  TT_LAUNCH(costs_kernel, grid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
-            flats, orig, filled, N);
+  // One pixel per thread: each pixel's root lookup is a chain of dependent
+  // loads, best overlapped across many threads.
+  TT_LAUNCH(costs_kernel, (int)std::min<int64_t>((N + 255) / 256, INT_MAX), 256, 0, st,
+            costs, conncomps, L, maxkey, argmax, flats, orig, filled, N);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

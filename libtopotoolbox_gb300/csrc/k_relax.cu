@@ -99,7 +99,10 @@ __device__ __forceinline__ void fence_acq_rel_gpu() {
 // 4-byte asynchronous copy global -> shared, cached in L1 (read-only inputs).
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+  // No memory clobber: the copies may interleave with the other staging
+  // loads; cp_async_wait_all() orders them before any use, and the warp
+  // barriers before staging order them after the previous visit's reads.
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem));
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
@@ -531,10 +534,7 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
       int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
       int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
       for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) {
-          int *fl = &qa.dirty[tj * qa.tm + ti];
-          if (*fl == 0) *fl = DIRTY_FULL;
-        }
+        for (int ti = ti0; ti <= ti1; ti++) qa.dirty[tj * qa.tm + ti] = DIRTY_FULL;
     }
   }
 }
