@@ -337,6 +337,33 @@ hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
       }
   }
   __syncthreads();
+  // Tiles at least two pixels away from every grid edge use central
+  // differences only: no per-pixel border tests, and the float gradients
+  // dx, dy are formed only where the float-float path is not finite.
+  const bool deep = MODE == 0 && i0 >= 2 && i0 + kTile + 2 <= m && j0 >= 2 && j0 + kTile + 2 <= n;
+  if (deep) {
+    for (int c = ty; c < kTile; c += kBlockY) {
+      const int r = tx + 2, cc = c + 2;
+      const float zc0 = z[cc][r];
+      const F2 ex = f2_mul(two_sum(z[cc][r + 1], -z[cc][r - 1]), F2{s2.rh, s2.rl});
+      const F2 ey = f2_mul(two_sum(z[cc + 1][r], -z[cc - 1][r]), F2{s2.rh, s2.rl});
+      float h = NAN;
+      if (zc0 == zc0 && isfinite(ex.hi) && isfinite(ey.hi)) {
+        const F2 num = f2_add(f2_add(f2_mul(ex, F2{-s2.sxh, -s2.sxl}),
+                                     f2_mul(ey, F2{-s2.syh, -s2.syl})),
+                              F2{s2.szh, s2.szl});
+        const float q = __fmaf_rn(ex.hi, ex.hi, __fmaf_rn(ey.hi, ey.hi, 1.0f));
+        h = __fdiv_rn(__fadd_rn(num.hi, num.lo), __fsqrt_rn(q));
+      }
+      if (!isfinite(h)) {  // NaN / INF exactly as the reference
+        const float dx = isnan(zc0) ? NAN : __fdiv_rn(__fsub_rn(z[cc][r + 1], z[cc][r - 1]), twoh);
+        const float dy = isnan(zc0) ? NAN : __fdiv_rn(__fsub_rn(z[cc + 1][r], z[cc - 1][r]), twoh);
+        h = shade(dx, dy, sx, sy, sz);
+      }
+      out0[(j0 + c) * m + i0 + tx] = h;
+    }
+    return;
+  }
   for (int c = ty; c < kTile; c += kBlockY) {
     int64_t j = j0 + c;
     int64_t i = i0 + tx;
@@ -436,6 +463,39 @@ hillshade_bwd_kernel(float *__restrict__ gdem, const float *__restrict__ dem,
     }
   }
   __syncthreads();
+  // Tiles whose centres and samples all lie at least two pixels inside the
+  // grid take a fast path: central differences only, multiplication by
+  // 1 / (2h) and rsqrtf (each within an ulp or two of the exact path, far
+  // inside the adjoint's 1e-5 tolerance), no per-pixel border tests.
+  const bool deep = i0 >= 4 && i0 + kTile + 4 <= m && j0 >= 4 && j0 + kTile + 4 <= n;
+  if (deep) {
+    const float r2h = 1.0f / twoh;
+    for (int e = tid; e < kHG * kHG; e += kThreads) {
+      const int c = e / kHG, r = e % kHG;
+      const int zc = c + 2, zr = r + 2;
+      const float z0 = z[zc][zr];
+      const float dx = (z[zc][zr + 1] - z[zc][zr - 1]) * r2h;
+      const float dy = (z[zc + 1][zr] - z[zc - 1][zr]) * r2h;
+      const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, 1.0f)));
+      const float num = fmaf(-dx, sx, fmaf(-dy, sy, sz));
+      float ax = 0.f, ay = 0.f;
+      if (z0 == z0 && !isnan(num * inv)) {
+        const float tt = num * (inv * inv * inv);
+        const float g = gx[c][r];
+        ax = g * (-sx * inv - dx * tt);
+        ay = g * (-sy * inv - dy * tt);
+      }
+      gx[c][r] = ax;  // this thread alone read gx[c][r]
+      gy[c][r] = ay;
+    }
+    __syncthreads();
+    for (int cy = threadIdx.y; cy < kTile; cy += kBlockY) {
+      const int r = threadIdx.x + 2, cc = cy + 2;
+      const float acc = ((gx[cc][r - 1] - gx[cc][r + 1]) + gy[cc - 1][r]) - gy[cc + 1][r];
+      gdem[(j0 + cy) * m + i0 + threadIdx.x] = acc * r2h;
+    }
+    return;
+  }
   // dH/d(dx) * g and dH/d(dy) * g at the 36 x 36 centres.
   for (int e = tid; e < kHG * kHG; e += kThreads) {
     const int c = e / kHG, r = e % kHG;
