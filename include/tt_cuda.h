@@ -149,6 +149,44 @@ TT_CUDA_API void tt_cuda_hillshade_fused(float *output, float *dem,
                                          float cellsize, ptrdiff_t dims[2]);
 
 /* ------------------------------------------------------------------ */
+/* Edge-list forms (the callers of the path's outputs)                  */
+/* ------------------------------------------------------------------ */
+
+/** include/topotoolbox.h:912 flow_routing_d8_edgelist
+ *  (src/flow_routing.c:258-312).  One edge (u, receiver(u)) per pixel with a
+ *  direction, in `node` order, bit-identical to the reference for the same
+ *  `node` and `direction`.  `source` and `target` need room for every pixel;
+ *  only the first (returned) count entries are written. */
+TT_CUDA_API ptrdiff_t tt_cuda_flow_routing_d8_edgelist(ptrdiff_t *source,
+                                                       ptrdiff_t *target,
+                                                       ptrdiff_t *node,
+                                                       uint8_t *direction,
+                                                       ptrdiff_t dims[2],
+                                                       unsigned int order);
+/** include/topotoolbox.h:1019 flow_accumulation_edgelist
+ *  (src/flow_accumulation.c:10-30) for the edge list of a D8 forest (each
+ *  pixel the source of at most one edge, to one of its eight neighbours in
+ *  the column-major interpretation of `dims`) with unit fractions: the
+ *  exact forest sum of tt_cuda_flow_accumulation.  Other edge lists are
+ *  refused with TT_CUDA_ERR_INVALID_ARGUMENT. */
+TT_CUDA_API void tt_cuda_flow_accumulation_edgelist(float *acc, ptrdiff_t *source,
+                                                    ptrdiff_t *target,
+                                                    float *fraction, float *weights,
+                                                    ptrdiff_t edge_count,
+                                                    ptrdiff_t dims[2]);
+/** include/topotoolbox.h:2304 drainagebasins (src/drainagebasins.c:6-27).
+ *  For a topologically ordered edge list (as flow_routing_d8_edgelist
+ *  produces) the labels equal the reference's on the same list. */
+TT_CUDA_API void tt_cuda_drainagebasins(ptrdiff_t *basins, ptrdiff_t *source,
+                                        ptrdiff_t *target, ptrdiff_t edge_count,
+                                        ptrdiff_t dims[2]);
+/** include/topotoolbox.h:1853 edgelist_degree (src/streamquad.c:209-224).
+ *  uint8 degrees, wrapping modulo 256 as the reference's counters do. */
+TT_CUDA_API void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
+                                         ptrdiff_t *source, ptrdiff_t *target,
+                                         ptrdiff_t node_count, ptrdiff_t edge_count);
+
+/* ------------------------------------------------------------------ */
 /* Adjoints (no counterpart in the reference)                           */
 /* ------------------------------------------------------------------ */
 
@@ -232,6 +270,23 @@ TT_CUDA_API tt_cuda_status tt_cuda_hillshade_fused_dev(
 TT_CUDA_API tt_cuda_status tt_cuda_hillshade_backward_dev(
     float *grad_dem, const float *dem, const float *grad_output, float azimuth,
     float altitude, float cellsize, const ptrdiff_t dims[2], void *stream);
+/** Device-pointer forms of the edge-list functions above; the edge count of
+ *  tt_cuda_flow_routing_d8_edgelist_dev is written to *edge_count (host). */
+TT_CUDA_API tt_cuda_status tt_cuda_flow_routing_d8_edgelist_dev(
+    ptrdiff_t *source, ptrdiff_t *target, ptrdiff_t *edge_count,
+    const ptrdiff_t *node, const uint8_t *direction, const ptrdiff_t dims[2],
+    unsigned int order, void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_flow_accumulation_edgelist_dev(
+    float *acc, const ptrdiff_t *source, const ptrdiff_t *target,
+    const float *fraction, const float *weights, ptrdiff_t edge_count,
+    const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_drainagebasins_dev(
+    ptrdiff_t *basins, const ptrdiff_t *source, const ptrdiff_t *target,
+    ptrdiff_t edge_count, const ptrdiff_t dims[2], void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_edgelist_degree_dev(
+    uint8_t *indegree, uint8_t *outdegree, const ptrdiff_t *source,
+    const ptrdiff_t *target, ptrdiff_t node_count, ptrdiff_t edge_count,
+    void *stream);
 /** fillsinks on device pointers without allocating anything.  No
  *  counterpart in the reference.  For callers that cannot call cudaMalloc
  *  while they run -- a framework whose own memory pool already owns the

@@ -43,6 +43,10 @@ SIGNATURES = {
     "tt_cuda_flow_accumulation_backward": (None, [P, P, P, P, PD]),
     "tt_cuda_hillshade_backward": (None, [P, P, P, F, F, F, PD]),
     "tt_cuda_d8_pipeline": (None, [P, P, P, P, P, P, P, P, P, PD]),
+    "tt_cuda_flow_routing_d8_edgelist": (I64, [P, P, P, P, PD, U]),
+    "tt_cuda_flow_accumulation_edgelist": (None, [P, P, P, P, P, I64, PD]),
+    "tt_cuda_drainagebasins": (None, [P, P, P, I64, PD]),
+    "tt_cuda_edgelist_degree": (None, [P, P, P, P, I64, I64]),
     # device-pointer forms
     "tt_cuda_fillsinks_dev": (ST, [P, P, P, PD, P]),
     "tt_cuda_fillsinks_noalloc_dev": (ST, [P, P, P, PD, P]),
@@ -57,6 +61,10 @@ SIGNATURES = {
     "tt_cuda_hillshade_fused_dev": (ST, [P, P, F, F, F, PD, P]),
     "tt_cuda_hillshade_backward_dev": (ST, [P, P, P, F, F, F, PD, P]),
     "tt_cuda_d8_pipeline_dev": (ST, [P, P, P, P, P, P, P, P, P, P, F, F, F, PD, P]),
+    "tt_cuda_flow_routing_d8_edgelist_dev": (ST, [P, P, C.POINTER(I64), P, P, PD, U, P]),
+    "tt_cuda_flow_accumulation_edgelist_dev": (ST, [P, P, P, P, P, I64, PD, P]),
+    "tt_cuda_drainagebasins_dev": (ST, [P, P, P, I64, PD, P]),
+    "tt_cuda_edgelist_degree_dev": (ST, [P, P, P, P, I64, I64, P]),
     # batched form
     "tt_cuda_batch_create": (ST, [C.c_int, PD, I64, C.POINTER(P)]),
     "tt_cuda_batch_info": (ST, [P, C.POINTER(I64)]),

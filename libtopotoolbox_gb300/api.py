@@ -209,6 +209,58 @@ def hillshade_backward(dem, grad_output, azimuth, altitude, cellsize):
     return out
 
 
+def flow_routing_d8_edgelist(node, direction, order=0):
+    """(source, target) (include/topotoolbox.h:912, src/flow_routing.c:258-312):
+    one edge per pixel with a direction, in `node` order."""
+    node = np.asfortranarray(node, dtype=np.int64)
+    direction = _u8(direction)
+    src = np.empty(direction.size, dtype=np.int64)
+    tgt = np.empty(direction.size, dtype=np.int64)
+    dp, keep = N.dims_arg(_dims(direction))
+    e = N.lib().tt_cuda_flow_routing_d8_edgelist(_ptr(src), _ptr(tgt), _ptr(node),
+                                                 _ptr(direction), dp, int(order))
+    _after("flow_routing_d8_edgelist")
+    return src[:e].copy(), tgt[:e].copy()
+
+
+def flow_accumulation_edgelist(source, target, fraction, shape, weights=None):
+    """acc (include/topotoolbox.h:1019, src/flow_accumulation.c:10-30) for the
+    edge list of a D8 forest with unit fractions."""
+    src = np.ascontiguousarray(source, dtype=np.int64)
+    tgt = np.ascontiguousarray(target, dtype=np.int64)
+    fr = np.ascontiguousarray(fraction, dtype=np.float32)
+    w = _f32(weights) if weights is not None else None
+    acc = np.empty(shape, dtype=np.float32, order="F")
+    dp, keep = N.dims_arg(tuple(shape))
+    N.lib().tt_cuda_flow_accumulation_edgelist(_ptr(acc), _ptr(src), _ptr(tgt), _ptr(fr),
+                                               _ptr(w), len(src), dp)
+    _after("flow_accumulation_edgelist")
+    return acc
+
+
+def drainagebasins(source, target, shape):
+    """basins (include/topotoolbox.h:2304, src/drainagebasins.c:6-27)."""
+    src = np.ascontiguousarray(source, dtype=np.int64)
+    tgt = np.ascontiguousarray(target, dtype=np.int64)
+    out = np.empty(shape, dtype=np.int64, order="F")
+    dp, keep = N.dims_arg(tuple(shape))
+    N.lib().tt_cuda_drainagebasins(_ptr(out), _ptr(src), _ptr(tgt), len(src), dp)
+    _after("drainagebasins")
+    return out
+
+
+def edgelist_degree(source, target, node_count):
+    """(indegree, outdegree) (include/topotoolbox.h:1853, src/streamquad.c:209-224)."""
+    src = np.ascontiguousarray(source, dtype=np.int64)
+    tgt = np.ascontiguousarray(target, dtype=np.int64)
+    indeg = np.empty(node_count, dtype=np.uint8)
+    outdeg = np.empty(node_count, dtype=np.uint8)
+    N.lib().tt_cuda_edgelist_degree(_ptr(indeg), _ptr(outdeg), _ptr(src), _ptr(tgt),
+                                    int(node_count), len(src))
+    _after("edgelist_degree")
+    return indeg, outdeg
+
+
 def d8_pipeline(dem, bc, weights=None):
     """The reference call sequence fill -> flats -> costs -> gwdt -> carve ->
     accumulation in one call (host buffers).  Returns a dict."""
@@ -322,6 +374,45 @@ class dev:  # namespace
         N.check(N.lib().tt_cuda_flow_accumulation_dev(dev._p(out), dev._p(direction),
                                                       dev._p(weights), dp, dev._stream()),
                 "flow_accumulation_dev")
+        return out
+
+    @staticmethod
+    def flow_routing_d8_edgelist(node, direction, order=0):
+        """Returns (source, target) CUDA tensors trimmed to the edge count."""
+        import torch
+
+        n = direction.numel()
+        src = torch.empty(n, dtype=torch.int64, device=direction.device)
+        tgt = torch.empty(n, dtype=torch.int64, device=direction.device)
+        cnt = N.C.c_int64(0)
+        dp, keep = N.dims_arg(dev._dims(direction))
+        N.check(N.lib().tt_cuda_flow_routing_d8_edgelist_dev(
+            dev._p(src), dev._p(tgt), N.C.byref(cnt), dev._p(node), dev._p(direction), dp,
+            int(order), dev._stream()), "flow_routing_d8_edgelist_dev")
+        return src[:cnt.value], tgt[:cnt.value]
+
+    @staticmethod
+    def flow_accumulation_edgelist(source, target, fraction, like, weights=None, out=None):
+        import torch
+
+        out = torch.empty(like.shape, dtype=torch.float32, device=like.device) \
+            if out is None else out
+        dp, keep = N.dims_arg(dev._dims(like))
+        N.check(N.lib().tt_cuda_flow_accumulation_edgelist_dev(
+            dev._p(out), dev._p(source), dev._p(target), dev._p(fraction), dev._p(weights),
+            int(source.numel()), dp, dev._stream()), "flow_accumulation_edgelist_dev")
+        return out
+
+    @staticmethod
+    def drainagebasins(source, target, like, out=None):
+        import torch
+
+        out = torch.empty(like.shape, dtype=torch.int64, device=like.device) \
+            if out is None else out
+        dp, keep = N.dims_arg(dev._dims(like))
+        N.check(N.lib().tt_cuda_drainagebasins_dev(dev._p(out), dev._p(source), dev._p(target),
+                                                   int(source.numel()), dp, dev._stream()),
+                "drainagebasins_dev")
         return out
 
     @staticmethod

@@ -183,6 +183,20 @@ tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,
                                       float altitude, float cellsize,
                                       const GridDims &g, cudaStream_t st);
 
+// Edge-list forms.
+tt_cuda_status edgelist_dev(ptrdiff_t *source, ptrdiff_t *target, int64_t *count,
+                            const ptrdiff_t *node, const uint8_t *dir, const GridDims &g,
+                            unsigned order, cudaStream_t st);
+tt_cuda_status accumulate_edgelist_dev(float *acc, const ptrdiff_t *source,
+                                       const ptrdiff_t *target, const float *fraction,
+                                       const float *weights, int64_t E, const GridDims &g,
+                                       cudaStream_t st);
+tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
+                                  const ptrdiff_t *target, int64_t E, const GridDims &g,
+                                  cudaStream_t st);
+tt_cuda_status degree_dev(uint8_t *indegree, uint8_t *outdegree, const ptrdiff_t *source,
+                          const ptrdiff_t *target, int64_t N, int64_t E, cudaStream_t st);
+
 // Sun vector of src/hillshade.c:104-106, evaluated in double and rounded.
 void sun_vector(float azimuth, float altitude, float *sx, float *sy, float *sz);
 

@@ -357,6 +357,61 @@ tt_cuda_status tt_cuda_flow_accumulation_dev(float *acc,
   });
 }
 
+// Edge-list forms (device pointers).
+static bool edges_ok(ptrdiff_t E) { return E >= 0 && E < (1LL << 31); }
+
+tt_cuda_status tt_cuda_flow_routing_d8_edgelist_dev(ptrdiff_t *source, ptrdiff_t *target,
+                                                    ptrdiff_t *edge_count,
+                                                    const ptrdiff_t *node,
+                                                    const uint8_t *direction,
+                                                    const ptrdiff_t dims[2],
+                                                    unsigned int order, void *stream) {
+  if (!source || !target || !edge_count || !node || !direction)
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    int64_t c = 0;
+    tt_cuda_status s = edgelist_dev(source, target, &c, node, direction, g, order, st);
+    *edge_count = (ptrdiff_t)c;
+    return s;
+  });
+}
+
+tt_cuda_status tt_cuda_flow_accumulation_edgelist_dev(float *acc, const ptrdiff_t *source,
+                                                      const ptrdiff_t *target,
+                                                      const float *fraction,
+                                                      const float *weights,
+                                                      ptrdiff_t edge_count,
+                                                      const ptrdiff_t dims[2], void *stream) {
+  if (!acc || (edge_count > 0 && (!source || !target || !fraction)) || !edges_ok(edge_count))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return accumulate_edgelist_dev(acc, source, target, fraction, weights, edge_count, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
+                                          const ptrdiff_t *target, ptrdiff_t edge_count,
+                                          const ptrdiff_t dims[2], void *stream) {
+  if (!basins || (edge_count > 0 && (!source || !target)) || !edges_ok(edge_count))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(dims, stream, [&](const GridDims &g, cudaStream_t st) {
+    return drainagebasins_dev(basins, source, target, edge_count, g, st);
+  });
+}
+
+tt_cuda_status tt_cuda_edgelist_degree_dev(uint8_t *indegree, uint8_t *outdegree,
+                                           const ptrdiff_t *source, const ptrdiff_t *target,
+                                           ptrdiff_t node_count, ptrdiff_t edge_count,
+                                           void *stream) {
+  if (!indegree || !outdegree || (edge_count > 0 && (!source || !target)) ||
+      !edges_ok(edge_count))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  const ptrdiff_t nd[2] = {node_count, 1};
+  return dev_call(nd, stream, [&](const GridDims &g, cudaStream_t st) {
+    return degree_dev(indegree, outdegree, source, target, g.cells(), edge_count, st);
+  });
+}
+
 tt_cuda_status tt_cuda_flow_accumulation_backward_dev(float *grad_weights,
                                                       const uint8_t *direction,
                                                       const float *grad_acc,
@@ -621,6 +676,87 @@ void tt_cuda_flow_accumulation(float *acc, ptrdiff_t *source,
             [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
               return accumulate_dev((float *)a[0].dev, (const uint8_t *)a[1].dev,
                                     weights ? (const float *)a[2].dev : nullptr, g, st);
+            });
+}
+
+ptrdiff_t tt_cuda_flow_routing_d8_edgelist(ptrdiff_t *source, ptrdiff_t *target,
+                                           ptrdiff_t *node, uint8_t *direction,
+                                           ptrdiff_t dims[2], unsigned int order) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  if (!source || !target) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return 0;
+  }
+  int64_t count = 0;
+  host_call(dims,
+            {{node, N * 8, true, false}, {direction, N, true, false},
+             {source, N * 8, false, false}, {target, N * 8, false, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              tt_cuda_status s = edgelist_dev((ptrdiff_t *)a[2].dev, (ptrdiff_t *)a[3].dev,
+                                              &count, (const ptrdiff_t *)a[0].dev,
+                                              (const uint8_t *)a[1].dev, g, order, st);
+              if (s != TT_CUDA_SUCCESS) return s;
+              // only the edges found are copied back
+              TT_TRY(d2h(source, a[2].dev, (size_t)count * 8, st));
+              TT_TRY(d2h(target, a[3].dev, (size_t)count * 8, st));
+              return TT_CUDA_SUCCESS;
+            });
+  return get_status() == TT_CUDA_SUCCESS ? (ptrdiff_t)count : 0;
+}
+
+void tt_cuda_flow_accumulation_edgelist(float *acc, ptrdiff_t *source, ptrdiff_t *target,
+                                        float *fraction, float *weights,
+                                        ptrdiff_t edge_count, ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  if (!edges_ok(edge_count)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  const size_t E = (size_t)edge_count;
+  host_call(dims,
+            {{acc, N * 4, false, true}, {source, E * 8, E > 0, false},
+             {target, E * 8, E > 0, false}, {fraction, E * 4, E > 0, false},
+             {weights, weights ? N * 4 : 0, weights != nullptr, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return accumulate_edgelist_dev(
+                  (float *)a[0].dev, (const ptrdiff_t *)a[1].dev, (const ptrdiff_t *)a[2].dev,
+                  (const float *)a[3].dev, weights ? (const float *)a[4].dev : nullptr,
+                  edge_count, g, st);
+            });
+}
+
+void tt_cuda_drainagebasins(ptrdiff_t *basins, ptrdiff_t *source, ptrdiff_t *target,
+                            ptrdiff_t edge_count, ptrdiff_t dims[2]) {
+  size_t N = dims ? (size_t)(dims[0] * dims[1]) : 0;
+  if (!edges_ok(edge_count)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  const size_t E = (size_t)edge_count;
+  host_call(dims,
+            {{basins, N * 8, false, true}, {source, E * 8, E > 0, false},
+             {target, E * 8, E > 0, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return drainagebasins_dev((ptrdiff_t *)a[0].dev, (const ptrdiff_t *)a[1].dev,
+                                        (const ptrdiff_t *)a[2].dev, edge_count, g, st);
+            });
+}
+
+void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree, ptrdiff_t *source,
+                             ptrdiff_t *target, ptrdiff_t node_count, ptrdiff_t edge_count) {
+  if (!edges_ok(edge_count)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  const size_t E = (size_t)edge_count, N = node_count > 0 ? (size_t)node_count : 0;
+  ptrdiff_t nd[2] = {node_count, 1};
+  host_call(nd,
+            {{indegree, N, false, true}, {outdegree, N, false, true},
+             {source, E * 8, E > 0, false}, {target, E * 8, E > 0, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return degree_dev((uint8_t *)a[0].dev, (uint8_t *)a[1].dev,
+                                (const ptrdiff_t *)a[2].dev, (const ptrdiff_t *)a[3].dev,
+                                g.cells(), edge_count, st);
             });
 }
 

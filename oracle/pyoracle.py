@@ -83,6 +83,10 @@ class Oracle:
             "flow_accumulation": (None, [P, P, P, P, PD]),
             "hillshade_fused": (None, [P, P, F, F, F, PD]),
             "hillshade": (None, [P, P, P, P, F, F, F, PD]),
+            "flow_routing_d8_edgelist": (C.c_int64, [P, P, P, P, PD, C.c_uint]),
+            "flow_accumulation_edgelist": (None, [P, P, P, P, P, C.c_int64, PD]),
+            "drainagebasins": (None, [P, P, P, C.c_int64, PD]),
+            "edgelist_degree": (None, [P, P, P, P, C.c_int64, C.c_int64]),
         }
         if kind == "port":
             sig.update({
@@ -91,6 +95,7 @@ class Oracle:
                 "flow_accumulation_f64w": (None, [P, P, P, P, PD]),
                 "hillshade_f64": (None, [P, P, D, D, D, PD]),
                 "hillshade_backward_f64": (None, [P, P, P, D, D, D, PD]),
+                "flow_accumulation_edgelist_f64": (None, [P, P, P, P, P, C.c_int64, PD]),
             })
         self.fn = {}
         for name, (res, args) in sig.items():
@@ -224,6 +229,47 @@ class Oracle:
         self.fn["hillshade_backward_f64"](_ptr(out), _ptr(dem), _ptr(g), float(az), float(alt),
                                           float(cs), dp)
         return out
+
+    # ---- edge-list forms -------------------------------------------------
+    def flow_routing_d8_edgelist(self, node, direction, order=0):
+        node = np.asfortranarray(node, dtype=np.int64)
+        direction = np.asfortranarray(direction, dtype=np.uint8)
+        n = direction.size
+        src = np.empty(n, dtype=np.int64)
+        tgt = np.empty(n, dtype=np.int64)
+        dp, k = _dims(direction.shape)
+        e = self.fn["flow_routing_d8_edgelist"](_ptr(src), _ptr(tgt), _ptr(node),
+                                                _ptr(direction), dp, int(order))
+        return src[:e].copy(), tgt[:e].copy()
+
+    def flow_accumulation_edgelist(self, source, target, fraction, shape, weights=None,
+                                   f64=False):
+        src = np.ascontiguousarray(source, dtype=np.int64)
+        tgt = np.ascontiguousarray(target, dtype=np.int64)
+        fr = np.ascontiguousarray(fraction, dtype=np.float32)
+        w = _f32(weights) if weights is not None else None
+        acc = np.empty(shape, dtype=np.float64 if f64 else np.float32, order="F")
+        dp, k = _dims(shape)
+        name = "flow_accumulation_edgelist_f64" if f64 else "flow_accumulation_edgelist"
+        self.fn[name](_ptr(acc), _ptr(src), _ptr(tgt), _ptr(fr), _ptr(w), len(src), dp)
+        return acc
+
+    def drainagebasins(self, source, target, shape):
+        src = np.ascontiguousarray(source, dtype=np.int64)
+        tgt = np.ascontiguousarray(target, dtype=np.int64)
+        out = np.empty(shape, dtype=np.int64, order="F")
+        dp, k = _dims(shape)
+        self.fn["drainagebasins"](_ptr(out), _ptr(src), _ptr(tgt), len(src), dp)
+        return out
+
+    def edgelist_degree(self, source, target, node_count):
+        src = np.ascontiguousarray(source, dtype=np.int64)
+        tgt = np.ascontiguousarray(target, dtype=np.int64)
+        indeg = np.empty(node_count, dtype=np.uint8)
+        outdeg = np.empty(node_count, dtype=np.uint8)
+        self.fn["edgelist_degree"](_ptr(indeg), _ptr(outdeg), _ptr(src), _ptr(tgt),
+                                   int(node_count), len(src))
+        return indeg, outdeg
 
     def pipeline(self, dem, bc, weights=None, hybrid=True):
         """fill -> flats -> costs -> gwdt -> carve -> accumulation, the call

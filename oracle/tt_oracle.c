@@ -653,3 +653,79 @@ void orc_hillshade_backward_f64(double *grad_dem, const double *dem,
       grad_axis_adj(grad_dem, p, m, j, n, cs, g * hy);
     }
 }
+
+/* ------------------------------------------------------------------
+ * Edge-list forms.
+ * ------------------------------------------------------------------ */
+
+/* src/flow_routing.c:258-312.  With strides s0 (between rows) and s1
+ * (between columns) of the given memory order, bit r of a direction byte
+ * points at linear offset {s1, s0+s1, s0, s0-s1, -s1, -s0-s1, -s0, -s0+s1}[r]. */
+ptrdiff_t orc_flow_routing_d8_edgelist(ptrdiff_t *source, ptrdiff_t *target,
+                                       const ptrdiff_t *node,
+                                       const uint8_t *direction,
+                                       const ptrdiff_t dims[2], unsigned order) {
+  const ptrdiff_t s0 = (order & 1) ? dims[0] : 1;
+  const ptrdiff_t s1 = (order & 1) ? 1 : dims[0];
+  const ptrdiff_t off[8] = {s1, s0 + s1, s0, s0 - s1, -s1, -s0 - s1, -s0, -s0 + s1};
+  const ptrdiff_t n = dims[0] * dims[1];
+  ptrdiff_t count = 0;
+  for (ptrdiff_t k = 0; k < n; k++) {
+    const ptrdiff_t u = node[k];
+    const uint8_t d = direction[u];
+    if (!d) continue;
+    source[count] = u;
+    target[count] = u + off[bit_index(d)];
+    count++;
+  }
+  return count;
+}
+
+/* src/flow_accumulation.c:10-30 */
+void orc_flow_accumulation_edgelist(float *acc, const ptrdiff_t *source,
+                                    const ptrdiff_t *target,
+                                    const float *fraction, const float *weights,
+                                    ptrdiff_t edge_count, const ptrdiff_t dims[2]) {
+  const ptrdiff_t n = dims[0] * dims[1];
+  for (ptrdiff_t p = 0; p < n; p++) acc[p] = weights ? weights[p] : 1.0f;
+  for (ptrdiff_t e = 0; e < edge_count; e++) {
+    const float add = fraction[e] * acc[source[e]];
+    acc[target[e]] = acc[target[e]] + add;
+  }
+}
+
+void orc_flow_accumulation_edgelist_f64(double *acc, const ptrdiff_t *source,
+                                        const ptrdiff_t *target,
+                                        const float *fraction,
+                                        const float *weights,
+                                        ptrdiff_t edge_count,
+                                        const ptrdiff_t dims[2]) {
+  const ptrdiff_t n = dims[0] * dims[1];
+  for (ptrdiff_t p = 0; p < n; p++) acc[p] = weights ? (double)weights[p] : 1.0;
+  for (ptrdiff_t e = 0; e < edge_count; e++)
+    acc[target[e]] += (double)fraction[e] * acc[source[e]];
+}
+
+/* src/drainagebasins.c:6-27 */
+void orc_drainagebasins(ptrdiff_t *basins, const ptrdiff_t *source,
+                        const ptrdiff_t *target, ptrdiff_t edge_count,
+                        const ptrdiff_t dims[2]) {
+  const ptrdiff_t n = dims[0] * dims[1];
+  for (ptrdiff_t p = 0; p < n; p++) basins[p] = 0;
+  ptrdiff_t next = 1;
+  for (ptrdiff_t e = edge_count - 1; e >= 0; e--) {
+    if (basins[target[e]] == 0) basins[target[e]] = next++;
+    basins[source[e]] = basins[target[e]];
+  }
+}
+
+/* src/streamquad.c:209-224 */
+void orc_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
+                         const ptrdiff_t *source, const ptrdiff_t *target,
+                         ptrdiff_t node_count, ptrdiff_t edge_count) {
+  for (ptrdiff_t v = 0; v < node_count; v++) indegree[v] = outdegree[v] = 0;
+  for (ptrdiff_t e = 0; e < edge_count; e++) {
+    indegree[target[e]]++;
+    outdegree[source[e]]++;
+  }
+}

@@ -83,6 +83,41 @@ void orc_hillshade_backward_f64(double *grad_dem, const double *dem,
                                 double altitude, double cellsize,
                                 const ptrdiff_t dims[2]);
 
+/* ---- Edge-list forms (the callers of the path's outputs) ---- */
+
+/* src/flow_routing.c:258-312: one edge (u, receiver(u)) per pixel u with a
+ * direction, listed in `node` order; neighbour offsets from the memory
+ * order (order & 1: row-major).  Returns the edge count. */
+ptrdiff_t orc_flow_routing_d8_edgelist(ptrdiff_t *source, ptrdiff_t *target,
+                                       const ptrdiff_t *node,
+                                       const uint8_t *direction,
+                                       const ptrdiff_t dims[2], unsigned order);
+/* src/flow_accumulation.c:10-30: acc = weights (or 1), then
+ * acc[target] += fraction * acc[source] edge by edge in list order. */
+void orc_flow_accumulation_edgelist(float *acc, const ptrdiff_t *source,
+                                    const ptrdiff_t *target,
+                                    const float *fraction, const float *weights,
+                                    ptrdiff_t edge_count, const ptrdiff_t dims[2]);
+/* The same sweep in FP64 (fractions and weights widened).  No counterpart in
+ * the reference; the tolerance oracle for the float32 results. */
+void orc_flow_accumulation_edgelist_f64(double *acc, const ptrdiff_t *source,
+                                        const ptrdiff_t *target,
+                                        const float *fraction,
+                                        const float *weights,
+                                        ptrdiff_t edge_count,
+                                        const ptrdiff_t dims[2]);
+/* src/drainagebasins.c:6-27: labels 1, 2, ... assigned in reverse edge
+ * order to the first unlabelled target met; every source takes its
+ * target's label; pixels on no edge stay 0. */
+void orc_drainagebasins(ptrdiff_t *basins, const ptrdiff_t *source,
+                        const ptrdiff_t *target, ptrdiff_t edge_count,
+                        const ptrdiff_t dims[2]);
+/* src/streamquad.c:209-224: in- and out-degree of every node (uint8,
+ * wrapping as the reference's counters do). */
+void orc_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
+                         const ptrdiff_t *source, const ptrdiff_t *target,
+                         ptrdiff_t node_count, ptrdiff_t edge_count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,3 +122,38 @@ def test_reference_properties(port, idx):
     assert np.all((costs > 0) == ((flats & 1) > 0))  # :203-214
     assert topo_positions_ok(r["node"], r["direction"])
     assert np.all(r["acc"] <= dem.size)  # :417-425
+
+
+@pytest.mark.parametrize("idx", range(len(DEMS)))
+@pytest.mark.parametrize("order", [0, 1])
+def test_port_edgelists_equal_reference(port, ref, idx, order):
+    """Edge lists, edge-list accumulation, drainage basins and degrees
+    (src/flow_routing.c:258-312, src/flow_accumulation.c:10-30,
+    src/drainagebasins.c:6-27, src/streamquad.c:209-224)."""
+    name, dem, bc = DEMS[idx]
+    r = port.pipeline(dem, bc)
+    node, direction = port.flow_routing_d8_carve(r["filled"], r["dist"], r["flats"], order)
+    sp, tp = port.flow_routing_d8_edgelist(node, direction, order)
+    sr, tr = ref.flow_routing_d8_edgelist(node, direction, order)
+    assert np.array_equal(sp, sr) and np.array_equal(tp, tr), name
+    fr = np.ones(len(sp), np.float32)
+    rng = np.random.default_rng(idx)
+    w = np.asfortranarray(rng.uniform(0.5, 1.5, dem.shape).astype(np.float32))
+    for weights in (None, w):
+        a = port.flow_accumulation_edgelist(sp, tp, fr, dem.shape, weights)
+        b = ref.flow_accumulation_edgelist(sp, tp, fr, dem.shape, weights)
+        assert same_float(a, b), name
+    fr2 = rng.uniform(0.0, 1.0, len(sp)).astype(np.float32)
+    assert same_float(port.flow_accumulation_edgelist(sp, tp, fr2, dem.shape),
+                      ref.flow_accumulation_edgelist(sp, tp, fr2, dem.shape)), name
+    assert np.array_equal(port.drainagebasins(sp, tp, dem.shape),
+                          ref.drainagebasins(sp, tp, dem.shape)), name
+    for a, b in zip(port.edgelist_degree(sp, tp, dem.size), ref.edgelist_degree(sp, tp, dem.size)):
+        assert np.array_equal(a, b), name
+    # the edge list is the D8 forest in topological order: every source
+    # appears once, before any edge whose source is its target
+    assert len(np.unique(sp)) == len(sp)
+    pos = np.full(dem.size, -1)
+    pos[sp] = np.arange(len(sp))
+    later = pos[tp]
+    assert np.all((later == -1) | (later > np.arange(len(sp))))
