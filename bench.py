@@ -278,6 +278,61 @@ def batch_leg(dev, reps=3):
             "graph_nodes": info["graph_nodes"], "tuned_canvas_cols": best["canvas_cols"]}
 
 
+def edges_leg(dev, node, direction, reps=5):
+    """The edge-list rows on the workload's own node order and directions:
+    flow_routing_d8_edgelist, drainagebasins and flow_accumulation_edgelist
+    (device pointers, CUDA events), beside the oracle's C restatement of the
+    reference on one host core."""
+    import torch
+
+    from libtopotoolbox_gb300.api import dev as D
+
+    cells = direction.numel()
+    src, tgt = D.flow_routing_d8_edgelist(node, direction)
+    fr = torch.ones(src.numel(), dtype=torch.float32, device=dev)
+    like = torch.empty(direction.shape, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    ms = {
+        "flow_routing_d8_edgelist": timed(lambda: D.flow_routing_d8_edgelist(node, direction)),
+        "drainagebasins": timed(lambda: D.drainagebasins(src, tgt, like)),
+        "flow_accumulation_edgelist": timed(lambda: D.flow_accumulation_edgelist(src, tgt, fr,
+                                                                                   like)),
+    }
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    orc = pyoracle.Oracle("port")
+    nd = node.cpu().numpy().T.copy(order="F")
+    dr = direction.cpu().numpy().T.copy(order="F")
+    cpu = {}
+    t0 = time.perf_counter()
+    hs, ht = orc.flow_routing_d8_edgelist(nd, dr)
+    cpu["flow_routing_d8_edgelist"] = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    orc.drainagebasins(hs, ht, dr.shape)
+    cpu["drainagebasins"] = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    orc.flow_accumulation_edgelist(hs, ht, np.ones(len(hs), np.float32), dr.shape)
+    cpu["flow_accumulation_edgelist"] = (time.perf_counter() - t0) * 1e3
+    return {"workload": f"edge list of the {dr.shape[0]}x{dr.shape[1]} workload "
+                        f"({int(src.numel())} edges)",
+            "gpu_ms": ms, "gcells_s": {k: cells / (v * 1e-3) / 1e9 for k, v in ms.items()},
+            "cpu_port_ms_1core": cpu,
+            "speedup_vs_cpu": {k: cpu[k] / ms[k] for k in ms}}
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -342,6 +397,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-edges", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -521,6 +577,8 @@ def main():
         line["adjoint"] = adjoint_leg(dev)
     if not args.no_batch:
         line["batched"] = batch_leg(dev)
+    if not args.no_edges:
+        line["edges"] = edges_leg(dev, o["node"], o["direction"])
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
     print(json.dumps(line), flush=True)

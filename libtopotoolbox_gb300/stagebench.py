@@ -21,11 +21,12 @@ BYTES = {
     "flow_routing_d8_carve": 21, "flow_accumulation": 13,
     "flow_accumulation_weighted": 17, "flow_accumulation_backward": 9,
     "hillshade_fused": 8, "hillshade_backward": 12, "pipeline": 87,
+    "flow_routing_d8_edgelist": 25, "drainagebasins": 24, "flow_accumulation_edgelist": 24,
 }
 STAGES = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
           "flow_routing_d8_carve", "flow_accumulation", "flow_accumulation_weighted",
           "flow_accumulation_backward", "hillshade_fused", "hillshade_backward", "pipeline",
-          "batch"]
+          "flow_routing_d8_edgelist", "drainagebasins", "flow_accumulation_edgelist", "batch"]
 
 
 def load(workload, size):
@@ -137,9 +138,15 @@ def main(argv=None):
         flats = dev.identifyflats(filled)
         costs, _ = dev.gwdt_computecosts(flats, d_dem, filled)
         dist = dev.gwdt(costs, flats)
-        _, direction = dev.flow_routing_d8_carve(filled, dist, flats, want_node=False)
+        edges = st in ("flow_routing_d8_edgelist", "drainagebasins", "flow_accumulation_edgelist")
+        node, direction = dev.flow_routing_d8_carve(filled, dist, flats, want_node=edges)
         g = torch.rand_like(d_dem) * 2 - 1
-        ctx = dict(filled=filled, flats=flats, costs=costs, dist=dist, direction=direction, g=g)
+        src = tgt = fr = None
+        if edges:
+            src, tgt = dev.flow_routing_d8_edgelist(node, direction)
+            fr = torch.ones(src.numel(), dtype=torch.float32, device=dv)
+        ctx = dict(filled=filled, flats=flats, costs=costs, dist=dist, direction=direction, g=g,
+                   node=node, src=src, tgt=tgt, fr=fr)
     torch.cuda.synchronize()
 
     def call():
@@ -164,6 +171,12 @@ def main(argv=None):
             dev.hillshade_fused(d_dem, 3.9269908, 1.0471976, cs)
         elif st == "hillshade_backward":
             dev.hillshade_backward(d_dem, c["g"], 3.9269908, 1.0471976, cs)
+        elif st == "flow_routing_d8_edgelist":
+            dev.flow_routing_d8_edgelist(c["node"], c["direction"])
+        elif st == "drainagebasins":
+            dev.drainagebasins(c["src"], c["tgt"], d_dem)
+        elif st == "flow_accumulation_edgelist":
+            dev.flow_accumulation_edgelist(c["src"], c["tgt"], c["fr"], d_dem)
         else:
             dev.d8_pipeline(d_dem, d_bc)
 
