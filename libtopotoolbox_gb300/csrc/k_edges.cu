@@ -210,30 +210,109 @@ __global__ void basins_parent_kernel(const ptrdiff_t *__restrict__ source,
   }
 }
 
-// One round of pointer jumping: parent = parent[parent]; counts changes.
-__global__ void basins_jump_kernel(const int *__restrict__ in, int *__restrict__ out,
-                                   int64_t N, int *__restrict__ changed) {
+// One block per 32 x 32 tile: every pixel's in-tile terminal (a root, or an
+// exit: a pixel whose parent lies in another tile) by pointer jumping in
+// shared memory; exits are appended to a list.  J[p] = p for roots and
+// parent(p) for exits (the coarse pointer the next kernel jumps on).
+__global__ void __launch_bounds__(256)
+basins_tile_kernel(const int *__restrict__ parent, int64_t m, int64_t n, int tm, int tn,
+                   int *__restrict__ term, int *__restrict__ J, int *__restrict__ exits,
+                   int *__restrict__ nexits, int *__restrict__ err) {
+  __shared__ int ptr[kTile * kTile];
+  const int T = tm * tn;
+  for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
+    const int ti = tile % tm, tj = tile / tm;
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+      const int64_t i = i0 + (e & 31), j = j0 + (e >> 5);
+      int v = e;
+      if (i < m && j < n) {
+        const int64_t p = j * m + i, q = parent[p];
+        const int64_t qi = q % m, qj = q / m;
+        if (q != p && qi >= i0 && qi < i0 + kTile && qj >= j0 && qj < j0 + kTile)
+          v = (int)((qj - j0) * kTile + (qi - i0));
+      }
+      ptr[e] = v;
+    }
+    __syncthreads();
+    for (int round = 0; round < 12; round++) {
+      int moved = 0;
+      for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int a = ptr[e], b = ptr[a];
+        if (a != b) {
+          ptr[e] = b;
+          moved = 1;
+        }
+      }
+      if (!__syncthreads_or(moved)) break;
+    }
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+      const int64_t i = i0 + (e & 31), j = j0 + (e >> 5);
+      if (i >= m || j >= n) continue;
+      const int64_t p = j * m + i;
+      const int t = ptr[e];
+      if (ptr[t] != t) atomicOr(err, EL_CYCLE);  // chain never ended in-tile
+      term[p] = (int)((j0 + (t >> 5)) * m + (i0 + (t & 31)));
+      if (t == e) {  // a terminal: root, or exit with its parent outside
+        const int q = parent[p];
+        J[p] = q;
+        if (q != (int)p) exits[atomicAdd(nexits, 1)] = (int)p;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Coarse pointers: an exit's pointer starts at its parent's in-tile
+// terminal; one round of jumping over the exit list.
+__global__ void exits_init_kernel(const int *__restrict__ exits, const int *__restrict__ nexits,
+                                  const int *__restrict__ term, int *__restrict__ J) {
+  const int E = *nexits;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < E; k += gridDim.x * blockDim.x) {
+    const int x = exits[k];
+    J[x] = term[J[x]];
+  }
+}
+
+__global__ void exits_jump_kernel(const int *__restrict__ exits, const int *__restrict__ nexits,
+                                  int *__restrict__ J, int *__restrict__ changed) {
+  const int E = *nexits;
   int c = 0;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int q = in[p];
-    const int r = in[q];
-    out[p] = r;
-    c |= r != q;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < E; k += gridDim.x * blockDim.x) {
+    const int x = exits[k];
+    const int a = J[x], b = J[a];
+    if (a != b) {
+      J[x] = b;
+      c = 1;
+    }
   }
   if (__any_sync(0xffffffffu, c) && (threadIdx.x & 31) == 0) atomicOr(changed, 1);
 }
 
+__global__ void basins_root_kernel(const int *__restrict__ term, const int *__restrict__ J,
+                                   int64_t N, int *__restrict__ root) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x)
+    root[p] = J[term[p]];
+}
+
 // key[root] = largest edge index among the pixels of the basin.  A root
 // must have no out-edge; one that has lies on a cycle of the edge list.
+// Large basins put millions of pixels on one key: lanes with the same root
+// are reduced first and one atomic per root and warp is issued.
 __global__ void basins_key_kernel(const int *__restrict__ root, const int *__restrict__ first,
                                   int64_t N, int *__restrict__ key, int *__restrict__ err) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int f = first[p];
-    const int r = root[p];
-    if (f != INT_MAX) atomicMax(&key[r], f);
-    if (r == (int)p && f != INT_MAX) atomicOr(err, EL_CYCLE);
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < N;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;  // whole warps iterate together
+    const bool in = p < N;
+    const int f = in ? first[p] : INT_MAX;
+    const int r = in ? root[p] : -1;
+    if (in && r == (int)p && f != INT_MAX) atomicOr(err, EL_CYCLE);
+    const unsigned grp = __match_any_sync(0xffffffffu, r);
+    const int mx = __reduce_max_sync(grp, f == INT_MAX ? -1 : f);
+    if (in && lane == __ffs(grp) - 1 && mx >= 0) atomicMax(&key[r], mx);
   }
 }
 
@@ -400,14 +479,16 @@ tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
   const int64_t Em = std::max<int64_t>(E, 1);
   const int nb = (int)((Em + kScanBlock - 1) / kScanBlock);
   Workspace &ws = workspace();
-  const size_t need = 4 * align_up((size_t)N * 4) + 2 * align_up((size_t)Em * 4) +
+  const size_t need = 6 * align_up((size_t)N * 4) + 2 * align_up((size_t)Em * 4) +
                       2 * align_up((size_t)(nb + 1) * 4) + 256;
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
-  int *ctl = (int *)ws.take(256);  // [0] error bits, [1] changed
+  int *ctl = (int *)ws.take(256);  // [0] error bits, [1] changed, [2] exit count
   int *first = (int *)ws.take((size_t)N * 4);
   int *pa = (int *)ws.take((size_t)N * 4);
   int *pb = (int *)ws.take((size_t)N * 4);
   int *key = (int *)ws.take((size_t)N * 4);
+  int *rootp = (int *)ws.take((size_t)N * 4);
+  int *ex_list = (int *)ws.take((size_t)N * 4);
   int *mark = (int *)ws.take((size_t)Em * 4);
   int *ex = (int *)ws.take((size_t)Em * 4);
   int *cnt = (int *)ws.take((size_t)(nb + 1) * 4);
@@ -418,27 +499,33 @@ tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
   TT_LAUNCH(basins_first_kernel, gE, 256, 0, st, source, E, N, first, ctl);
   TT_LAUNCH(basins_parent_kernel, gE, 256, 0, st, source, target, E, N, first, pa, ctl);
   TT_CHECK(cudaGetLastError());
-  // Pointer jumping to the roots; a chain of length L needs log2(L) rounds.
-  int *cur = pa, *nxt = pb;
+  // Roots: in-tile terminals by pointer jumping in shared memory, then
+  // jumping over the exits only, then every pixel through its terminal.
+  int *term = pb, *J = key, *root = rootp;  // key is free until the keys are taken
+  int *exits = ex_list, *nexits = ctl + 2;
+  TT_LAUNCH(basins_tile_kernel, (int)std::min<int64_t>(g.tiles(), (int64_t)sm_count() * 8), 256,
+            0, st, pa, g.m, g.n, g.tm, g.tn, term, J, exits, nexits, ctl);
+  TT_LAUNCH(exits_init_kernel, gN, 256, 0, st, exits, nexits, term, J);
   int *h = (int *)pinned_scratch();
   if (!h) return TT_CUDA_ERR_ALLOC;
   bool converged = false;
   for (int round = 0; round < 40; round += 4) {
     TT_CHECK(cudaMemsetAsync(ctl + 1, 0, 4, st));
-    for (int k = 0; k < 4; k++) {
-      TT_LAUNCH(basins_jump_kernel, gN, 256, 0, st, cur, nxt, N, ctl + 1);
-      std::swap(cur, nxt);
-    }
+    for (int k = 0; k < 4; k++)
+      TT_LAUNCH(exits_jump_kernel, gN, 256, 0, st, exits, nexits, J, ctl + 1);
     TT_CHECK(cudaGetLastError());
     TT_CHECK(cudaMemcpyAsync(h, ctl, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     TT_CHECK(cudaStreamSynchronize(st));
-    if (h[0]) return TT_CUDA_ERR_INVALID_ARGUMENT;
+    if (h[0] & EL_BAD_INDEX) return TT_CUDA_ERR_INVALID_ARGUMENT;
+    if (h[0] & EL_CYCLE) return TT_CUDA_ERR_CYCLE;
     if (!h[1]) {
       converged = true;
       break;
     }
   }
   if (!converged) return TT_CUDA_ERR_CYCLE;
+  TT_LAUNCH(basins_root_kernel, gN, 256, 0, st, term, J, N, root);
+  int *cur = root;
   TT_CHECK(cudaMemsetAsync(key, 0xff, (size_t)N * 4, st));  // -1: no edge in basin
   TT_CHECK(cudaMemsetAsync(mark, 0, (size_t)Em * 4, st));
   TT_LAUNCH(basins_key_kernel, gN, 256, 0, st, cur, first, N, key, ctl);
