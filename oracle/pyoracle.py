@@ -72,6 +72,7 @@ class Oracle:
             raise FileNotFoundError(path)
         self.lib = C.CDLL(str(path))
         pre = "orc_" if kind == "port" else ""
+        D = C.c_double
         self._pre = pre
         sig = {
             "fillsinks": (None, [P, P, P, PD]),
@@ -87,6 +88,10 @@ class Oracle:
             "flow_accumulation_edgelist": (None, [P, P, P, P, P, C.c_int64, PD]),
             "drainagebasins": (None, [P, P, P, C.c_int64, PD]),
             "edgelist_degree": (None, [P, P, P, P, C.c_int64, C.c_int64]),
+            "compute_sfgraph": (None, [P, P, P, P, P, P, P, P, D,
+                                       C.c_int if kind == "port" else C.c_bool]),
+            "compute_drainage_area_single_flow": (None, [P, P, P, P, D]),
+            "compute_weighted_drainage_area_single_flow": (None, [P, P, P, P, P, D]),
         }
         if kind == "port":
             sig.update({
@@ -270,6 +275,37 @@ class Oracle:
         self.fn["edgelist_degree"](_ptr(indeg), _ptr(outdeg), _ptr(src), _ptr(tgt),
                                    int(node_count), len(src))
         return indeg, outdeg
+
+    # ---- graphflood single-flow graph (row-major, C-ordered arrays) -------
+    def compute_sfgraph(self, topo, bcs, dx, d8=True):
+        topo = np.ascontiguousarray(topo, dtype=np.float64)
+        bcs = np.ascontiguousarray(bcs, dtype=np.uint8)
+        n = topo.size
+        k = 8 if d8 else 4
+        rcv = np.empty(n, dtype=np.uint64)
+        dist = np.empty(n, dtype=np.float64)
+        don = np.zeros(n * k, dtype=np.uint64)
+        ndon = np.empty(n, dtype=np.uint8)
+        stack = np.empty(n, dtype=np.uint64)
+        dim = (C.c_size_t * 2)(*topo.shape)
+        self.fn["compute_sfgraph"](_ptr(topo), _ptr(rcv), _ptr(dist), _ptr(don), _ptr(ndon),
+                                   _ptr(stack), _ptr(bcs), C.cast(dim, P), float(dx),
+                                   bool(d8))
+        return rcv, dist, don.reshape(n, k), ndon, stack
+
+    def compute_drainage_area_single_flow(self, rcv, stack, shape, dx, weights=None):
+        rcv = np.ascontiguousarray(rcv, dtype=np.uint64)
+        stack = np.ascontiguousarray(stack, dtype=np.uint64)
+        out = np.empty(int(np.prod(shape)), dtype=np.float64)
+        dim = (C.c_size_t * 2)(*shape)
+        if weights is None:
+            self.fn["compute_drainage_area_single_flow"](_ptr(out), _ptr(rcv), _ptr(stack),
+                                                         C.cast(dim, P), float(dx))
+        else:
+            w = np.ascontiguousarray(weights, dtype=np.float64).ravel()
+            self.fn["compute_weighted_drainage_area_single_flow"](
+                _ptr(out), _ptr(w), _ptr(rcv), _ptr(stack), C.cast(dim, P), float(dx))
+        return out.reshape(shape)
 
     def pipeline(self, dem, bc, weights=None, hybrid=True):
         """fill -> flats -> costs -> gwdt -> carve -> accumulation, the call

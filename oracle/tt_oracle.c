@@ -729,3 +729,105 @@ void orc_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
     outdegree[source[e]]++;
   }
 }
+
+/* ------------------------------------------------------------------
+ * Graphflood single-flow graph.
+ * ------------------------------------------------------------------ */
+
+static int gf_can_give(uint8_t b) {
+  return b == 1 || b == 3 || b == 6 || b == 7 || b == 8 || b == 9;
+}
+static int gf_can_receive(uint8_t b) {
+  return b == 1 || b == 3 || b == 4 || b == 5 || b == 6 || b == 7 || b == 9;
+}
+
+/* Neighbour n of `node` exists (no wrap across the first/last row or
+ * column; src/graphflood/gf_utils.c:202-253). */
+static int gf_neighbour_ok(size_t node, int n, const size_t dim[2], int D8) {
+  const size_t N = dim[0] * dim[1], c = node % dim[1];
+  if (node < dim[1] && (D8 ? n < 3 : n == 0)) return 0;
+  if (node >= N - dim[1] && (D8 ? n >= 5 : n == 3)) return 0;
+  if (c == 0 && (D8 ? (n == 0 || n == 3 || n == 5) : n == 1)) return 0;
+  if (c == dim[1] - 1 && (D8 ? (n == 2 || n == 4 || n == 7) : n == 2)) return 0;
+  return 1;
+}
+
+void orc_compute_sfgraph(double *topo, size_t *Sreceivers, double *distToReceivers,
+                         size_t *Sdonors, uint8_t *NSdonors, size_t *Stack,
+                         const uint8_t *BCs, const size_t dim[2], double dx, int D8) {
+  const size_t N = dim[0] * dim[1];
+  const ptrdiff_t w = (ptrdiff_t)dim[1];
+  const ptrdiff_t off8[8] = {-w - 1, -w, -w + 1, -1, 1, w - 1, w, w + 1};
+  const ptrdiff_t off4[4] = {-w, -1, 1, w};
+  const double diag = (double)sqrt(2) * dx;
+  const double dx8[8] = {diag, dx, diag, dx, dx, diag, dx, diag};
+  const int K = D8 ? 8 : 4;
+  for (size_t node = 0; node < N; node++) {
+    Sreceivers[node] = node;
+    distToReceivers[node] = 0.;
+    NSdonors[node] = 0;
+    if (!gf_can_give(BCs[node])) continue;
+    size_t best = node;
+    double bestdx = 0., slope = 0.;
+    for (int n = 0; n < K; n++) {
+      if (!gf_neighbour_ok(node, n, dim, D8)) continue;
+      const size_t q = (size_t)((ptrdiff_t)node + (D8 ? off8[n] : off4[n]));
+      if (!gf_can_receive(BCs[q])) continue;
+      const double d = D8 ? dx8[n] : dx;
+      const double s = (topo[node] - topo[q]) / d;
+      if (s > slope) {
+        best = q;
+        bestdx = d;
+        slope = s;
+      }
+    }
+    Sreceivers[node] = best;
+    distToReceivers[node] = bestdx;
+  }
+  for (size_t node = 0; node < N; node++) {
+    const size_t r = Sreceivers[node];
+    if (r != node) Sdonors[r * K + NSdonors[r]++] = node;
+  }
+  /* preorder from each root, donors in listed order */
+  size_t *todo = (size_t *)malloc(N * sizeof(size_t));
+  size_t top = 0, pos = 0;
+  for (size_t root = 0; root < N; root++) {
+    if (Sreceivers[root] != root) continue;
+    todo[top++] = root;
+    while (top) {
+      const size_t v = todo[--top];
+      Stack[pos++] = v;
+      for (int k = NSdonors[v] - 1; k >= 0; k--) todo[top++] = Sdonors[v * K + k];
+    }
+  }
+  free(todo);
+}
+
+void orc_compute_drainage_area_single_flow(double *output, const size_t *Sreceivers,
+                                           const size_t *Stack, const size_t dim[2],
+                                           double dx) {
+  const size_t N = dim[0] * dim[1];
+  const double area = dx * dx;
+  for (size_t i = 0; i < N; i++) output[i] = 0.;
+  for (size_t i = N; i-- > 0;) {
+    const size_t v = Stack[i];
+    if (v == Sreceivers[v]) continue;
+    output[v] += area;
+    output[Sreceivers[v]] += output[v];
+  }
+}
+
+void orc_compute_weighted_drainage_area_single_flow(double *output, const double *weights,
+                                                    const size_t *Sreceivers,
+                                                    const size_t *Stack,
+                                                    const size_t dim[2], double dx) {
+  const size_t N = dim[0] * dim[1];
+  const double area = dx * dx;
+  for (size_t i = 0; i < N; i++) output[i] = 0.;
+  for (size_t i = N; i-- > 0;) {
+    const size_t v = Stack[i];
+    if (v == Sreceivers[v]) continue;
+    output[v] += area * weights[v];
+    output[Sreceivers[v]] += output[v];
+  }
+}

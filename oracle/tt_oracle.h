@@ -118,6 +118,28 @@ void orc_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
                          const ptrdiff_t *source, const ptrdiff_t *target,
                          ptrdiff_t node_count, ptrdiff_t edge_count);
 
+/* ---- Graphflood single-flow graph (FP64, row-major `dim`, own BC codes) ---- */
+
+/* src/graphflood/sfgraph.c:27-113: steepest-descent receiver of every node
+ * that can give (BC 1, 3, 6, 7, 8, 9) among the neighbours that can receive
+ * (BC 1, 3, 4, 5, 6, 7, 9), slope (z - z_n) / distance in double, first
+ * strict maximum in neighbour order; donors listed per receiver in node
+ * order (8 or 4 slots per node); the Braun-Willett stack: a depth-first
+ * preorder from every root in node order, donors in listed order.  The
+ * restatement walks the tree with an explicit stack (same order). */
+void orc_compute_sfgraph(double *topo, size_t *Sreceivers, double *distToReceivers,
+                         size_t *Sdonors, uint8_t *NSdonors, size_t *Stack,
+                         const uint8_t *BCs, const size_t dim[2], double dx, int D8);
+/* src/graphflood/gf_flowacc.c:19-35 (and :41-57 with weights): drainage
+ * area in reverse stack order; roots add their donors' areas only. */
+void orc_compute_drainage_area_single_flow(double *output, const size_t *Sreceivers,
+                                           const size_t *Stack, const size_t dim[2],
+                                           double dx);
+void orc_compute_weighted_drainage_area_single_flow(double *output, const double *weights,
+                                                    const size_t *Sreceivers,
+                                                    const size_t *Stack,
+                                                    const size_t dim[2], double dx);
+
 #ifdef __cplusplus
 }
 #endif

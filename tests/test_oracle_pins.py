@@ -157,3 +157,47 @@ def test_port_edgelists_equal_reference(port, ref, idx, order):
     pos[sp] = np.arange(len(sp))
     later = pos[tp]
     assert np.all((later == -1) | (later > np.arange(len(sp))))
+
+
+def graphflood_cases():
+    """Row-major DEMs with graphflood boundary codes: 1 inside, 3 (can leave
+    the grid) on the border, 0 (nodata) where the DEM is NaN, a few 4/8/9."""
+    out = []
+    for name, dem, bc in DEMS:
+        topo = np.ascontiguousarray(np.asarray(dem, dtype=np.float64).T)  # rows x cols
+        if topo.size < 4:
+            continue
+        bcs = np.ones(topo.shape, np.uint8)
+        bcs[0, :] = bcs[-1, :] = bcs[:, 0] = bcs[:, -1] = 3
+        bcs[np.isnan(topo)] = 0
+        rng = np.random.default_rng(topo.size)
+        pick = rng.random(topo.shape)
+        bcs[(pick < 0.01) & (bcs == 1)] = 4
+        bcs[(pick > 0.995) & (bcs == 1)] = 8
+        bcs[(pick > 0.5) & (pick < 0.505) & (bcs == 1)] = 9
+        out.append((name, np.nan_to_num(topo, nan=0.0), bcs))
+    return out
+
+
+GF = graphflood_cases()
+
+
+@pytest.mark.parametrize("idx", range(len(GF)))
+@pytest.mark.parametrize("d8", [True, False])
+def test_port_sfgraph_equals_reference(port, ref, idx, d8):
+    """compute_sfgraph and the drainage areas (src/graphflood/sfgraph.c:27-113,
+    src/graphflood/gf_flowacc.c:19-57)."""
+    name, topo, bcs = GF[idx]
+    a = port.compute_sfgraph(topo, bcs, 30.0, d8)
+    b = ref.compute_sfgraph(topo, bcs, 30.0, d8)
+    rcv, dist, don, ndon, stack = a
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), name
+    assert np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4]), name
+    for v in range(len(ndon)):
+        assert np.array_equal(a[2][v, :ndon[v]], b[2][v, :ndon[v]]), (name, v)
+    w = np.random.default_rng(idx).uniform(0.5, 2.0, topo.shape)
+    for weights in (None, w):
+        assert np.array_equal(port.compute_drainage_area_single_flow(rcv, stack, topo.shape, 30.0,
+                                                                     weights),
+                              ref.compute_drainage_area_single_flow(rcv, stack, topo.shape, 30.0,
+                                                                    weights)), name
