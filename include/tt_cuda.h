@@ -35,6 +35,9 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -187,6 +190,26 @@ TT_CUDA_API void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
                                          ptrdiff_t node_count, ptrdiff_t edge_count);
 
 /* ------------------------------------------------------------------ */
+/* Graphflood single-flow graph (row-major dim = {rows, cols}, FP64)     */
+/* ------------------------------------------------------------------ */
+
+/** include/topotoolbox.h:2053 compute_sfgraph (src/graphflood/sfgraph.c:27-113).
+ *  Receivers, distances, donor lists and the Braun-Willett stack, all
+ *  bit-identical to the reference.  Donor slots past NSdonors are left as the
+ *  caller passed them, as in the reference. */
+TT_CUDA_API void tt_cuda_compute_sfgraph(double *topo, size_t *Sreceivers,
+                                         double *distToReceivers, size_t *Sdonors,
+                                         uint8_t *NSdonors, size_t *Stack, uint8_t *BCs,
+                                         size_t *dim, double dx, bool D8);
+/** include/topotoolbox.h:2122 compute_drainage_area_single_flow
+ *  (src/graphflood/gf_flowacc.c:19-35): cell area times the exact subtree
+ *  pixel count (the node itself left out at roots).  `Stack` is accepted and
+ *  not read: the count does not depend on the order. */
+TT_CUDA_API void tt_cuda_compute_drainage_area_single_flow(double *output, size_t *Sreceivers,
+                                                           size_t *Stack, size_t *dim,
+                                                           double dx);
+
+/* ------------------------------------------------------------------ */
 /* Adjoints (no counterpart in the reference)                           */
 /* ------------------------------------------------------------------ */
 
@@ -287,6 +310,13 @@ TT_CUDA_API tt_cuda_status tt_cuda_edgelist_degree_dev(
     uint8_t *indegree, uint8_t *outdegree, const ptrdiff_t *source,
     const ptrdiff_t *target, ptrdiff_t node_count, ptrdiff_t edge_count,
     void *stream);
+/** Device-pointer forms of the graphflood functions above. */
+TT_CUDA_API tt_cuda_status tt_cuda_compute_sfgraph_dev(
+    const double *topo, size_t *Sreceivers, double *distToReceivers, size_t *Sdonors,
+    uint8_t *NSdonors, size_t *Stack, const uint8_t *BCs, const size_t dim[2], double dx,
+    bool D8, void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_compute_drainage_area_single_flow_dev(
+    double *output, const size_t *Sreceivers, const size_t dim[2], double dx, void *stream);
 /** fillsinks on device pointers without allocating anything.  No
  *  counterpart in the reference.  For callers that cannot call cudaMalloc
  *  while they run -- a framework whose own memory pool already owns the

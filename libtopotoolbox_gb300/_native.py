@@ -47,6 +47,8 @@ SIGNATURES = {
     "tt_cuda_flow_accumulation_edgelist": (None, [P, P, P, P, P, I64, PD]),
     "tt_cuda_drainagebasins": (None, [P, P, P, I64, PD]),
     "tt_cuda_edgelist_degree": (None, [P, P, P, P, I64, I64]),
+    "tt_cuda_compute_sfgraph": (None, [P, P, P, P, P, P, P, P, C.c_double, C.c_bool]),
+    "tt_cuda_compute_drainage_area_single_flow": (None, [P, P, P, P, C.c_double]),
     # device-pointer forms
     "tt_cuda_fillsinks_dev": (ST, [P, P, P, PD, P]),
     "tt_cuda_fillsinks_noalloc_dev": (ST, [P, P, P, PD, P]),
@@ -65,6 +67,8 @@ SIGNATURES = {
     "tt_cuda_flow_accumulation_edgelist_dev": (ST, [P, P, P, P, P, I64, PD, P]),
     "tt_cuda_drainagebasins_dev": (ST, [P, P, P, I64, PD, P]),
     "tt_cuda_edgelist_degree_dev": (ST, [P, P, P, P, I64, I64, P]),
+    "tt_cuda_compute_sfgraph_dev": (ST, [P, P, P, P, P, P, P, P, C.c_double, C.c_bool, P]),
+    "tt_cuda_compute_drainage_area_single_flow_dev": (ST, [P, P, P, C.c_double, P]),
     # batched form
     "tt_cuda_batch_create": (ST, [C.c_int, PD, I64, C.POINTER(P)]),
     "tt_cuda_batch_info": (ST, [P, C.POINTER(I64)]),

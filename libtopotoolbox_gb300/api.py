@@ -261,6 +261,38 @@ def edgelist_degree(source, target, node_count):
     return indeg, outdeg
 
 
+def compute_sfgraph(topo, bcs, dx, d8=True):
+    """Graphflood single-flow graph (include/topotoolbox.h:2053,
+    src/graphflood/sfgraph.c:27-113) of a row-major (rows, cols) float64
+    grid: (receivers, distances, donors (N, 8|4), donor counts, stack)."""
+    topo = np.ascontiguousarray(topo, dtype=np.float64)
+    bcs = np.ascontiguousarray(bcs, dtype=np.uint8)
+    n, k = topo.size, (8 if d8 else 4)
+    rcv = np.empty(n, np.uint64)
+    dist = np.empty(n, np.float64)
+    don = np.zeros(n * k, np.uint64)
+    ndon = np.empty(n, np.uint8)
+    stack = np.empty(n, np.uint64)
+    dim = (N.C.c_size_t * 2)(*topo.shape)
+    N.lib().tt_cuda_compute_sfgraph(_ptr(topo), _ptr(rcv), _ptr(dist), _ptr(don), _ptr(ndon),
+                                    _ptr(stack), _ptr(bcs), N.C.cast(dim, N.C.c_void_p),
+                                    float(dx), bool(d8))
+    _after("compute_sfgraph")
+    return rcv, dist, don.reshape(n, k), ndon, stack
+
+
+def compute_drainage_area_single_flow(receivers, shape, dx, stack=None):
+    """Drainage area (include/topotoolbox.h:2122, src/graphflood/gf_flowacc.c:19-35)."""
+    rcv = np.ascontiguousarray(receivers, dtype=np.uint64)
+    out = np.empty(int(np.prod(shape)), np.float64)
+    dim = (N.C.c_size_t * 2)(*shape)
+    st = np.ascontiguousarray(stack, dtype=np.uint64) if stack is not None else None
+    N.lib().tt_cuda_compute_drainage_area_single_flow(_ptr(out), _ptr(rcv), _ptr(st),
+                                                      N.C.cast(dim, N.C.c_void_p), float(dx))
+    _after("compute_drainage_area_single_flow")
+    return out.reshape(shape)
+
+
 def d8_pipeline(dem, bc, weights=None):
     """The reference call sequence fill -> flats -> costs -> gwdt -> carve ->
     accumulation in one call (host buffers).  Returns a dict."""

@@ -542,6 +542,20 @@ tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
   return TT_CUDA_SUCCESS;
 }
 
+int scan_blocks_for(int64_t n) {
+  return (int)((std::max<int64_t>(n, 1) + kScanBlock - 1) / kScanBlock);
+}
+
+tt_cuda_status scan_exclusive_dev(const int *in, int64_t n, int *out, int *cnt, int *off,
+                                  cudaStream_t st) {
+  const int nb = scan_blocks_for(n);
+  TT_LAUNCH(mark_count_kernel, nb, kScanThreads, 0, st, in, n, cnt);
+  TT_LAUNCH(scan_blocks_kernel, 1, kScanThreads, 0, st, cnt, off, nb);
+  TT_LAUNCH(mark_scan_kernel, nb, kScanThreads, 0, st, in, n, off, out);
+  TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
 tt_cuda_status degree_dev(uint8_t *indegree, uint8_t *outdegree, const ptrdiff_t *source,
                           const ptrdiff_t *target, int64_t N, int64_t E, cudaStream_t st) {
   Workspace &ws = workspace();

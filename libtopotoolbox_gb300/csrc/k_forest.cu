@@ -91,6 +91,7 @@ struct UpArgs {
   int *elist;       // per exit id: the exit's pixel
   int *ecount;
   float *acc_out;
+  int *count_out;  // unit weights: the exact count as int (or nullptr)
   int *h_out;
   int *hmax;
   int *err;
@@ -370,7 +371,9 @@ __global__ void __launch_bounds__(kUpThreads, 8) forest_fin_kernel(UpArgs a) {
       const int ii = e % kTile, jj = e / kTile;
       if (ii >= ilim || jj >= jlim) continue;
       const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
-      if (a.want_acc) {
+      if (a.want_acc && a.count_out) {
+        a.count_out[gp] = (int)t.acc[e];
+      } else if (a.want_acc) {
         const float v = __ll2float_rn(t.acc[e]);
         a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
       }
@@ -840,7 +843,8 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
 // Runs both tile passes and the coarse walk.
 tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
                       const GridDims &g, unsigned order, bool want_acc,
-                      bool want_h, float *acc_out, UpWork &w, cudaStream_t st) {
+                      bool want_h, float *acc_out, UpWork &w, cudaStream_t st,
+                      int *count_out = nullptr) {
   const int T = g.tiles();
   TT_CHECK(cudaMemsetAsync(w.counters, 0, 256, st));
   UpArgs a{};
@@ -865,6 +869,7 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.elist = w.elist;
   a.ecount = w.counters + 0;
   a.acc_out = acc_out;
+  a.count_out = count_out;
   a.h_out = w.h;
   a.hmax = w.counters + 3;
   a.err = w.counters + 4;
@@ -909,6 +914,22 @@ tt_cuda_status up_status(UpWork &w, cudaStream_t st, int *host6) {
 }
 
 }  // namespace
+
+// Exact pixel counts of every subtree (unit weights), as int: the number of
+// pixels whose flow path passes through each pixel, itself included.
+tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cudaStream_t st) {
+  UpWork w;
+  {
+    tt_cuda_status s = up_alloc(g, true, false, w);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  {
+    tt_cuda_status s = up_run(dir, nullptr, 0, g, 0, true, false, nullptr, w, st, count);
+    if (s != TT_CUDA_SUCCESS) return s;
+  }
+  int h6[6];
+  return up_status(w, st, h6);
+}
 
 tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,

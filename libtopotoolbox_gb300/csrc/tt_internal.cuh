@@ -169,6 +169,8 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
 tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,
                               cudaStream_t st);
+// Exact subtree pixel counts (int) of the forest of `dir`.
+tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cudaStream_t st);
 tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
                                        const float *grad_acc,
                                        const GridDims &g, cudaStream_t st);
@@ -196,6 +198,19 @@ tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
                                   cudaStream_t st);
 tt_cuda_status degree_dev(uint8_t *indegree, uint8_t *outdegree, const ptrdiff_t *source,
                           const ptrdiff_t *target, int64_t N, int64_t E, cudaStream_t st);
+
+// Exclusive scan of n ints: out[k] = sum of in[0..k); the total lands in
+// off[scan_blocks_for(n)].  cnt and off hold scan_blocks_for(n) + 1 ints.
+int scan_blocks_for(int64_t n);
+tt_cuda_status scan_exclusive_dev(const int *in, int64_t n, int *out, int *cnt, int *off,
+                                  cudaStream_t st);
+
+// Graphflood single-flow graph (row-major dim = {rows, cols}).
+tt_cuda_status sfgraph_dev(const double *topo, size_t *rcv, double *dist, size_t *donors,
+                           uint8_t *ndonors, size_t *stack, const uint8_t *bcs, int64_t rows,
+                           int64_t cols, double dx, bool d8, cudaStream_t st);
+tt_cuda_status sf_drainage_area_dev(double *area, const size_t *rcv, int64_t rows,
+                                    int64_t cols, double dx, cudaStream_t st);
 
 // Sun vector of src/hillshade.c:104-106, evaluated in double and rounded.
 void sun_vector(float azimuth, float altitude, float *sx, float *sy, float *sz);

@@ -412,6 +412,41 @@ tt_cuda_status tt_cuda_edgelist_degree_dev(uint8_t *indegree, uint8_t *outdegree
   });
 }
 
+// Graphflood single-flow graph (device pointers; dim = {rows, cols}).
+static bool gf_dim_ok(const size_t dim[2], ptrdiff_t pd[2]) {
+  if (!dim) return false;
+  pd[0] = (ptrdiff_t)dim[1];
+  pd[1] = (ptrdiff_t)dim[0];
+  return dim[0] > 0 && dim[1] > 0 && dim[0] < (1ULL << 31) && dim[1] < (1ULL << 31);
+}
+
+tt_cuda_status tt_cuda_compute_sfgraph_dev(const double *topo, size_t *Sreceivers,
+                                           double *distToReceivers, size_t *Sdonors,
+                                           uint8_t *NSdonors, size_t *Stack, const uint8_t *BCs,
+                                           const size_t dim[2], double dx, bool D8,
+                                           void *stream) {
+  ptrdiff_t pd[2] = {0, 0};
+  if (!topo || !Sreceivers || !distToReceivers || !Sdonors || !NSdonors || !Stack || !BCs ||
+      !gf_dim_ok(dim, pd))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(pd, stream, [&](const GridDims &g, cudaStream_t st) {
+    return sfgraph_dev(topo, Sreceivers, distToReceivers, Sdonors, NSdonors, Stack, BCs, g.n,
+                       g.m, dx, D8, st);
+  });
+}
+
+tt_cuda_status tt_cuda_compute_drainage_area_single_flow_dev(double *output,
+                                                             const size_t *Sreceivers,
+                                                             const size_t dim[2], double dx,
+                                                             void *stream) {
+  ptrdiff_t pd[2] = {0, 0};
+  if (!output || !Sreceivers || !gf_dim_ok(dim, pd))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  return dev_call(pd, stream, [&](const GridDims &g, cudaStream_t st) {
+    return sf_drainage_area_dev(output, Sreceivers, g.n, g.m, dx, st);
+  });
+}
+
 tt_cuda_status tt_cuda_flow_accumulation_backward_dev(float *grad_weights,
                                                       const uint8_t *direction,
                                                       const float *grad_acc,
@@ -757,6 +792,44 @@ void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree, ptrdiff_t *s
               return degree_dev((uint8_t *)a[0].dev, (uint8_t *)a[1].dev,
                                 (const ptrdiff_t *)a[2].dev, (const ptrdiff_t *)a[3].dev,
                                 g.cells(), edge_count, st);
+            });
+}
+
+void tt_cuda_compute_sfgraph(double *topo, size_t *Sreceivers, double *distToReceivers,
+                             size_t *Sdonors, uint8_t *NSdonors, size_t *Stack, uint8_t *BCs,
+                             size_t *dim, double dx, bool D8) {
+  ptrdiff_t pd[2] = {0, 0};
+  if (!gf_dim_ok(dim, pd)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  const size_t N = (size_t)(pd[0] * pd[1]), K = D8 ? 8 : 4;
+  // Sdonors goes both ways: slots past each count keep the caller's bytes.
+  host_call(pd,
+            {{topo, N * 8, true, false}, {Sreceivers, N * 8, false, true},
+             {distToReceivers, N * 8, false, true}, {Sdonors, N * K * 8, true, true},
+             {NSdonors, N, false, true}, {Stack, N * 8, false, true}, {BCs, N, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return sfgraph_dev((const double *)a[0].dev, (size_t *)a[1].dev,
+                                 (double *)a[2].dev, (size_t *)a[3].dev, (uint8_t *)a[4].dev,
+                                 (size_t *)a[5].dev, (const uint8_t *)a[6].dev, g.n, g.m, dx,
+                                 D8, st);
+            });
+}
+
+void tt_cuda_compute_drainage_area_single_flow(double *output, size_t *Sreceivers,
+                                               size_t *Stack, size_t *dim, double dx) {
+  (void)Stack;
+  ptrdiff_t pd[2] = {0, 0};
+  if (!gf_dim_ok(dim, pd)) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  const size_t N = (size_t)(pd[0] * pd[1]);
+  host_call(pd, {{output, N * 8, false, true}, {Sreceivers, N * 8, true, false}},
+            [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
+              return sf_drainage_area_dev((double *)a[0].dev, (const size_t *)a[1].dev, g.n,
+                                          g.m, dx, st);
             });
 }
 
