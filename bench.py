@@ -333,6 +333,74 @@ def edges_leg(dev, node, direction, reps=5):
             "speedup_vs_cpu": {k: cpu[k] / ms[k] for k in ms}}
 
 
+def graphflood_leg(dem, cs, reps=5):
+    """Graphflood's single-flow graph and drainage area on the workload DEM
+    (float64, row-major, border BC 3) through the device API, beside the
+    oracle's C restatement of the reference on one host core."""
+    import ctypes as C
+
+    import torch
+
+    from libtopotoolbox_gb300 import _native as N
+
+    topo = np.ascontiguousarray(np.asarray(dem, np.float64).T)
+    bcs = np.ones(topo.shape, np.uint8)
+    bcs[0, :] = bcs[-1, :] = bcs[:, 0] = bcs[:, -1] = 3
+    n = topo.size
+    dv = torch.device("cuda", torch.cuda.current_device())
+    d_topo = torch.from_numpy(topo).to(dv)
+    d_bcs = torch.from_numpy(bcs).to(dv)
+    rcv = torch.empty(n, dtype=torch.int64, device=dv)
+    stack = torch.empty(n, dtype=torch.int64, device=dv)
+    dist = torch.empty(n, dtype=torch.float64, device=dv)
+    don = torch.empty(n * 8, dtype=torch.int64, device=dv)
+    ndon = torch.empty(n, dtype=torch.uint8, device=dv)
+    area = torch.empty(n, dtype=torch.float64, device=dv)
+    dim = (C.c_size_t * 2)(*topo.shape)
+    lib = N.lib()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def graph():
+        N.check(lib.tt_cuda_compute_sfgraph_dev(p(d_topo), p(rcv), p(dist), p(don), p(ndon),
+                                                p(stack), p(d_bcs), C.cast(dim, C.c_void_p),
+                                                float(cs), True, st), "compute_sfgraph_dev")
+
+    def drain():
+        N.check(lib.tt_cuda_compute_drainage_area_single_flow_dev(
+            p(area), p(rcv), C.cast(dim, C.c_void_p), float(cs), st),
+            "compute_drainage_area_single_flow_dev")
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    ms = {"compute_sfgraph": timed(graph), "compute_drainage_area_single_flow": timed(drain)}
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    orc = pyoracle.Oracle("port")
+    t0 = time.perf_counter()
+    r = orc.compute_sfgraph(topo, bcs, float(cs), True)
+    cpu = {"compute_sfgraph": (time.perf_counter() - t0) * 1e3}
+    t0 = time.perf_counter()
+    orc.compute_drainage_area_single_flow(r[0], r[4], topo.shape, float(cs))
+    cpu["compute_drainage_area_single_flow"] = (time.perf_counter() - t0) * 1e3
+    return {"workload": f"graphflood single-flow graph, D8, {topo.shape[0]}x{topo.shape[1]} "
+                        f"float64 workload DEM",
+            "gpu_ms": ms, "gcells_s": {k: n / (v * 1e-3) / 1e9 for k, v in ms.items()},
+            "cpu_port_ms_1core": cpu, "speedup_vs_cpu": {k: cpu[k] / ms[k] for k in ms}}
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -398,6 +466,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-edges", action="store_true")
+    ap.add_argument("--no-graphflood", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -579,6 +648,8 @@ def main():
         line["batched"] = batch_leg(dev)
     if not args.no_edges:
         line["edges"] = edges_leg(dev, o["node"], o["direction"])
+    if not args.no_graphflood:
+        line["graphflood"] = graphflood_leg(dem, cs)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
     print(json.dumps(line), flush=True)
