@@ -401,6 +401,49 @@ def graphflood_leg(dem, cs, reps=5):
             "cpu_port_ms_1core": cpu, "speedup_vs_cpu": {k: cpu[k] / ms[k] for k in ms}}
 
 
+def io_leg(dem, reps=5):
+    """The I/O step before the path: the workload DEM as a Fortran-order
+    .npy streamed into device memory by the native loader (two pinned
+    buffers, reads overlapping copies), against numpy.load + a pageable
+    torch upload.  The file sits in the page cache (it was just written), so
+    this measures the host-memory-to-device path, not the disk."""
+    import tempfile
+
+    import torch
+
+    from libtopotoolbox_gb300 import rasterio
+
+    d = tempfile.mkdtemp(prefix="tt_io_")
+    path = os.path.join(d, "dem.npy")
+    np.save(path, np.asfortranarray(dem))
+    nbytes = dem.size * 4
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3
+
+    native = timed(lambda: rasterio.read_npy(path))
+    base = timed(lambda: torch.from_numpy(np.ascontiguousarray(np.load(path).T)).cuda())
+    t = rasterio.read_npy(path)
+    out = os.path.join(d, "back.npy")
+    wr = timed(lambda: rasterio.write_npy(out, t))
+    ok = bool(np.array_equal(np.load(out), dem))
+    os.remove(path)
+    os.remove(out)
+    os.rmdir(d)
+    return {"workload": f"{dem.shape[0]}x{dem.shape[1]} float32 .npy ({nbytes} bytes), page cache",
+            "read_ms": native, "read_gbs": nbytes / native / 1e6,
+            "numpy_load_upload_ms": base, "write_ms": wr, "write_gbs": nbytes / wr / 1e6,
+            "roundtrip_exact": ok}
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -467,6 +510,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-edges", action="store_true")
     ap.add_argument("--no-graphflood", action="store_true")
+    ap.add_argument("--no-io", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -650,6 +694,8 @@ def main():
         line["edges"] = edges_leg(dev, o["node"], o["direction"])
     if not args.no_graphflood:
         line["graphflood"] = graphflood_leg(dem, cs)
+    if not args.no_io:
+        line["io"] = io_leg(dem)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
     print(json.dumps(line), flush=True)

@@ -57,7 +57,8 @@ typedef enum {
   TT_CUDA_ERR_CUDA = 3,             /**< a CUDA runtime call failed */
   TT_CUDA_ERR_NOT_CONVERGED = 4,    /**< an iteration cap was reached */
   TT_CUDA_ERR_CYCLE = 5,            /**< the direction grid contains a cycle */
-  TT_CUDA_ERR_NO_DEVICE = 6         /**< no CUDA device is visible */
+  TT_CUDA_ERR_NO_DEVICE = 6,        /**< no CUDA device is visible */
+  TT_CUDA_ERR_IO = 7                /**< a file could not be opened, read or written */
 } tt_cuda_status;
 
 /* ------------------------------------------------------------------ */
@@ -317,6 +318,17 @@ TT_CUDA_API tt_cuda_status tt_cuda_compute_sfgraph_dev(
     bool D8, void *stream);
 TT_CUDA_API tt_cuda_status tt_cuda_compute_drainage_area_single_flow_dev(
     double *output, const size_t *Sreceivers, const size_t dim[2], double dx, void *stream);
+/** Raster I/O before and after the path (no counterpart in the reference,
+ *  whose callers read DEMs with GDAL): `bytes` bytes of the file at `path`
+ *  from byte `offset` into device memory at `dst`, or from `src` into the
+ *  file at byte `offset` (the file is created if missing, not truncated), in
+ *  chunks staged through two pinned host buffers so that disk transfers and
+ *  host-device copies overlap.  Returns when the data has arrived.
+ *  TT_CUDA_ERR_IO if the file cannot be opened or is short. */
+TT_CUDA_API tt_cuda_status tt_cuda_read_file_dev(void *dst, const char *path, int64_t offset,
+                                                 int64_t bytes, void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_write_file_dev(const char *path, int64_t offset,
+                                                  const void *src, int64_t bytes, void *stream);
 /** fillsinks on device pointers without allocating anything.  No
  *  counterpart in the reference.  For callers that cannot call cudaMalloc
  *  while they run -- a framework whose own memory pool already owns the

@@ -69,6 +69,8 @@ SIGNATURES = {
     "tt_cuda_edgelist_degree_dev": (ST, [P, P, P, P, I64, I64, P]),
     "tt_cuda_compute_sfgraph_dev": (ST, [P, P, P, P, P, P, P, P, C.c_double, C.c_bool, P]),
     "tt_cuda_compute_drainage_area_single_flow_dev": (ST, [P, P, P, C.c_double, P]),
+    "tt_cuda_read_file_dev": (ST, [P, C.c_char_p, I64, I64, P]),
+    "tt_cuda_write_file_dev": (ST, [C.c_char_p, I64, P, I64, P]),
     # batched form
     "tt_cuda_batch_create": (ST, [C.c_int, PD, I64, C.POINTER(P)]),
     "tt_cuda_batch_info": (ST, [P, C.POINTER(I64)]),

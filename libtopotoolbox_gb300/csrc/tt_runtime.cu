@@ -230,6 +230,7 @@ const char *tt_cuda_status_string(tt_cuda_status s) {
     case TT_CUDA_ERR_NOT_CONVERGED: return "iteration cap reached";
     case TT_CUDA_ERR_CYCLE: return "direction grid contains a cycle";
     case TT_CUDA_ERR_NO_DEVICE: return "no CUDA device";
+    case TT_CUDA_ERR_IO: return "file input/output failed";
   }
   return "unknown status";
 }
