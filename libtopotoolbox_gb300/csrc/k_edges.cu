@@ -394,12 +394,6 @@ __global__ void degree_narrow_kernel(const int *__restrict__ indeg, const int *_
   }
 }
 
-#define TT_TRY_STATUS(expr)                 \
-  do {                                      \
-    tt_cuda_status _s = (expr);             \
-    if (_s != TT_CUDA_SUCCESS) return _s;   \
-  } while (0)
-
 int grid_for(int64_t n) {
   const int64_t b = (n + 255) / 256;
   const int64_t cap = (int64_t)sm_count() * 32;

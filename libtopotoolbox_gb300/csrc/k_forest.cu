@@ -931,56 +931,38 @@ tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cuda
   return up_status(w, st, h6);
 }
 
-tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
-                              const float *weights, const GridDims &g,
-                              cudaStream_t st) {
-  UpWork w;
-  {
-    tt_cuda_status s = up_alloc(g, true, false, w);
-    if (s != TT_CUDA_SUCCESS) return s;
+namespace {
+
+// Fixed-point shift for weighted sums: the largest |w| times the pixel count
+// must stay below 2^62.  Unit weights (nullptr) need none.
+tt_cuda_status weight_shift(const float *weights, const GridDims &g, UpWork &w,
+                            cudaStream_t st, int *wshift) {
+  *wshift = 0;
+  if (!weights) return TT_CUDA_SUCCESS;
+  unsigned *mx = (unsigned *)(w.counters + 5);
+  TT_CHECK(cudaMemsetAsync(mx, 0, 4, st));
+  TT_LAUNCH(maxabs_kernel, list_grid(g.cells()), 256, 0, st, weights, g.cells(), mx);
+  unsigned *h = (unsigned *)pinned_scratch();
+  if (!h) return TT_CUDA_ERR_ALLOC;
+  TT_CHECK(cudaMemcpyAsync(h, mx, 4, cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaStreamSynchronize(st));
+  unsigned bits = *h;
+  float mxv;
+  std::memcpy(&mxv, &bits, 4);
+  if (bits >= 0x7f800000u) mxv = 0.0f;  // non-finite weights are flagged per pixel
+  if (mxv > 0.0f) {
+    double bound = (double)mxv * (double)g.cells();
+    int e = (int)std::ceil(std::log2(bound));
+    *wshift = 62 - e;
   }
-  int wshift = 0;
-  if (weights) {
-    unsigned *mx = (unsigned *)(w.counters + 5);
-    TT_CHECK(cudaMemsetAsync(mx, 0, 4, st));
-    TT_LAUNCH(maxabs_kernel, list_grid(g.cells()), 256, 0, st, weights, g.cells(), mx);
-    unsigned *h = (unsigned *)pinned_scratch();
-    if (!h) return TT_CUDA_ERR_ALLOC;
-    TT_CHECK(cudaMemcpyAsync(h, mx, 4, cudaMemcpyDeviceToHost, st));
-    TT_CHECK(cudaStreamSynchronize(st));
-    unsigned bits = *h;
-    float mxv;
-    std::memcpy(&mxv, &bits, 4);
-    if (bits >= 0x7f800000u) mxv = 0.0f;  // non-finite weights are flagged per pixel
-    if (mxv > 0.0f) {
-      double bound = (double)mxv * (double)g.cells();
-      int e = (int)std::ceil(std::log2(bound));
-      wshift = 62 - e;
-    }
-  }
-  {
-    tt_cuda_status s = up_run(dir, weights, wshift, g, 0, true, false, acc, w, st);
-    if (s != TT_CUDA_SUCCESS) return s;
-  }
-  int h6[6];
-  return up_status(w, st, h6);
+  return TT_CUDA_SUCCESS;
 }
 
-tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
-                              const GridDims &g, unsigned order,
-                              cudaStream_t st) {
-  UpWork w;
-  {
-    tt_cuda_status s = up_alloc(g, false, true, w);
-    if (s != TT_CUDA_SUCCESS) return s;
-  }
-  {
-    tt_cuda_status s = up_run(dir, nullptr, 0, g, order, false, true, nullptr, w, st);
-    if (s != TT_CUDA_SUCCESS) return s;
-  }
-  int h6[6];
-  tt_cuda_status s = up_status(w, st, h6);
-  if (s == TT_CUDA_ERR_CYCLE) return s;
+// Node order from the subtree heights of a finished up_run: pixels sorted
+// by height (a donor's height is below its receiver's), stable within a
+// height by a counting sort.
+tt_cuda_status node_scatter(ptrdiff_t *node, UpWork &w, const int h6[6], const GridDims &g,
+                            cudaStream_t st) {
   const int H = h6[3] + 1;
   // hist, off and cursor reuse the coarse arrays (no longer needed).
   int *hist = w.xmap, *off = w.xsteps, *cursor = reinterpret_cast<int *>(w.cell);
@@ -992,6 +974,51 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
   TT_LAUNCH(scan_kernel, 1, 1024, 0, st, hist, off, H);
   TT_LAUNCH(node_scatter_kernel, eg, 256, 0, st, w.h, g.cells(), off, cursor, node);
   TT_CHECK(cudaGetLastError());
+  return TT_CUDA_SUCCESS;
+}
+
+}  // namespace
+
+tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
+                              const float *weights, const GridDims &g,
+                              cudaStream_t st) {
+  UpWork w;
+  TT_TRY_STATUS(up_alloc(g, true, false, w));
+  int wshift = 0;
+  TT_TRY_STATUS(weight_shift(weights, g, w, st, &wshift));
+  TT_TRY_STATUS(up_run(dir, weights, wshift, g, 0, true, false, acc, w, st));
+  int h6[6];
+  return up_status(w, st, h6);
+}
+
+tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
+                              const GridDims &g, unsigned order,
+                              cudaStream_t st) {
+  UpWork w;
+  TT_TRY_STATUS(up_alloc(g, false, true, w));
+  TT_TRY_STATUS(up_run(dir, nullptr, 0, g, order, false, true, nullptr, w, st));
+  int h6[6];
+  tt_cuda_status s = up_status(w, st, h6);
+  if (s == TT_CUDA_ERR_CYCLE) return s;
+  TT_TRY_STATUS(node_scatter(node, w, h6, g, st));
+  return s;
+}
+
+// Column-major node order and flow accumulation from one contraction of the
+// receiver forest: the tile and coarse passes carry the subtree sums and the
+// subtree heights together, so the pipeline walks the forest once for both.
+tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *dir,
+                                  const float *weights, const GridDims &g,
+                                  cudaStream_t st) {
+  UpWork w;
+  TT_TRY_STATUS(up_alloc(g, true, true, w));
+  int wshift = 0;
+  TT_TRY_STATUS(weight_shift(weights, g, w, st, &wshift));
+  TT_TRY_STATUS(up_run(dir, weights, wshift, g, 0, true, true, acc, w, st));
+  int h6[6];
+  tt_cuda_status s = up_status(w, st, h6);
+  if (s == TT_CUDA_ERR_CYCLE) return s;
+  TT_TRY_STATUS(node_scatter(node, w, h6, g, st));
   return s;
 }
 

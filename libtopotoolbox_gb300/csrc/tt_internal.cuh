@@ -78,6 +78,13 @@ bool cuda_ok(cudaError_t e, const char *what);
     if (!::tt::cuda_ok((expr), #expr)) return TT_CUDA_ERR_CUDA;            \
   } while (0)
 
+// Returns any status other than success to the caller.
+#define TT_TRY_STATUS(expr)                 \
+  do {                                      \
+    tt_cuda_status _s = (expr);             \
+    if (_s != TT_CUDA_SUCCESS) return _s;   \
+  } while (0)
+
 // A grow-only bump allocator over one device allocation per device.  Every
 // public call resets it on entry and carves its scratch from it; calls are
 // serialised per device (see DeviceLock).
@@ -170,6 +177,9 @@ tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,
                               cudaStream_t st);
 // Exact subtree pixel counts (int) of the forest of `dir`.
+tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *dir,
+                                  const float *weights, const GridDims &g,
+                                  cudaStream_t st);
 tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cudaStream_t st);
 tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
                                        const float *grad_acc,

@@ -28,6 +28,10 @@ struct DeviceState {
   Workspace io;
   void *pinned = nullptr;
   int sms = 0;
+  // side stream and events for device-to-host copies that overlap the
+  // later stages of a host-pointer pipeline call
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ready[8] = {};
 };
 
 DeviceState g_dev[kMaxDevices];
@@ -120,6 +124,25 @@ void *pinned_scratch() {
     }
   }
   return d.pinned;
+}
+
+// The per-device copy stream and its events, created on first use.
+static bool copy_lane(cudaStream_t *cs, cudaEvent_t **ev) {
+  DeviceState &d = g_dev[current_device()];
+  if (!d.copy && cudaStreamCreateWithFlags(&d.copy, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    d.copy = nullptr;
+    return false;
+  }
+  for (auto &e : d.ready)
+    if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      e = nullptr;
+      return false;
+    }
+  *cs = d.copy;
+  *ev = d.ready;
+  return true;
 }
 
 int sm_count() {
@@ -501,22 +524,91 @@ tt_cuda_status tt_cuda_hillshade_backward_dev(float *grad_dem, const float *dem,
 
 // The pipeline body shared by the device and host forms.  Missing
 // intermediates are carved from the io workspace by the caller.
+// True for page-locked (pinned or registered) host memory.
+static bool host_pinned(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// Device-to-host copies of a host-pointer pipeline's outputs.  A copy into
+// page-locked memory is issued as soon as the stage that writes its array
+// has been enqueued: it runs on a side stream after an event on the compute
+// stream, so it overlaps the later stages.  No later stage writes an array
+// once its copy is issued.  A copy into pageable memory blocks the calling
+// thread until it is done, so those are deferred to the end of the call and
+// issued on the compute stream, after every kernel has been enqueued.
+struct EarlyOut {
+  void *filled = nullptr, *flats = nullptr, *dist = nullptr;
+  void *node = nullptr, *direction = nullptr, *acc = nullptr;
+  cudaStream_t cs = nullptr;
+  cudaEvent_t *ev = nullptr;
+  int used = 0;
+  struct Late {
+    void *host;
+    const void *dev;
+    size_t bytes;
+  } late[6];
+  int nlate = 0;
+
+  tt_cuda_status send(void *host, const void *dev, size_t bytes, cudaStream_t st) {
+    if (!host) return TT_CUDA_SUCCESS;
+    if (!cs || !host_pinned(host)) {
+      late[nlate++] = {host, dev, bytes};
+      return TT_CUDA_SUCCESS;
+    }
+    TT_CHECK(cudaEventRecord(ev[used], st));
+    TT_CHECK(cudaStreamWaitEvent(cs, ev[used], 0));
+    used++;
+    TT_CHECK(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, cs));
+    return TT_CUDA_SUCCESS;
+  }
+  // the compute stream waits for every early copy, so a sync on it covers
+  // them; the deferred copies follow on the compute stream
+  tt_cuda_status join(cudaStream_t st) {
+    if (cs && used) {
+      TT_CHECK(cudaEventRecord(ev[used], cs));
+      TT_CHECK(cudaStreamWaitEvent(st, ev[used], 0));
+    }
+    for (int k = 0; k < nlate; k++) TT_TRY(d2h(late[k].host, late[k].dev, late[k].bytes, st));
+    return TT_CUDA_SUCCESS;
+  }
+};
+
 static tt_cuda_status pipeline_body(float *filled, int32_t *flats, float *dist,
                                     ptrdiff_t *node, uint8_t *direction,
                                     float *acc, float *hill, const float *dem,
                                     const uint8_t *bc, const float *weights,
                                     float az, float alt, float cs,
                                     float *costs, ptrdiff_t *conncomps,
-                                    const GridDims &g, cudaStream_t st) {
+                                    const GridDims &g, cudaStream_t st,
+                                    EarlyOut *out = nullptr) {
   tt_cuda_status soft = TT_CUDA_SUCCESS;
+  const size_t n = (size_t)g.m * (size_t)g.n;
   TT_TRY_SOFT(fill_dev(filled, dem, bc, g, st), soft);
+  if (out) TT_TRY(out->send(out->filled, filled, n * 4, st));
   TT_TRY(identifyflats_dev(flats, filled, g, nullptr, st));
+  if (out) TT_TRY(out->send(out->flats, flats, n * 4, st));
   TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));
   TT_TRY_SOFT(gwdt_dev(dist, nullptr, costs, flats, g, st), soft);
+  if (out) TT_TRY(out->send(out->dist, dist, n * 4, st));
   TT_TRY(directions_dev(direction, filled, dist, flats, g, 0, st));
-  if (node) TT_TRY_SOFT(node_order_dev(node, direction, g, 0, st), soft);
-  if (acc) TT_TRY_SOFT(accumulate_dev(acc, direction, weights, g, st), soft);
+  if (out) TT_TRY(out->send(out->direction, direction, n, st));
+  if (node && acc) {  // one forest contraction for both
+    TT_TRY_SOFT(node_order_acc_dev(node, acc, direction, weights, g, st), soft);
+    if (out) TT_TRY(out->send(out->acc, acc, n * 4, st));
+    if (out) TT_TRY(out->send(out->node, node, n * 8, st));
+  } else {
+    if (node) TT_TRY_SOFT(node_order_dev(node, direction, g, 0, st), soft);
+    if (out && node) TT_TRY(out->send(out->node, node, n * 8, st));
+    if (acc) TT_TRY_SOFT(accumulate_dev(acc, direction, weights, g, st), soft);
+    if (out && acc) TT_TRY(out->send(out->acc, acc, n * 4, st));
+  }
   if (hill) TT_TRY(hillshade_dev(hill, dem, az, alt, cs, g, st));
+  if (out) TT_TRY(out->join(st));
   return soft;
 }
 
@@ -922,22 +1014,37 @@ void tt_cuda_d8_pipeline(float *filled, int32_t *flats, float *dist,
   host_call(dims,
             {{dem, N * 4, true, false}, {bc, N, true, false},
              {weights, weights ? N * 4 : 0, weights != nullptr, false},
-             {filled, N * 4, false, filled != nullptr},
-             {flats, N * 4, false, flats != nullptr},
-             {dist, N * 4, false, dist != nullptr},
-             {node, node ? N * 8 : 0, false, node != nullptr},
-             {direction, N, false, direction != nullptr},
-             {acc, acc ? N * 4 : 0, false, acc != nullptr},
+             // outputs: copied back by EarlyOut as their stages finish
+             {nullptr, N * 4, false, false},
+             {nullptr, N * 4, false, false},
+             {nullptr, N * 4, false, false},
+             {nullptr, node ? N * 8 : 0, false, false},
+             {nullptr, N, false, false},
+             {nullptr, acc ? N * 4 : 0, false, false},
              {nullptr, N * 4, false, false},   // costs
              {nullptr, N * 8, false, false}},  // conncomps
             [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
-              return pipeline_body((float *)a[3].dev, (int32_t *)a[4].dev,
-                                   (float *)a[5].dev, node ? (ptrdiff_t *)a[6].dev : nullptr,
-                                   (uint8_t *)a[7].dev, acc ? (float *)a[8].dev : nullptr,
-                                   nullptr, (const float *)a[0].dev,
-                                   (const uint8_t *)a[1].dev,
-                                   weights ? (const float *)a[2].dev : nullptr, 0.f, 0.f,
-                                   1.f, (float *)a[9].dev, (ptrdiff_t *)a[10].dev, g, st);
+              EarlyOut out;
+              out.filled = filled;
+              out.flats = flats;
+              out.dist = dist;
+              out.node = node;
+              out.direction = direction;
+              out.acc = acc;
+              if (!copy_lane(&out.cs, &out.ev)) out.cs = nullptr;
+              tt_cuda_status s = pipeline_body(
+                  (float *)a[3].dev, (int32_t *)a[4].dev, (float *)a[5].dev,
+                  node ? (ptrdiff_t *)a[6].dev : nullptr, (uint8_t *)a[7].dev,
+                  acc ? (float *)a[8].dev : nullptr, nullptr, (const float *)a[0].dev,
+                  (const uint8_t *)a[1].dev, weights ? (const float *)a[2].dev : nullptr,
+                  0.f, 0.f, 1.f, (float *)a[9].dev, (ptrdiff_t *)a[10].dev, g, st, &out);
+              // copies already issued end before the call returns, even when
+              // a later stage failed
+              if (out.cs && out.used && cudaStreamSynchronize(out.cs) != cudaSuccess) {
+                cudaGetLastError();
+                if (s == TT_CUDA_SUCCESS) s = TT_CUDA_ERR_CUDA;
+              }
+              return s;
             });
 }
 
