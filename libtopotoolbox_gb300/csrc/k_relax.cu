@@ -119,41 +119,6 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
   return y;
 }
 
-// The update at pixel (c, r) from all eight neighbours.  Neighbour values may
-// be old or new: every value is an upper bound of the fixpoint, so any mix
-// gives a valid (and never higher) result.
-template <int KIND>
-__device__ __forceinline__ float relax8(const WarpTile &t, int c, int r, float cur) {
-  if (KIND == FILL) {
-    const float a0 = fminf(t.s[c - 1][r - 1], t.s[c - 1][r]);
-    const float a1 = fminf(t.s[c - 1][r + 1], t.s[c][r - 1]);
-    const float a2 = fminf(t.s[c][r + 1], t.s[c + 1][r - 1]);
-    const float a3 = fminf(t.s[c + 1][r], t.s[c + 1][r + 1]);
-    const float lo = fminf(cur, fminf(fminf(a0, a1), fminf(a2, a3)));
-    const float z = t.a[c][r];
-    return (lo > z) ? lo : z;
-  } else {
-    // Non-flat and off-grid pixels are staged as state +INF and cost NaN:
-    // every path through them evaluates to +INF or NaN, which never wins
-    // the minimum, and a non-flat centre (cost NaN) keeps its value.
-    const float cs = t.a[c][r];
-    float best = cur;
-#pragma unroll
-    for (int dc = -1; dc <= 1; dc++) {
-#pragma unroll
-      for (int dr = -1; dr <= 1; dr++) {
-        if (!(dc || dr)) continue;
-        const float sum = __fadd_rn(cs, t.a[c + dc][r + dr]);
-        // chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
-        const float w = (dc && dr) ? __fmul_rn(__fmul_rn(kSqrt2, sum), 0.5f)
-                                   : __fmul_rn(sum, 0.5f);
-        best = fminf(best, __fadd_rn(t.s[c + dc][r + dr], w));
-      }
-    }
-    return best;
-  }
-}
-
 // One Gauss-Seidel sweep.  Each lane carries one line of the tile: a column
 // (ALONG_C false: the sweep walks down or up the rows) or a row (ALONG_C
 // true: it walks right or left along the columns).  `nd` marks the pixels of
@@ -161,50 +126,22 @@ __device__ __forceinline__ float relax8(const WarpTile &t, int c, int r, float c
 // against all eight neighbours, `dm` collects the pixels that changed; both
 // live in registers, bit k = k-th pixel of the line.
 //
-// A step (one pixel per lane) runs when some lane's pixel is marked or the
-// previous step changed something, and then evaluates every lane's pixel:
-// in SIMT that costs the same as evaluating only the marked ones, and it
-// keeps the per-step dependency chain down to the loads, the minimum and a
-// vote.  After the sweep a pixel is marked again if a neighbour evaluated in
-// the same step or a later one changed (neighbours of earlier steps were
-// already final when it was evaluated), and unevaluated pixels keep their
-// marks.  An unmarked pixel therefore cannot be lowered by any neighbour,
-// and the tile is at its local fixpoint exactly when no pixel is marked.
+// A step (one pixel per lane) evaluates every lane's pixel: in SIMT that
+// costs the same as evaluating only the marked ones, and it keeps the
+// per-step dependency chain down to the loads and the minimum.  After the
+// sweep a pixel is marked again if a neighbour evaluated in the same step or
+// a later one changed (neighbours of earlier steps were already final when
+// it was evaluated), and unevaluated pixels keep their marks.  An unmarked
+// pixel therefore cannot be lowered by any neighbour, and the tile is at its
+// local fixpoint exactly when no pixel is marked.  Neighbour values may be
+// old or new: every value is an upper bound of the fixpoint, so any mix
+// gives a valid (and never higher) result.
 //
 // Fill (a cheap update) runs every step from the first marked one to the
 // end of the line with no vote at all; gwdt (a heavier update) votes after
 // each step and skips steps with nothing to do.
-template <int KIND, bool ALONG_C>
-__device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &nd,
-                                      uint32_t &dm_all) {
-  constexpr bool kVote = KIND == GWDT;
-  constexpr int kUnroll = KIND == GWDT ? 2 : 4;
-  uint32_t dm = 0, evald = 0;
-  bool prev = false;
-  int first = 0;
-  if (!kVote) {
-    const uint32_t steps = __reduce_or_sync(0xffffffffu, nd);
-    if (!steps) return;
-    first = dir > 0 ? __ffs(steps) - 1 : kTile - 1 - (31 - __clz(steps));
-  }
-#pragma unroll kUnroll
-  for (int s = first; s < kTile; s++) {
-    const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
-    const uint32_t bit = 1u << k;
-    if (kVote && !prev && !__any_sync(0xffffffffu, nd & bit)) continue;
-    evald |= bit;
-    const int c = ALONG_C ? k + 1 : lane + 1;
-    const int r = ALONG_C ? lane + 1 : k + 1;
-    const float cur = t.s[c][r];
-    const float nv = relax8<KIND>(t, c, r, cur);
-    const bool ch = nv < cur;
-    if (ch) {
-      t.s[c][r] = nv;
-      dm |= bit;
-    }
-    if (kVote) prev = __any_sync(0xffffffffu, ch);
-    __syncwarp();
-  }
+__device__ __forceinline__ void remark(int lane, int dir, uint32_t dm, uint32_t evald,
+                                       uint32_t &nd, uint32_t &dm_all) {
   const uint32_t from_prev = __shfl_up_sync(0xffffffffu, dm, 1);
   const uint32_t from_next = __shfl_down_sync(0xffffffffu, dm, 1);
   const uint32_t side = (lane > 0 ? from_prev : 0u) | (lane < 31 ? from_next : 0u);
@@ -212,6 +149,123 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
   const uint32_t later = dir > 0 ? (any3 >> 1) : (any3 << 1);
   nd = (nd & ~evald) | side | later;
   dm_all |= dm;
+}
+
+// Fill sweep.  A step reads what an evaluation after the previous step's
+// stores would read, but carries part of it in registers: the lane's own
+// pixel behind (its previous result), its own pixel and the adjacent lines'
+// pixels at the current position (read one step ahead; only this step
+// writes them).  It loads only the adjacent lines' pixels behind (written by
+// the previous step) and the three pixels ahead: five state loads a step
+// instead of nine, on the shared-memory pipe that all warps of an SM share.
+template <bool ALONG_C>
+__device__ __forceinline__ void sweep_fill(WarpTile &t, int lane, int dir, uint32_t &nd,
+                                           uint32_t &dm_all) {
+  const uint32_t steps = __reduce_or_sync(0xffffffffu, nd);
+  if (!steps) return;
+  const int first = dir > 0 ? __ffs(steps) - 1 : kTile - 1 - (31 - __clz(steps));
+  // Pixel (line l, position p): t.s[l][p] in the column layout, t.s[p][l]
+  // in the row layout.  The lane's line is l = lane + 1.
+  constexpr int PS = ALONG_C ? kPitch : 1;  // between positions
+  constexpr int LS = ALONG_C ? 1 : kPitch;  // between lines
+  float *const sline = ALONG_C ? &t.s[0][lane + 1] : &t.s[lane + 1][0];
+  const float *const aline = ALONG_C ? &t.a[0][lane + 1] : &t.a[lane + 1][0];
+  const int D = dir * PS;  // to the next position of the sweep
+  uint32_t dm = 0, evald = 0;
+  float ob = 0.f, op = 0.f, lp = 0.f, rp = 0.f;  // own behind / here, adjacent here
+  bool have = false;  // the registers hold the previous step's values
+#pragma unroll 4
+  for (int s = first; s < kTile; s++) {
+    const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
+    const uint32_t bit = 1u << k;
+    evald |= bit;
+    float *const sp = sline + (k + 1) * PS;
+    if (!have) {
+      ob = sp[-D];
+      op = sp[0];
+      lp = sp[-LS];
+      rp = sp[LS];
+    }
+    const float lb = sp[-LS - D], rb = sp[LS - D];  // written by the previous step
+    const float oa = sp[D], la = sp[-LS + D], ra = sp[LS + D];
+    const float cur = op;
+    const float z = aline[(k + 1) * PS];
+    const float a0 = fminf(lb, lp), a1 = fminf(la, ob);
+    const float a2 = fminf(oa, rb), a3 = fminf(rp, ra);
+    const float lo = fminf(cur, fminf(fminf(a0, a1), fminf(a2, a3)));
+    const float nv = (lo > z) ? lo : z;
+    const bool ch = nv < cur;
+    if (ch) {
+      sp[0] = nv;
+      dm |= bit;
+    }
+    ob = ch ? nv : cur;
+    op = oa;
+    lp = la;
+    rp = ra;
+    have = true;
+    __syncwarp();
+  }
+  remark(lane, dir, dm, evald, nd, dm_all);
+}
+
+// The gwdt update at pixel (c, r) from all eight neighbours.  Non-flat and
+// off-grid pixels are staged as state +INF and cost NaN: every path through
+// them evaluates to +INF or NaN, which never wins the minimum, and a
+// non-flat centre (cost NaN) keeps its value.
+__device__ __forceinline__ float relax8_gwdt(const WarpTile &t, int c, int r, float cur) {
+  const float cs = t.a[c][r];
+  float best = cur;
+#pragma unroll
+  for (int dc = -1; dc <= 1; dc++) {
+#pragma unroll
+    for (int dr = -1; dr <= 1; dr++) {
+      if (!(dc || dr)) continue;
+      const float sum = __fadd_rn(cs, t.a[c + dc][r + dr]);
+      // chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
+      const float w = (dc && dr) ? __fmul_rn(__fmul_rn(kSqrt2, sum), 0.5f)
+                                 : __fmul_rn(sum, 0.5f);
+      best = fminf(best, __fadd_rn(t.s[c + dc][r + dr], w));
+    }
+  }
+  return best;
+}
+
+// Gwdt sweep: a step runs when some lane's pixel is marked or the previous
+// step changed something (a vote), and reads all eight neighbours afresh.
+template <bool ALONG_C>
+__device__ __forceinline__ void sweep_gwdt(WarpTile &t, int lane, int dir, uint32_t &nd,
+                                           uint32_t &dm_all) {
+  uint32_t dm = 0, evald = 0;
+  bool prev = false;
+#pragma unroll 2
+  for (int s = 0; s < kTile; s++) {
+    const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
+    const uint32_t bit = 1u << k;
+    if (!prev && !__any_sync(0xffffffffu, nd & bit)) continue;
+    evald |= bit;
+    const int c = ALONG_C ? k + 1 : lane + 1;
+    const int r = ALONG_C ? lane + 1 : k + 1;
+    const float cur = t.s[c][r];
+    const float nv = relax8_gwdt(t, c, r, cur);
+    const bool ch = nv < cur;
+    if (ch) {
+      t.s[c][r] = nv;
+      dm |= bit;
+    }
+    prev = __any_sync(0xffffffffu, ch);
+    __syncwarp();
+  }
+  remark(lane, dir, dm, evald, nd, dm_all);
+}
+
+template <int KIND, bool ALONG_C>
+__device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &nd,
+                                      uint32_t &dm_all) {
+  if (KIND == FILL)
+    sweep_fill<ALONG_C>(t, lane, dir, nd, dm_all);
+  else
+    sweep_gwdt<ALONG_C>(t, lane, dir, nd, dm_all);
 }
 
 template <int KIND>
@@ -471,13 +525,14 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
     const int ni = ti + di, nj = tj + dj;
     tgt = (ni < 0 || nj < 0 || ni >= a.tm || nj >= a.tn) ? -1 : nj * a.tm + ni;
   }
+  // Every lane fences its own stores, then the warp barrier orders those
+  // fences before the flag atomics (the fence-then-barrier publication
+  // pattern): a warp that takes a flag and fences sees every store made
+  // before it.
   if (!__any_sync(0xffffffffu, tgt >= 0)) return;
-  fence_acq_rel_gpu();  // release: this lane's writes before any flag below
+  fence_acq_rel_gpu();
   __syncwarp();
-  if (tgt >= 0) {
-    fence_acq_rel_gpu();  // cumulative over the warp's writes seen at the barrier
-    atomicOr(&a.dirty[tgt], val);
-  }
+  if (tgt >= 0) atomicOr(&a.dirty[tgt], val);
 }
 
 // f = dem where bc == 1 (and where dem is NaN), +INF elsewhere
