@@ -77,7 +77,6 @@ constexpr long long kSpinLimit = 1LL << 22;  // idle scans before giving up
 struct RelaxArgs {
   float *state;
   const float *aux;
-  const int32_t *flats;
   int64_t m, n;
   int tm, tn;
   QueueCtl *ctl;
@@ -372,14 +371,19 @@ template <int KIND>
 __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
   const int ti = tile % a.tm, tj = tile / a.tm;
   const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-  int *const sflat = reinterpret_cast<int *>(&t.s[0][0]);  // flats, before the state
 
+  __syncwarp();  // the previous visit's reads of the tile are done
   // Stage tile + halo with every load in flight at once.  Lane l carries
   // halo row l (pixel row i0 - 1 + l) of all 34 columns; the two last halo
   // rows (32, 33) are spread over the warp, three columns per lane.  The
   // state (updated concurrently by other SMs) is read from L2 into
-  // registers; the read-only aux and flats go straight to shared memory by
-  // asynchronous copies.
+  // registers; the read-only aux goes straight to shared memory by
+  // asynchronous copies.  Off-grid pixels are staged as state +INF with aux
+  // +INF (fill: never lowered, never lowers) or NaN (gwdt: a NaN cost makes
+  // every path through the pixel NaN, which never wins a minimum).  gwdt's
+  // non-flat pixels arrive that way from global memory already (state +INF,
+  // cost NaN during the run), so no flat flags are staged.
+  constexpr float kOffAux = KIND == FILL ? INFINITY : NAN;
   float sv[kHalo], sx[3];
   const int64_t im = i0 - 1 + lane;
   const bool im_ok = im >= 0 && im < a.m;
@@ -394,11 +398,8 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
       const int64_t p = j * a.m + im;
       sv[c] = __ldcg(&a.state[p]);
       cp_async4(&t.a[c][lane], &a.aux[p]);
-      if (KIND == GWDT) cp_async4(&sflat[c * kPitch + lane], &a.flats[p]);
-    } else if (KIND == GWDT) {
-      sflat[c * kPitch + lane] = 0;  // off-grid: never flat, never evaluated
     } else {
-      t.a[c][lane] = INFINITY;  // off-grid pixels of the tile stay at +INF
+      t.a[c][lane] = kOffAux;
     }
   }
 #pragma unroll
@@ -411,34 +412,10 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
         const int64_t p = j * a.m + ix;
         sx[u] = __ldcg(&a.state[p]);
         cp_async4(&t.a[c][rx], &a.aux[p]);
-        if (KIND == GWDT) cp_async4(&sflat[c * kPitch + rx], &a.flats[p]);
-      } else if (KIND == GWDT) {
-        sflat[c * kPitch + rx] = 0;
       } else {
-        t.a[c][rx] = INFINITY;
+        t.a[c][rx] = kOffAux;
       }
     }
-  }
-  cp_async_wait_all();
-  __syncwarp();
-  if (KIND == GWDT) {  // non-flat (and off-grid) pixels: state +INF, cost NaN
-#pragma unroll
-    for (int c = 0; c < kHalo; c++) {
-      const bool fl = sflat[c * kPitch + lane] & 1;
-      if (!fl) {
-        sv[c] = INFINITY;
-        t.a[c][lane] = NAN;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 3; u++) {
-      const int c = (lane >> 1) + 16 * u;
-      if (c < kHalo && !(sflat[c * kPitch + rx] & 1)) {
-        sx[u] = INFINITY;
-        t.a[c][rx] = NAN;
-      }
-    }
-    __syncwarp();
   }
 #pragma unroll
   for (int c = 0; c < kHalo; c++) t.s[c][lane] = sv[c];
@@ -447,6 +424,7 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
     const int c = (lane >> 1) + 16 * u;
     if (c < kHalo) t.s[c][rx] = sx[u];
   }
+  cp_async_wait_all();
   __syncwarp();
 
   // Marks in the column layout: lane l holds interior column l + 1, bit k =
@@ -572,18 +550,20 @@ __global__ void dirty_all_kernel(int *dirty, int n) {
     dirty[t] = DIRTY_FULL;
 }
 
-// dist = 1 at presills, +INF at other flats, 0 elsewhere; flag every tile
-// whose pixels or halo contain a presill (plain stores: idempotent).
-__global__ void gwdt_init_kernel(float *__restrict__ dist,
+// gwdt working arrays: distance 1 at presills and +INF at other flats, as
+// src/gwdt.c:296-308 starts; non-flat pixels take +INF with cost NaN for the
+// run (no path passes through them and they are never lowered) and get
+// their 0 back from gwdt_fix_kernel.  Tiles next to a presill start dirty.
+__global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ wcost,
+                                 const float *__restrict__ costs,
                                  const int32_t *__restrict__ flats, int64_t m,
                                  int64_t n, RelaxArgs qa) {
   const int64_t N = m * n;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
     int32_t f = flats[p];
-    float d = 0.0f;
-    if (f & 1) d = (f & 4) ? 1.0f : INFINITY;
-    dist[p] = d;
+    dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
+    wcost[p] = (f & 1) ? costs[p] : NAN;
     if ((f & 5) == 5) {
       int64_t i = p % m, j = p / m;
       int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
@@ -592,6 +572,14 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist,
         for (int ti = ti0; ti <= ti1; ti++) qa.dirty[tj * qa.tm + ti] = DIRTY_FULL;
     }
   }
+}
+
+// Non-flat pixels: distance 0 (src/gwdt.c:300-302).
+__global__ void gwdt_fix_kernel(float *__restrict__ dist, const int32_t *__restrict__ flats,
+                                int64_t N) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x)
+    if (!(flats[p] & 1)) dist[p] = 0.0f;
 }
 
 // A valid back-link for every reached flat: the first flat neighbour u (in
@@ -650,13 +638,16 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   const int T = g.tiles();
   Workspace &ws = workspace();
   size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
+  if (KIND == GWDT) need += align_up((size_t)g.cells() * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
   int *dirty = (int *)ws.take((size_t)T * 4);
+  // gwdt relaxes over a copy of the costs with NaN at non-flat pixels
+  float *wcost = KIND == GWDT ? (float *)ws.take((size_t)g.cells() * 4) : nullptr;
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
   if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  RelaxArgs ra{state, aux, flats, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
+  RelaxArgs ra{state, KIND == GWDT ? wcost : aux, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
   const int64_t cap_rounds = max_rounds();
   ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
@@ -665,8 +656,8 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
     TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, T);
   } else {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
-    TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats,
-              g.m, g.n, ra);
+    TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, wcost, aux,
+              flats, g.m, g.n, ra);
   }
   TT_CHECK(cudaGetLastError());
   static int blocks_per_sm[2] = {0, 0};
@@ -681,6 +672,8 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
   TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
+  if (KIND == GWDT)
+    TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
   if (status_sink()) {  // deferred: record the abort word, no round trip
     int *rec = sink_record(REC_RELAX, st);
@@ -788,7 +781,7 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
   TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, T);
   TT_CHECK(cudaGetLastError());
-  RelaxArgs ra{f, dem, nullptr, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
+  RelaxArgs ra{f, dem, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
   ra.max_visits = (unsigned long long)T *
                   (unsigned long long)std::min<int64_t>(max_rounds(), 1LL << 20);
   int b = 0;
