@@ -307,16 +307,18 @@ struct Sun2 {
 
 constexpr int kHS = kTile + 4;  // 2-pixel halo for one-sided borders
 
+// Block (x, y) computes tile (x, y + jt0): a launch may cover a band of tile
+// columns, whose DEM columns (plus two on each side) must be in place.
 template <int MODE>  // 0: hillshade, 1: gradients
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 hillshade_kernel(float *__restrict__ out0, float *__restrict__ out1,
                  const float *__restrict__ dem, const float *__restrict__ gout,
                  int64_t m, int64_t n, float twoh, float sx, float sy, float sz,
-                 Sun2 s2) {
+                 Sun2 s2, int jt0) {
   __shared__ float z[kHS][kHS + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
-  const int64_t j0 = (int64_t)blockIdx.y * kTile;
+  const int64_t j0 = (int64_t)(blockIdx.y + jt0) * kTile;
   {  // stage the DEM with every load in flight at once
     constexpr int kC = (kHS + kBlockY - 1) / kBlockY;
     float v[kC][2];
@@ -593,14 +595,15 @@ tt_cuda_status gradient2_dev(float *p0, float *p1, const float *dem,
                              float cellsize, const GridDims &g,
                              cudaStream_t st) {
   TT_LAUNCH(hillshade_kernel<1>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            p0, p1, dem, nullptr, g.m, g.n, 2 * cellsize, 0.f, 0.f, 0.f, Sun2{});
+            p0, p1, dem, nullptr, g.m, g.n, 2 * cellsize, 0.f, 0.f, 0.f, Sun2{}, 0);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
 
-tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
-                             float altitude, float cellsize, const GridDims &g,
-                             cudaStream_t st) {
+tt_cuda_status hillshade_cols_dev(float *out, const float *dem, float azimuth,
+                                  float altitude, float cellsize, const GridDims &g,
+                                  int jt0, int jt1, cudaStream_t st) {
+  if (jt1 <= jt0) return TT_CUDA_SUCCESS;
   float sx, sy, sz;
   sun_vector(azimuth, altitude, &sx, &sy, &sz);
   double zen = 1.57079632679489661923132169163975 - (double)altitude;
@@ -611,10 +614,16 @@ tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
   const float rh = (float)rinv;
   Sun2 s2{sx, (float)(dsx - (double)sx), sy, (float)(dsy - (double)sy),
           sz, (float)(dsz - (double)sz), rh, (float)(rinv - (double)rh)};
-  TT_LAUNCH(hillshade_kernel<0>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st,
-            out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz, s2);
+  TT_LAUNCH(hillshade_kernel<0>, dim3(g.tm, jt1 - jt0), dim3(kBlockX, kBlockY), 0, st,
+            out, nullptr, dem, nullptr, g.m, g.n, 2 * cellsize, sx, sy, sz, s2, jt0);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
+                             float altitude, float cellsize, const GridDims &g,
+                             cudaStream_t st) {
+  return hillshade_cols_dev(out, dem, azimuth, altitude, cellsize, g, 0, g.tn, st);
 }
 
 tt_cuda_status hillshade_backward_dev(float *grad_dem, const float *dem,

@@ -187,6 +187,11 @@ tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
 tt_cuda_status gradient2_dev(float *p0, float *p1, const float *dem,
                              float cellsize, const GridDims &g,
                              cudaStream_t st);
+// Hillshade of tile columns [jt0, jt1) only (DEM columns 32 * jt0 - 2 to
+// 32 * jt1 + 1 must be in place).
+tt_cuda_status hillshade_cols_dev(float *out, const float *dem, float azimuth,
+                                  float altitude, float cellsize, const GridDims &g,
+                                  int jt0, int jt1, cudaStream_t st);
 tt_cuda_status hillshade_dev(float *out, const float *dem, float azimuth,
                              float altitude, float cellsize, const GridDims &g,
                              cudaStream_t st);

@@ -21,6 +21,7 @@ thread_local Workspace *g_ws_override = nullptr;
 int64_t g_max_rounds_override = 0;
 
 constexpr int kMaxDevices = 64;
+constexpr int kCopyEvents = 24;
 
 struct DeviceState {
   std::mutex mu;
@@ -28,10 +29,10 @@ struct DeviceState {
   Workspace io;
   void *pinned = nullptr;
   int sms = 0;
-  // side stream and events for device-to-host copies that overlap the
-  // later stages of a host-pointer pipeline call
-  cudaStream_t copy = nullptr;
-  cudaEvent_t ready[8] = {};
+  // side streams and events for host-device copies that overlap the
+  // kernels of a host-pointer call
+  cudaStream_t copy = nullptr, copy2 = nullptr;
+  cudaEvent_t ready[kCopyEvents] = {};
 };
 
 DeviceState g_dev[kMaxDevices];
@@ -126,14 +127,15 @@ void *pinned_scratch() {
   return d.pinned;
 }
 
-// The per-device copy stream and its events, created on first use.
-static bool copy_lane(cudaStream_t *cs, cudaEvent_t **ev) {
+// The per-device copy streams and their events, created on first use.
+static bool copy_lanes(cudaStream_t *cs, cudaStream_t *cs2, cudaEvent_t **ev) {
   DeviceState &d = g_dev[current_device()];
-  if (!d.copy && cudaStreamCreateWithFlags(&d.copy, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaGetLastError();
-    d.copy = nullptr;
-    return false;
-  }
+  for (cudaStream_t *p : {&d.copy, &d.copy2})
+    if (!*p && cudaStreamCreateWithFlags(p, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      *p = nullptr;
+      return false;
+    }
   for (auto &e : d.ready)
     if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
       cudaGetLastError();
@@ -141,6 +143,7 @@ static bool copy_lane(cudaStream_t *cs, cudaEvent_t **ev) {
       return false;
     }
   *cs = d.copy;
+  if (cs2) *cs2 = d.copy2;
   *ev = d.ready;
   return true;
 }
@@ -697,6 +700,57 @@ tt_cuda_status host_call(const ptrdiff_t dims[2], std::vector<HostArg> args,
   return finish(s, st);
 }
 
+// Host-pointer hillshade in bands of tile columns: the DEM goes up on one
+// copy stream band by band, each band's kernel starts once its columns and
+// the next band's first columns (the stencil's halo) are in place, and its
+// output goes down on a second copy stream while later bands still copy
+// and compute.  Copies into or out of pageable memory block the calling
+// thread, so those calls keep the plain upload, kernel, download sequence.
+tt_cuda_status hillshade_banded(float *hout, const float *hdem, float *dout, float *ddem,
+                                float az, float alt, float cs, const GridDims &g,
+                                cudaStream_t st) {
+  const size_t N = (size_t)g.m * (size_t)g.n;
+  cudaStream_t cin = nullptr, cout = nullptr;
+  cudaEvent_t *ev = nullptr;
+  const int B = (int)std::min<int64_t>(8, g.tn);  // bands
+  if (B < 2 || !host_pinned(hdem) || !host_pinned(hout) || !copy_lanes(&cin, &cout, &ev)) {
+    TT_TRY(h2d(ddem, hdem, N * 4, st));
+    TT_TRY(hillshade_dev(dout, ddem, az, alt, cs, g, st));
+    return d2h(hout, dout, N * 4, st);
+  }
+  auto tile_of = [&](int b) { return (int)((int64_t)b * g.tn / B); };  // first tile column
+  auto col_of = [&](int t) { return std::min<int64_t>((int64_t)t * kTile, g.n); };
+  auto body = [&]() -> tt_cuda_status {
+    TT_CHECK(cudaEventRecord(ev[0], st));  // after earlier work on the staging buffers
+    TT_CHECK(cudaStreamWaitEvent(cin, ev[0], 0));
+    for (int b = 0; b < B; b++) {
+      const int64_t c0 = col_of(tile_of(b)), c1 = col_of(tile_of(b + 1));
+      TT_CHECK(cudaMemcpyAsync(ddem + c0 * g.m, hdem + c0 * g.m, (size_t)((c1 - c0) * g.m) * 4,
+                               cudaMemcpyHostToDevice, cin));
+      TT_CHECK(cudaEventRecord(ev[1 + b], cin));
+    }
+    for (int b = 0; b < B; b++) {
+      TT_CHECK(cudaStreamWaitEvent(st, ev[1 + std::min(b + 1, B - 1)], 0));  // band and halo
+      TT_TRY(hillshade_cols_dev(dout, ddem, az, alt, cs, g, tile_of(b), tile_of(b + 1), st));
+      TT_CHECK(cudaEventRecord(ev[1 + B + b], st));
+      TT_CHECK(cudaStreamWaitEvent(cout, ev[1 + B + b], 0));
+      const int64_t c0 = col_of(tile_of(b)), c1 = col_of(tile_of(b + 1));
+      TT_CHECK(cudaMemcpyAsync(hout + c0 * g.m, dout + c0 * g.m, (size_t)((c1 - c0) * g.m) * 4,
+                               cudaMemcpyDeviceToHost, cout));
+    }
+    TT_CHECK(cudaEventRecord(ev[1 + 2 * B], cout));
+    TT_CHECK(cudaStreamWaitEvent(st, ev[1 + 2 * B], 0));
+    return TT_CUDA_SUCCESS;
+  };
+  tt_cuda_status s = body();
+  // nothing issued may still run into the caller's buffers after return
+  if (cudaStreamSynchronize(cin) != cudaSuccess || cudaStreamSynchronize(cout) != cudaSuccess) {
+    cudaGetLastError();
+    if (s == TT_CUDA_SUCCESS) s = TT_CUDA_ERR_CUDA;
+  }
+  return s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -981,10 +1035,10 @@ void tt_cuda_hillshade_fused(float *output, float *dem, float azimuth,
     return;
   }
   size_t N = (size_t)(dims[0] * dims[1]);
-  host_call(dims, {{output, N * 4, false, true}, {dem, N * 4, true, false}},
+  host_call(dims, {{output, N * 4, false, false}, {dem, N * 4, false, false}},
             [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
-              return hillshade_dev((float *)a[0].dev, (const float *)a[1].dev, azimuth,
-                                   altitude, cellsize, g, st);
+              return hillshade_banded(output, dem, (float *)a[0].dev, (float *)a[1].dev,
+                                      azimuth, altitude, cellsize, g, st);
             });
 }
 
@@ -1031,7 +1085,7 @@ void tt_cuda_d8_pipeline(float *filled, int32_t *flats, float *dist,
               out.node = node;
               out.direction = direction;
               out.acc = acc;
-              if (!copy_lane(&out.cs, &out.ev)) out.cs = nullptr;
+              if (!copy_lanes(&out.cs, nullptr, &out.ev)) out.cs = nullptr;
               tt_cuda_status s = pipeline_body(
                   (float *)a[3].dev, (int32_t *)a[4].dev, (float *)a[5].dev,
                   node ? (ptrdiff_t *)a[6].dev : nullptr, (uint8_t *)a[7].dev,

@@ -266,3 +266,48 @@ def test_pipeline(gpu, port, case):
     assert np.array_equal(got["direction"], r["direction"])
     assert topo_positions_ok(got["node"], got["direction"])
     assert np.array_equal(got["acc"], r["acc"])
+
+
+@pytest.mark.parametrize("shape", [(300, 700), (257, 65), (1000, 33), (64, 2000), (37, 95)])
+def test_pinned_host_paths(gpu, shape):
+    """Host-pointer calls on page-locked buffers take the overlapped paths
+    (column bands for hillshade, early output copies for the pipeline) and
+    give the same bits as the pageable path."""
+    import torch
+
+    from libtopotoolbox_gb300 import _native as N
+    from libtopotoolbox_gb300 import api, dems
+
+    m, n = shape
+    dem = dems.pcg4d_dem(shape, 7)
+    bc = dems.border_bc(shape)
+
+    def pinned(dtype):  # column-major (m, n) view of a page-locked buffer
+        return torch.empty((n, m), dtype=dtype, pin_memory=True).numpy().T
+
+    h_dem = pinned(torch.float32)
+    h_dem[:] = dem
+    h_bc = pinned(torch.uint8)
+    h_bc[:] = bc
+    ptr = lambda a: N.C.c_void_p(a.ctypes.data)  # noqa: E731
+    dp, keep = N.dims_arg((m, n))
+    lib = N.lib()
+
+    hs = pinned(torch.float32)
+    lib.tt_cuda_hillshade_fused(ptr(hs), ptr(h_dem), HS_AZ, HS_ALT, 30.0, dp)
+    N.check(N.last_status(), "hillshade_fused")
+    assert same_float(hs, api.hillshade_fused(dem, HS_AZ, HS_ALT, 30.0))
+
+    out = {k: pinned(t) for k, t in [("filled", torch.float32), ("flats", torch.int32),
+                                      ("dist", torch.float32), ("node", torch.int64),
+                                      ("direction", torch.uint8), ("acc", torch.float32)]}
+    lib.tt_cuda_d8_pipeline(ptr(out["filled"]), ptr(out["flats"]), ptr(out["dist"]),
+                            ptr(out["node"]), ptr(out["direction"]), ptr(out["acc"]),
+                            ptr(h_dem), ptr(h_bc), None, dp)
+    N.check(N.last_status(), "d8_pipeline")
+    ref = api.d8_pipeline(dem, bc)
+    for k in ("filled", "dist", "acc"):
+        assert same_float(out[k], ref[k]), k
+    for k in ("flats", "direction"):
+        assert np.array_equal(out[k], ref[k]), k
+    assert topo_positions_ok(out["node"], out["direction"])
