@@ -1009,7 +1009,8 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
 // subtree heights together, so the pipeline walks the forest once for both.
 tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *dir,
                                   const float *weights, const GridDims &g,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, tt_cuda_status (*acc_done)(void *),
+                                  void *ctx) {
   UpWork w;
   TT_TRY_STATUS(up_alloc(g, true, true, w));
   int wshift = 0;
@@ -1018,6 +1019,7 @@ tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *di
   int h6[6];
   tt_cuda_status s = up_status(w, st, h6);
   if (s == TT_CUDA_ERR_CYCLE) return s;
+  if (acc_done) TT_TRY_STATUS(acc_done(ctx));  // acc is complete on `st` here
   TT_TRY_STATUS(node_scatter(node, w, h6, g, st));
   return s;
 }

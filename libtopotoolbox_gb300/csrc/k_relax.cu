@@ -514,13 +514,26 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
 }
 
 // f = dem where bc == 1 (and where dem is NaN), +INF elsewhere
-// (src/fillsinks.c:24-37 in the un-negated space).
+// (src/fillsinks.c:24-37 in the un-negated space).  With `dirty`, the tiles
+// whose pixels or halo hold such a seed start dirty: every other tile is
+// +INF throughout and already at its local fixpoint until a neighbour
+// publishes a change (plain stores: idempotent).
 __global__ void fill_init_kernel(float *__restrict__ f, const float *__restrict__ dem,
-                                 const uint8_t *__restrict__ bc, int64_t N) {
+                                 const uint8_t *__restrict__ bc, int64_t m, int64_t n,
+                                 int *__restrict__ dirty, int tm) {
+  const int64_t N = m * n;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
     float z = dem[p];
-    f[p] = (bc[p] == 1 || isnan(z)) ? z : INFINITY;
+    const bool seed = bc[p] == 1 || isnan(z);
+    f[p] = seed ? z : INFINITY;
+    if (seed && dirty) {
+      const int64_t i = p % m, j = p / m;
+      const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
+      const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
+      for (int tj = tj0; tj <= tj1; tj++)
+        for (int ti = ti0; ti <= ti1; ti++) dirty[tj * tm + ti] = DIRTY_FULL;
+    }
   }
 }
 
@@ -631,10 +644,12 @@ int elementwise_grid(int64_t N) {
 }
 
 // Host driver: mark the starting tiles, run one persistent launch, read the
-// status.
+// status.  `bc` (sink filling only) selects the seeded start: the fill's
+// initial state is written here and only tiles next to a seed start dirty;
+// without it every tile starts dirty on the caller's initial state.
 template <int KIND>
 tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
-                         const GridDims &g, cudaStream_t st) {
+                         const GridDims &g, cudaStream_t st, const uint8_t *bc = nullptr) {
   const int T = g.tiles();
   Workspace &ws = workspace();
   size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
@@ -652,7 +667,11 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
   const int tgrid = (T + 255) / 256;
-  if (KIND == FILL) {
+  if (KIND == FILL && bc) {
+    TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
+    TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, aux, bc, g.m,
+              g.n, dirty, g.tm);
+  } else if (KIND == FILL) {
     TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, T);
   } else {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
@@ -693,10 +712,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
 
 tt_cuda_status fill_dev(float *f, const float *dem, const uint8_t *bc,
                         const GridDims &g, cudaStream_t st) {
-  TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem,
-            bc, g.cells());
-  TT_CHECK(cudaGetLastError());
-  return run_queue<FILL>(f, dem, nullptr, g, st);
+  return run_queue<FILL>(f, dem, nullptr, g, st, bc);
 }
 
 tt_cuda_status reconstruct_dev(float *marker, const float *mask,
@@ -776,8 +792,8 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   QueueCtl *ctl = (QueueCtl *)base;
   int *dirty = (int *)base + kNoAllocHeaderWords;
   const int T = g.tiles();
-  TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem, bc,
-            g.cells());
+  TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem, bc, g.m,
+            g.n, nullptr, g.tm);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
   TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, T);
   TT_CHECK(cudaGetLastError());

@@ -177,9 +177,14 @@ tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,
                               cudaStream_t st);
 // Exact subtree pixel counts (int) of the forest of `dir`.
+// Node order and accumulation from one forest contraction; `acc_done(ctx)`
+// (may be null) runs once the accumulation is enqueued, before the node
+// order's sort.
 tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *dir,
                                   const float *weights, const GridDims &g,
-                                  cudaStream_t st);
+                                  cudaStream_t st,
+                                  tt_cuda_status (*acc_done)(void *) = nullptr,
+                                  void *ctx = nullptr);
 tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cudaStream_t st);
 tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
                                        const float *grad_acc,

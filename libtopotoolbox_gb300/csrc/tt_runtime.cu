@@ -601,8 +601,22 @@ static tt_cuda_status pipeline_body(float *filled, int32_t *flats, float *dist,
   TT_TRY(directions_dev(direction, filled, dist, flats, g, 0, st));
   if (out) TT_TRY(out->send(out->direction, direction, n, st));
   if (node && acc) {  // one forest contraction for both
-    TT_TRY_SOFT(node_order_acc_dev(node, acc, direction, weights, g, st), soft);
-    if (out) TT_TRY(out->send(out->acc, acc, n * 4, st));
+    struct AccCopy {
+      EarlyOut *out;
+      float *acc;
+      size_t bytes;
+      cudaStream_t st;
+      bool sent;
+    } ac{out, acc, n * 4, st, false};
+    auto send_acc = [](void *c) -> tt_cuda_status {  // overlaps the node sort
+      AccCopy *a = static_cast<AccCopy *>(c);
+      a->sent = true;
+      return a->out->send(a->out->acc, a->acc, a->bytes, a->st);
+    };
+    TT_TRY_SOFT(node_order_acc_dev(node, acc, direction, weights, g, st,
+                                   out ? +send_acc : nullptr, &ac),
+                soft);
+    if (out && !ac.sent) TT_TRY(out->send(out->acc, acc, n * 4, st));
     if (out) TT_TRY(out->send(out->node, node, n * 8, st));
   } else {
     if (node) TT_TRY_SOFT(node_order_dev(node, direction, g, 0, st), soft);
