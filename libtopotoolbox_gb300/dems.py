@@ -151,12 +151,9 @@ def plain_16384(seed=3, size=16384):
     return np.asfortranarray(z, dtype=np.float32), border_bc(z.shape), 30.0
 
 
-def batch_tiles(seed=4, count=512, side_range=(128, 2048)):
-    """Workload 4: `count` independent tiles, side log-uniform in side_range,
-    aspect ratio U[0.5, 2], Hurst U[0.6, 0.9], relief U[50, 1500] m,
-    quantised to 0.1 m.  Returns a list of (dem, bc) pairs."""
+def _batch_params(seed, count, side_range):
+    """(index, nrows, ncols, hurst, relief) of every tile of workload 4."""
     rng = np.random.default_rng(seed + 4000)
-    out = []
     lo, hi = math.log(side_range[0]), math.log(side_range[1])
     for t in range(count):
         s = math.exp(rng.uniform(lo, hi))
@@ -165,6 +162,24 @@ def batch_tiles(seed=4, count=512, side_range=(128, 2048)):
         nc = max(8, int(round(s / math.sqrt(a))))
         h = rng.uniform(0.6, 0.9)
         relief = rng.uniform(50.0, 1500.0)
+        yield t, nr, nc, h, relief
+
+
+def batch_tile_shapes(seed=4, count=512, side_range=(128, 2048)):
+    """The (nrows, ncols) of every tile of `batch_tiles`, without building
+    the tiles."""
+    return [(nr, nc) for _, nr, nc, _, _ in _batch_params(seed, count, side_range)]
+
+
+def batch_tiles(seed=4, count=512, side_range=(128, 2048), only=None):
+    """Workload 4: `count` independent tiles, side log-uniform in side_range,
+    aspect ratio U[0.5, 2], Hurst U[0.6, 0.9], relief U[50, 1500] m,
+    quantised to 0.1 m.  Returns a list of (dem, bc) pairs; with `only` (a
+    collection of tile indices), just those tiles, in index order."""
+    out = []
+    for t, nr, nc, h, relief in _batch_params(seed, count, side_range):
+        if only is not None and t not in only:
+            continue
         z = fractal_surface((nr, nc), h, relief, seed * 100003 + t)
         z = (np.round(np.asarray(z, dtype=np.float64) * 10.0) / 10.0).astype(np.float32)
         out.append((np.asfortranarray(z), border_bc((nr, nc))))
