@@ -151,6 +151,12 @@ __device__ __forceinline__ int local_receiver(const uint8_t (*dir)[36], int ii,
 //     its receivers to the in-tile terminal and records it with the number
 //     of steps (first pass only).
 constexpr int kUpThreads = 128;
+// Resident blocks per SM for the two tile passes (48 and 40 registers a
+// thread, no spills; shared memory allows 10 and 15): walks wait at block
+// barriers for the block's longest chain, so more resident blocks keep the
+// SM busy meanwhile.
+constexpr int kUpBlocks = 10;
+constexpr int kFinBlocks = 12;
 constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
 
 struct UpTile {
@@ -172,7 +178,7 @@ __device__ __forceinline__ int ring_pixel(int k) {
   return (kTile - 1) * kTile + (k - 3 * kTile + 3);     // jj = 31, ii = 1..30
 }
 
-__global__ void __launch_bounds__(kUpThreads, 8) forest_up_kernel(UpArgs a) {
+__global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs a) {
   __shared__ UpTile t;
   const int tid = threadIdx.x;
   const int T = a.tm * a.tn;
@@ -318,7 +324,7 @@ struct FinTile {
   int16_t rl[kTileCells];
 };
 
-__global__ void __launch_bounds__(kUpThreads, 8) forest_fin_kernel(UpArgs a) {
+__global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpArgs a) {
   __shared__ FinTile t;
   const int tid = threadIdx.x;
   const int T = a.tm * a.tn;
@@ -873,7 +879,8 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.h_out = w.h;
   a.hmax = w.counters + 3;
   a.err = w.counters + 4;
-  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 16);
+  // one resident wave of blocks, each looping over tiles
+  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kUpBlocks);
   TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
@@ -885,7 +892,8 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   TT_LAUNCH(coarse_scatter_kernel, lg, 256, 0, st, w.counters + 0, w.elist, w.ccell,
             w.cell);
   a.phase = 3;
-  TT_LAUNCH(forest_fin_kernel, tgrid, kUpThreads, 0, st, a);
+  TT_LAUNCH(forest_fin_kernel, (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks),
+            kUpThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
