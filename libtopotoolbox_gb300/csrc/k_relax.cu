@@ -136,9 +136,9 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
 // old or new: every value is an upper bound of the fixpoint, so any mix
 // gives a valid (and never higher) result.
 //
-// Fill (a cheap update) runs every step from the first marked one to the
-// end of the line with no vote at all; gwdt (a heavier update) votes after
-// each step and skips steps with nothing to do.
+// Both kinds run every step from the first marked one to the end of the
+// line with no vote at all: a per-step vote would put a warp-wide round trip
+// on the chain between steps.
 __device__ __forceinline__ void remark(int lane, int dir, uint32_t dm, uint32_t evald,
                                        uint32_t &nd, uint32_t &dm_all) {
   const uint32_t from_prev = __shfl_up_sync(0xffffffffu, dm, 1);
@@ -208,51 +208,79 @@ __device__ __forceinline__ void sweep_fill(WarpTile &t, int lane, int dir, uint3
   remark(lane, dir, dm, evald, nd, dm_all);
 }
 
-// The gwdt update at pixel (c, r) from all eight neighbours.  Non-flat and
-// off-grid pixels are staged as state +INF and cost NaN: every path through
-// them evaluates to +INF or NaN, which never wins the minimum, and a
-// non-flat centre (cost NaN) keeps its value.
-__device__ __forceinline__ float relax8_gwdt(const WarpTile &t, int c, int r, float cur) {
-  const float cs = t.a[c][r];
-  float best = cur;
-#pragma unroll
-  for (int dc = -1; dc <= 1; dc++) {
-#pragma unroll
-    for (int dr = -1; dr <= 1; dr++) {
-      if (!(dc || dr)) continue;
-      const float sum = __fadd_rn(cs, t.a[c + dc][r + dr]);
-      // chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
-      const float w = (dc && dr) ? __fmul_rn(__fmul_rn(kSqrt2, sum), 0.5f)
-                                 : __fmul_rn(sum, 0.5f);
-      best = fminf(best, __fadd_rn(t.s[c + dc][r + dr], w));
-    }
-  }
-  return best;
-}
-
-// Gwdt sweep: a step runs when some lane's pixel is marked or the previous
-// step changed something (a vote), and reads all eight neighbours afresh.
+// Gwdt sweep in the fill's form: every step from the first marked one to
+// the end of the line, no votes, with the values a step would re-read
+// unchanged carried in registers (state of the lane's own pixel behind and
+// here, adjacent lines here; costs of all three lines behind and here).
+// Non-flat and off-grid pixels are staged as state +INF and cost NaN: every
+// path through them evaluates to +INF or NaN, which never wins the minimum,
+// and a non-flat centre (cost NaN) keeps its value.
 template <bool ALONG_C>
-__device__ __forceinline__ void sweep_gwdt(WarpTile &t, int lane, int dir, uint32_t &nd,
-                                           uint32_t &dm_all) {
+__device__ __forceinline__ void sweep_gwdt_run(WarpTile &t, int lane, int dir, uint32_t &nd,
+                                               uint32_t &dm_all) {
+  const uint32_t steps = __reduce_or_sync(0xffffffffu, nd);
+  if (!steps) return;
+  const int first = dir > 0 ? __ffs(steps) - 1 : kTile - 1 - (31 - __clz(steps));
+  constexpr int PS = ALONG_C ? kPitch : 1;
+  constexpr int LS = ALONG_C ? 1 : kPitch;
+  float *const sline = ALONG_C ? &t.s[0][lane + 1] : &t.s[lane + 1][0];
+  const float *const aline = ALONG_C ? &t.a[0][lane + 1] : &t.a[lane + 1][0];
+  const int D = dir * PS;
   uint32_t dm = 0, evald = 0;
-  bool prev = false;
+  float ob = 0.f, op = 0.f, lp = 0.f, rp = 0.f;
+  float cb0 = 0.f, cb1 = 0.f, cb2 = 0.f, cp0 = 0.f, cp1 = 0.f, cp2 = 0.f;
+  bool have = false;
 #pragma unroll 2
-  for (int s = 0; s < kTile; s++) {
-    const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
+  for (int s = first; s < kTile; s++) {
+    const int k = dir > 0 ? s : kTile - 1 - s;
     const uint32_t bit = 1u << k;
-    if (!prev && !__any_sync(0xffffffffu, nd & bit)) continue;
     evald |= bit;
-    const int c = ALONG_C ? k + 1 : lane + 1;
-    const int r = ALONG_C ? lane + 1 : k + 1;
-    const float cur = t.s[c][r];
-    const float nv = relax8_gwdt(t, c, r, cur);
+    float *const sp = sline + (k + 1) * PS;
+    const float *const ap = aline + (k + 1) * PS;
+    if (!have) {
+      ob = sp[-D];
+      op = sp[0];
+      lp = sp[-LS];
+      rp = sp[LS];
+      cb0 = ap[-LS - D];
+      cb1 = ap[-D];
+      cb2 = ap[LS - D];
+      cp0 = ap[-LS];
+      cp1 = ap[0];
+      cp2 = ap[LS];
+    }
+    const float lb = sp[-LS - D], rb = sp[LS - D];  // written by the previous step
+    const float oa = sp[D], la = sp[-LS + D], ra = sp[LS + D];
+    const float ca0 = ap[-LS + D], ca1 = ap[D], ca2 = ap[LS + D];
+    const float cur = op, cs = cp1;
+    // d(u) + chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
+    auto side = [&](float d, float c) {
+      return __fadd_rn(d, __fmul_rn(__fadd_rn(cs, c), 0.5f));
+    };
+    auto diag = [&](float d, float c) {
+      return __fadd_rn(d, __fmul_rn(__fmul_rn(kSqrt2, __fadd_rn(cs, c)), 0.5f));
+    };
+    float best = fminf(cur, fminf(side(oa, ca1), side(lp, cp0)));
+    best = fminf(best, fminf(side(rp, cp2), diag(la, ca0)));
+    best = fminf(best, diag(ra, ca2));
+    best = fminf(best, fminf(side(ob, cb1), fminf(diag(lb, cb0), diag(rb, cb2))));
+    const float nv = best;
     const bool ch = nv < cur;
     if (ch) {
-      t.s[c][r] = nv;
+      sp[0] = nv;
       dm |= bit;
     }
-    prev = __any_sync(0xffffffffu, ch);
+    ob = ch ? nv : cur;
+    op = oa;
+    lp = la;
+    rp = ra;
+    cb0 = cp0;
+    cb1 = cp1;
+    cb2 = cp2;
+    cp0 = ca0;
+    cp1 = ca1;
+    cp2 = ca2;
+    have = true;
     __syncwarp();
   }
   remark(lane, dir, dm, evald, nd, dm_all);
@@ -264,7 +292,7 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
   if (KIND == FILL)
     sweep_fill<ALONG_C>(t, lane, dir, nd, dm_all);
   else
-    sweep_gwdt<ALONG_C>(t, lane, dir, nd, dm_all);
+    sweep_gwdt_run<ALONG_C>(t, lane, dir, nd, dm_all);
 }
 
 template <int KIND>
