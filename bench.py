@@ -3,13 +3,15 @@
 
 One step = the plain pipeline (fillsinks -> identifyflats ->
 gwdt_computecosts -> gwdt -> flow_routing_d8_carve -> flow_accumulation, unit
-weights) plus hillshade on one synthetic DEM, through the library's device
-entry points with the DEM already in HBM.  The default workload is the
-4096 x 4096 fractal with 200 inverted Gaussian pits rounded to 1 m.
+weights) on one synthetic DEM, through the library's fused device entry point
+with the DEM already in HBM.  The default workload is the whole-chip
+16384 x 16384 fractal (5 % nodata disks as -INF outlets, 1000 closed
+depressions); the 4096 x 4096 workload with hillshade is measured beside it.
 
 Prints one JSON line (rank 0).  `--impl reference` times the CPU
 implementation of the same path (the oracle's C restatement of the
-reference) on the host cores instead.
+reference, pinned bit for bit to the compiled reference) on whole workload
+DEMs on the host cores instead.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
 """
@@ -40,12 +42,17 @@ BYTES = {
 }
 PIPELINE_BYTES = sum(v for k, v in BYTES.items() if k != "hillshade_fused")  # 87
 HS_AZ, HS_ALT = 3.9269908, 1.0471976
+# Host memory one whole-DEM oracle pipeline holds at its peak (gwdt: DEM, bc,
+# filled, flats, costs, dist, heap, back), bytes per pixel, with headroom.
+CPU_BYTES_PER_PIXEL = 40
 
+# name -> (generator in libtopotoolbox_gb300.dems, hillshade in the step)
 WORKLOADS = {
-    "plain_4096_hillshade": ("plain_4096", {}),
-    "plain_16384": ("plain_16384", {}),
-    "plain_512": ("plain_512", {}),
+    "plain_16384": ("plain_16384", False),
+    "plain_4096_hillshade": ("plain_4096", True),
+    "plain_512": ("plain_512", False),
 }
+SECONDARY = "plain_4096_hillshade"
 
 
 def peaks():
@@ -57,13 +64,15 @@ def peaks():
 
 
 def make_workload(name):
+    """(dem, bc, cellsize, hillshade) of a workload; NaN nodata becomes -INF
+    with bc = 1, the reference callers' convention (test/grid.c:505-515)."""
     from libtopotoolbox_gb300 import dems
 
-    gen, kw = WORKLOADS[name]
-    dem, bc, cs = getattr(dems, gen)(**kw)
+    gen, hs = WORKLOADS[name]
+    dem, bc, cs = getattr(dems, gen)()
     if np.isnan(dem).any():
         dem, bc, _ = dems.nan_to_outlets(dem, bc)
-    return dem, bc, cs
+    return dem, bc, cs, hs
 
 
 class ClockSampler:
@@ -73,13 +82,16 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, off=False):
         self.index = index
+        self.off = off
         self.proc = None
         self.lines = []
 
     def __enter__(self):
         self.start = 0
+        if self.off:
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
@@ -140,30 +152,42 @@ def load_traffic():
     return {}
 
 
-def cpu_baseline_sample(dem, bc, seconds_target=20.0):
-    """The oracle port on a bounded crop of the workload, one host core."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import pyoracle
+class CpuPipeline(threading.Thread):
+    """The oracle's C restatement of the reference pipeline on one whole
+    workload DEM, one host thread (the reference's pipeline is serial), run
+    beside the GPU legs: its ctypes calls release the GIL."""
 
-    orc = pyoracle.Oracle("port")
-    side = min(dem.shape[0], 1024)
-    crop = np.asfortranarray(dem[:side, :side])
-    cb = np.zeros(crop.shape, np.uint8, order="F")
-    cb[0, :] = cb[-1, :] = cb[:, 0] = cb[:, -1] = 1
-    cb |= np.asfortranarray(bc[:side, :side])
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
-        orc.pipeline(crop, cb, hybrid=True)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el > seconds_target or reps >= 50:
-            break
-    gcps = crop.size * reps / el / 1e9
-    return {"value": gcps, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{reps} x plain pipeline (hybrid fill) on a {side}x{side} crop of the "
-                      f"workload DEM, oracle C restatement of the reference, 1 thread, "
-                      f"{el:.1f} s"}
+    def __init__(self, dem, bc, cs, hillshade):
+        super().__init__(daemon=True)
+        self.args = (dem, bc, (HS_AZ, HS_ALT, cs) if hillshade else None)
+        self.seconds = None
+        self.error = None
+
+    def run(self):
+        try:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import pyoracle
+
+            orc = pyoracle.Oracle("port")
+            dem, bc, hs = self.args
+            t0 = time.perf_counter()
+            orc.run_pipeline(dem, bc, hillshade=hs)
+            self.seconds = time.perf_counter() - t0
+        except Exception as e:  # reported in the JSON line
+            self.error = repr(e)
+
+    def result(self, what):
+        self.join()
+        m, n = self.args[0].shape
+        if self.seconds is None:
+            return {"value": None, "unit": UNIT, "cores": 1, "kind": "port",
+                    "sample": what, "error": self.error}
+        return {"value": m * n / self.seconds / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                "seconds": self.seconds,
+                "sample": f"{what}: one whole {m}x{n} workload DEM through fillsinks_hybrid, "
+                          f"identifyflats, gwdt_computecosts, gwdt, flow_routing_d8_carve, "
+                          f"flow_accumulation (oracle C restatement of the reference, pinned bit "
+                          f"for bit to it), 1 thread, {self.seconds:.1f} s"}
 
 
 def adjoint_leg(dev, reps=5):
@@ -467,8 +491,24 @@ def io_leg(dem, reps=5):
             "roundtrip_exact": ok}
 
 
+def mem_available():
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                return int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
 def run_reference(args):
-    """--impl reference: the CPU implementation on the host cores."""
+    """--impl reference: the CPU implementation on whole workload DEMs.
+
+    Every step is one whole DEM of the workload (the same DEM, config and
+    metric as the GPU arm) through the oracle's C restatement of the
+    reference, which is serial per DEM; steps run concurrently on the host
+    cores, as many at once as the cores and the host memory allow.  W
+    warm-up steps, then K timed steps; value = K * pixels / wall time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -477,48 +517,233 @@ def run_reference(args):
     from concurrent.futures import ThreadPoolExecutor
 
     orc = pyoracle.Oracle("port")
-    dem, bc, cs = make_workload(args.workload)
+    dem, bc, cs, hs = make_workload(args.workload)
+    cells = dem.size
     cores = os.cpu_count() or 1
-    side = min(dem.shape[0], 1024)
-    crops = []
-    for k in range(cores):
-        i0 = (k * 613) % max(1, dem.shape[0] - side + 1)
-        j0 = (k * 389) % max(1, dem.shape[1] - side + 1)
-        c = np.asfortranarray(dem[i0:i0 + side, j0:j0 + side])
-        b = np.zeros(c.shape, np.uint8, order="F")
-        b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 1
-        b |= np.asfortranarray(bc[i0:i0 + side, j0:j0 + side])
-        crops.append((c, b))
+    per = cells * CPU_BYTES_PER_PIXEL
+    avail = mem_available()
+    conc = max(1, min(cores, args.steps, int(0.7 * avail / per) if avail else 1))
+    hsarg = (HS_AZ, HS_ALT, cs) if hs else None
 
-    def one(cb):
-        orc.pipeline(cb[0], cb[1], hybrid=True)
-        orc.hillshade_fused(cb[0], HS_AZ, HS_ALT, cs)
+    def one(_):
+        t0 = time.perf_counter()
+        orc.run_pipeline(dem, bc, hillshade=hsarg)
+        return time.perf_counter() - t0
 
-    with ThreadPoolExecutor(max_workers=cores) as ex:
-        for _ in range(args.warmup):
-            list(ex.map(one, crops))
-        times = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            list(ex.map(one, crops))
-            times.append(time.perf_counter() - t0)
-    cells = side * side * cores
-    ms = 1e3 * float(np.mean(times))
-    value = cells / (ms * 1e-3) / 1e9
+    with ThreadPoolExecutor(max_workers=conc) as ex:
+        warm = list(ex.map(one, range(args.warmup)))
+        t0 = time.perf_counter()
+        per_step = list(ex.map(one, range(args.steps)))
+        wall = time.perf_counter() - t0
+    ms = 1e3 * wall / args.steps
+    value = cells * args.steps / wall / 1e9
+    m, n = dem.shape
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "sample": f"{cores} concurrent {side}x{side} crops"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"per step: plain pipeline + hillshade on {cores} crops of "
-                                   f"{side}x{side}, one per host thread (oracle C restatement; "
-                                   f"the reference sources are not on this host)"},
+        "data": "synthetic", "config": workload_config(args.workload, dem.shape, hs, 1),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": conc, "kind": "port",
+                         "sample": f"per step one whole {m}x{n} workload DEM through the "
+                                   f"pipeline{' + hillshade' if hs else ''} (oracle C "
+                                   f"restatement of the reference, pinned bit for bit to it; "
+                                   f"the reference's sources are not on this host); {conc} "
+                                   f"steps at a time on {cores} host cores, limited by host "
+                                   f"memory ({avail / 2**30:.0f} GiB available)",
+                         "single_step_s": {"median": float(np.median(per_step)),
+                                           "min": float(np.min(per_step)),
+                                           "max": float(np.max(per_step))},
+                         "warmup_s": float(np.sum(warm))},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(name, shape, hillshade, world):
+    m, n = shape
+    cfg = {"workload": name, "dem": f"{m}x{n} float32 column-major", "weights": "unit",
+           "l2": "inputs larger than L2, and L2 flushed (512 MiB write) between timed steps",
+           "parallelism": "replicas" if world > 1 else "single"}
+    if name == "plain_16384":
+        cfg["nodata"] = "5 % NaN disks, as -INF outlets with bc = 1"
+    if hillshade:
+        cfg["hillshade"] = "azimuth 315, altitude 60"
+    return cfg
+
+
+def gpu_pipeline_leg(N, dev, name, steps, warmup, world=1, dist=None, clocks=None):
+    """Times one workload on the GPU.  Returns the measurements and the
+    device outputs (node, direction) for the legs that reuse them.
+
+    * fused: tt_cuda_d8_pipeline_dev on device-resident inputs (the
+      headline), CUDA events on the launching stream, L2 flushed between
+      steps;
+    * per function: one tt_cuda_<name>_dev call per reference function,
+      timed stage by stage;
+    * e2e: the host-pointer C ABI (tt_cuda_d8_pipeline, and
+      tt_cuda_hillshade_fused where the workload has hillshade) from pinned
+      host buffers, copies inside the timed region."""
+    import torch
+
+    lib = N.lib()
+    dem, bc, cs, hs = make_workload(name)
+    m, n = dem.shape
+    cells = m * n
+    d_dem = torch.from_numpy(np.ascontiguousarray(dem.T)).to(dev)
+    d_bc = torch.from_numpy(np.ascontiguousarray(bc.T)).to(dev)
+    mk = lambda dt: torch.empty((n, m), dtype=dt, device=dev)  # noqa: E731
+    o = {"filled": mk(torch.float32), "flats": mk(torch.int32), "costs": mk(torch.float32),
+         "conncomps": mk(torch.int64), "dist": mk(torch.float32), "node": mk(torch.int64),
+         "direction": mk(torch.uint8), "acc": mk(torch.float32)}
+    if hs:
+        o["hillshade"] = mk(torch.float32)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2
+    stream = torch.cuda.current_stream(dev)
+    sp = N.C.c_void_p(stream.cuda_stream)
+    dp, keep = N.dims_arg((m, n))
+    P = lambda t: N.C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+
+    stages = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
+              "flow_routing_d8_carve", "flow_accumulation"] + (["hillshade_fused"] if hs else [])
+    rounds = {}
+
+    def step(events=None):
+        calls = [
+            lambda: lib.tt_cuda_fillsinks_dev(P(o["filled"]), P(d_dem), P(d_bc), dp, sp),
+            lambda: lib.tt_cuda_identifyflats_dev(P(o["flats"]), P(o["filled"]), dp, None, sp),
+            lambda: lib.tt_cuda_gwdt_computecosts_dev(P(o["costs"]), P(o["conncomps"]),
+                                                      P(o["flats"]), P(d_dem), P(o["filled"]),
+                                                      dp, sp),
+            lambda: lib.tt_cuda_gwdt_dev(P(o["dist"]), None, P(o["costs"]), P(o["flats"]), dp, sp),
+            lambda: lib.tt_cuda_flow_routing_d8_carve_dev(P(o["node"]), P(o["direction"]),
+                                                          P(o["filled"]), P(o["dist"]),
+                                                          P(o["flats"]), dp, 0, sp),
+            lambda: lib.tt_cuda_flow_accumulation_dev(P(o["acc"]), P(o["direction"]), None, dp, sp),
+            lambda: lib.tt_cuda_hillshade_fused_dev(P(o.get("hillshade")), P(d_dem), HS_AZ, HS_ALT,
+                                                    cs, dp, sp),
+        ]
+        for k, st in enumerate(stages):
+            if events is not None:
+                events[k].record(stream)
+            N.check(calls[k](), st)
+            if st in ("fillsinks", "gwdt"):
+                rounds[st] = int(lib.tt_cuda_last_rounds())
+        if events is not None:
+            events[-1].record(stream)
+
+    def pipe_step():
+        N.check(lib.tt_cuda_d8_pipeline_dev(
+            P(o["filled"]), P(o["flats"]), P(o["dist"]), P(o["node"]), P(o["direction"]),
+            P(o["acc"]), P(o.get("hillshade")), P(d_dem), P(d_bc), None, HS_AZ, HS_ALT, cs,
+            dp, sp), "d8_pipeline_dev")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(warmup):
+        step()
+    for _ in range(warmup):
+        pipe_step()
+    torch.cuda.synchronize()
+
+    stage_ms = {s: [] for s in stages}
+    step_ms, fn_ms = [], []
+    with (clocks if clocks is not None else ClockSampler(None, off=True)) as clk:
+        barrier()
+        lib.tt_cuda_launch_count(1)
+        for _ in range(steps):
+            flush.fill_(1.0)  # L2 flush outside the timed events
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            pipe_step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        launches = int(lib.tt_cuda_launch_count(1)) / steps
+        barrier()
+    # The same work as one call per reference function, timed per stage.
+    for _ in range(steps):
+        flush.fill_(1.0)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)]
+        step(ev)
+        torch.cuda.synchronize()
+        for k, st in enumerate(stages):
+            stage_ms[st].append(ev[k].elapsed_time(ev[k + 1]))
+        fn_ms.append(ev[0].elapsed_time(ev[-1]))
+    barrier()
+    ms = float(np.mean(step_ms))
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # End to end through the host-pointer C ABI: pinned host buffers, copies
+    # inside the timed region.
+    def pinned(dtype):
+        return torch.empty((n, m), dtype=dtype, pin_memory=True).numpy()
+
+    h_dem = pinned(torch.float32)
+    h_dem[:] = dem.T
+    h_bc = pinned(torch.uint8)
+    h_bc[:] = bc.T
+    outs = ["filled", "flats", "dist", "node", "direction", "acc"] + (["hillshade"] if hs else [])
+    h_out = {k: pinned(o[k].dtype) for k in outs}
+    hp = lambda a: N.C.c_void_p(a.ctypes.data)  # noqa: E731
+
+    def e2e_step():
+        lib.tt_cuda_d8_pipeline(hp(h_out["filled"]), hp(h_out["flats"]), hp(h_out["dist"]),
+                                hp(h_out["node"]), hp(h_out["direction"]), hp(h_out["acc"]),
+                                hp(h_dem), hp(h_bc), None, dp)
+        N.check(N.last_status(), "d8_pipeline")
+        if hs:
+            lib.tt_cuda_hillshade_fused(hp(h_out["hillshade"]), hp(h_dem), HS_AZ, HS_ALT, cs, dp)
+            N.check(N.last_status(), "hillshade_fused")
+
+    e2e_step()
+    e2e_ms = []
+    for _ in range(max(2, min(steps, 5))):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    h2d = cells * (4 + 1) + (cells * 4 if hs else 0)  # dem + bc (+ dem for hillshade)
+    d2h = sum(o[k].element_size() for k in outs) * cells
+    mean_stage = {st: float(np.mean(v)) for st, v in stage_ms.items()}
+    per_fn_ms = float(np.mean(fn_ms))
+    res = {
+        "workload": name, "config": workload_config(name, (m, n), hs, world),
+        "cells": cells, "ms": ms, "value": cells * world / (ms * 1e-3) / 1e9,
+        "launches": launches, "stages_ms": mean_stage, "device_rounds": rounds,
+        "per_function": {"ms_per_step": per_fn_ms,
+                         "value": cells * world / (per_fn_ms * 1e-3) / 1e9,
+                         "calls": "one tt_cuda_<name>_dev call per reference function"},
+        "e2e": {"value": cells * world / (float(np.mean(e2e_ms)) * 1e-3) / 1e9, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": float(np.mean(e2e_ms)),
+                "path": "tt_cuda_d8_pipeline" + (" + tt_cuda_hillshade_fused" if hs else "")
+                        + " (host pointers, pinned buffers)"},
+        "hillshade": hs,
+    }
+    keep_out = {"node": o["node"], "direction": o["direction"], "dem": dem, "bc": bc, "cs": cs}
+    return res, keep_out
+
+
+def roofline_of(res, name):
+    hbm, peak_kind = peaks()
+    st = res["stages_ms"]
+    dom = max(st, key=st.get)
+    achieved = BYTES[dom] * res["cells"] / (st[dom] * 1e-3) / 1e9
+    pipe_bytes = PIPELINE_BYTES + (BYTES["hillshade_fused"] if res["hillshade"] else 0)
+    pipe_gbs = pipe_bytes * res["cells"] / (res["ms"] * 1e-3) / 1e9
+    return ({"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+             "frac": achieved / hbm, "traffic": load_traffic().get(f"{name}:{dom}"),
+             "peak_source": peak_kind, "algorithmic_bytes_per_cell": BYTES[dom]},
+            {"bytes_per_cell": pipe_bytes, "ms": res["ms"], "achieved_gbs": pipe_gbs,
+             "frac": pipe_gbs / hbm, "peak_source": peak_kind})
 
 
 def main():
@@ -527,8 +752,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="plain_4096_hillshade", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="plain_16384", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-edges", action="store_true")
@@ -552,149 +778,28 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    from libtopotoolbox_gb300 import api
     from libtopotoolbox_gb300 import _native as N
 
-    lib = N.lib()
-    dem, bc, cs = make_workload(args.workload)
-    m, n = dem.shape
-    cells = m * n
-    # Device-resident inputs: column-major grid == (ncols, nrows) tensor.
-    d_dem = torch.from_numpy(np.ascontiguousarray(dem.T)).to(dev)
-    d_bc = torch.from_numpy(np.ascontiguousarray(bc.T)).to(dev)
-    o = {
-        "filled": torch.empty((n, m), dtype=torch.float32, device=dev),
-        "flats": torch.empty((n, m), dtype=torch.int32, device=dev),
-        "costs": torch.empty((n, m), dtype=torch.float32, device=dev),
-        "conncomps": torch.empty((n, m), dtype=torch.int64, device=dev),
-        "dist": torch.empty((n, m), dtype=torch.float32, device=dev),
-        "node": torch.empty((n, m), dtype=torch.int64, device=dev),
-        "direction": torch.empty((n, m), dtype=torch.uint8, device=dev),
-        "acc": torch.empty((n, m), dtype=torch.float32, device=dev),
-        "hillshade": torch.empty((n, m), dtype=torch.float32, device=dev),
-    }
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2
-    stream = torch.cuda.current_stream(dev)
-    sp = N.C.c_void_p(stream.cuda_stream)
-    dp, keep = N.dims_arg((m, n))
-    P = lambda t: N.C.c_void_p(t.data_ptr())  # noqa: E731
-
-    stages = ["fillsinks", "identifyflats", "gwdt_computecosts", "gwdt",
-              "flow_routing_d8_carve", "flow_accumulation", "hillshade_fused"]
-
-    def step(events=None):
-        calls = [
-            lambda: lib.tt_cuda_fillsinks_dev(P(o["filled"]), P(d_dem), P(d_bc), dp, sp),
-            lambda: lib.tt_cuda_identifyflats_dev(P(o["flats"]), P(o["filled"]), dp, None, sp),
-            lambda: lib.tt_cuda_gwdt_computecosts_dev(P(o["costs"]), P(o["conncomps"]),
-                                                      P(o["flats"]), P(d_dem), P(o["filled"]),
-                                                      dp, sp),
-            lambda: lib.tt_cuda_gwdt_dev(P(o["dist"]), None, P(o["costs"]), P(o["flats"]), dp, sp),
-            lambda: lib.tt_cuda_flow_routing_d8_carve_dev(P(o["node"]), P(o["direction"]),
-                                                          P(o["filled"]), P(o["dist"]),
-                                                          P(o["flats"]), dp, 0, sp),
-            lambda: lib.tt_cuda_flow_accumulation_dev(P(o["acc"]), P(o["direction"]), None, dp, sp),
-            lambda: lib.tt_cuda_hillshade_fused_dev(P(o["hillshade"]), P(d_dem), HS_AZ, HS_ALT,
-                                                    cs, dp, sp),
-        ]
-        for k, c in enumerate(calls):
-            if events is not None:
-                events[k].record(stream)
-            N.check(c(), stages[k])
-            if stages[k] in ("fillsinks", "gwdt"):
-                rounds[stages[k]] = int(lib.tt_cuda_last_rounds())
-        if events is not None:
-            events[-1].record(stream)
-
-    rounds = {}
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    # The headline step: the whole path through its fused entry point
-    # (tt_cuda_d8_pipeline_dev, hillshade included), which contracts the
-    # receiver forest once for both the node order and the accumulation.
-    def pipe_step():
-        N.check(lib.tt_cuda_d8_pipeline_dev(
-            P(o["filled"]), P(o["flats"]), P(o["dist"]), P(o["node"]), P(o["direction"]),
-            P(o["acc"]), P(o["hillshade"]), P(d_dem), P(d_bc), None, HS_AZ, HS_ALT, cs,
-            dp, sp), "d8_pipeline_dev")
-
-    for _ in range(args.warmup):
-        pipe_step()
-    torch.cuda.synchronize()
-
-    stage_ms = {s: [] for s in stages}
-    step_ms, fn_ms = [], []
-    with ClockSampler(local) as clk:
-        barrier()
-        lib.tt_cuda_launch_count(1)
-        for _ in range(args.steps):
-            flush.fill_(1.0)  # L2 flush outside the timed events
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            pipe_step()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-        launches = int(lib.tt_cuda_launch_count(1)) / args.steps
-        barrier()
-        # The same work as one call per reference function, timed per stage.
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)]
-            step(ev)
-            torch.cuda.synchronize()
-            for k, s in enumerate(stages):
-                stage_ms[s].append(ev[k].elapsed_time(ev[k + 1]))
-            fn_ms.append(ev[0].elapsed_time(ev[-1]))
-        barrier()
-    ms = float(np.mean(step_ms))
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cells * world / (ms * 1e-3) / 1e9
-
-    # End-to-end through the host-pointer C ABI: pinned host buffers, copies
-    # inside the timed region.
-    def pinned(shape, dtype):
-        t = torch.empty(shape, dtype=dtype, pin_memory=True)
-        return t.numpy()
-
-    h_dem = pinned((n, m), torch.float32)
-    h_dem[:] = dem.T
-    h_bc = pinned((n, m), torch.uint8)
-    h_bc[:] = bc.T
-    h_out = {k: pinned((n, m), t.dtype) for k, t in o.items()
-             if k in ("filled", "flats", "dist", "node", "direction", "acc", "hillshade")}
-    hp = lambda a: N.C.c_void_p(a.ctypes.data)  # noqa: E731
-
-    def e2e_step():
-        lib.tt_cuda_d8_pipeline(hp(h_out["filled"]), hp(h_out["flats"]), hp(h_out["dist"]),
-                                hp(h_out["node"]), hp(h_out["direction"]), hp(h_out["acc"]),
-                                hp(h_dem), hp(h_bc), None, dp)
-        N.check(N.last_status(), "d8_pipeline")
-        lib.tt_cuda_hillshade_fused(hp(h_out["hillshade"]), hp(h_dem), HS_AZ, HS_ALT, cs, dp)
-        N.check(N.last_status(), "hillshade_fused")
-
-    e2e_step()
-    e2e_ms = []
-    for _ in range(max(2, min(args.steps, 5))):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    h2d = cells * (4 + 1) + cells * 4  # dem + bc for the pipeline, dem for hillshade
-    d2h = cells * (4 + 4 + 4 + 8 + 1 + 4 + 4)
-    e2e_val = cells * world / (float(np.mean(e2e_ms)) * 1e-3) / 1e9
-
+    N.lib()
+    clk = ClockSampler(local)
+    head, out = gpu_pipeline_leg(N, dev, args.workload, args.steps, args.warmup, world, dist,
+                                 clocks=clk)
+    torch.cuda.empty_cache()
+    cpu_threads = {}
+    if rank == 0 and not args.no_cpu_baseline:
+        # Whole-DEM CPU runs of the headline (and secondary) workload, one
+        # host thread each, beside the remaining GPU legs.
+        cpu_threads["head"] = CpuPipeline(out["dem"], out["bc"], out["cs"], head["hillshade"])
+        cpu_threads["head"].start()
+    secondary = None
+    sec_out = None
+    if not args.no_secondary and args.workload != SECONDARY:
+        secondary, sec_out = gpu_pipeline_leg(N, dev, SECONDARY, args.steps, args.warmup,
+                                              world, dist)
+        if rank == 0 and not args.no_cpu_baseline:
+            cpu_threads["secondary"] = CpuPipeline(sec_out["dem"], sec_out["bc"], sec_out["cs"],
+                                                   secondary["hillshade"])
+            cpu_threads["secondary"].start()
     # The batched leg runs on every rank (each on its share of the DEMs).
     batched = None if args.no_batch else batch_leg(dev, rank=rank, world=world, dist=dist)
 
@@ -703,56 +808,43 @@ def main():
             dist.destroy_process_group()
         return 0
 
-    hbm, peak_kind = peaks()
-    # Dominant stage by time.
-    mean_stage = {s: float(np.mean(v)) for s, v in stage_ms.items()}
-    dom = max(mean_stage, key=mean_stage.get)
-    dom_bytes = BYTES[dom] * cells
-    achieved = dom_bytes / (mean_stage[dom] * 1e-3) / 1e9
-    traffic = load_traffic().get(f"{args.workload}:{dom}")
-    pipe_bytes = PIPELINE_BYTES + BYTES["hillshade_fused"]
-    pipe_gbs = pipe_bytes * cells / (ms * 1e-3) / 1e9
-    per_fn_ms = float(np.mean(fn_ms))
+    roof, pipe_roof = roofline_of(head, args.workload)
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "dem": f"{m}x{n} float32 column-major",
-                   "weights": "unit", "hillshade": "azimuth 315, altitude 60",
-                   "l2": "flushed (512 MiB write) between timed steps",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_cell": BYTES[dom]},
-        "step": "tt_cuda_d8_pipeline_dev (fill, flats, costs, gwdt, carve, "
-                "accumulation, hillshade) on device-resident inputs",
-        "pipeline_roofline": {"bytes_per_cell": pipe_bytes, "ms": ms,
-                              "achieved_gbs": pipe_gbs, "frac": pipe_gbs / hbm},
-        "per_function": {"ms_per_step": per_fn_ms,
-                         "value": cells * world / (per_fn_ms * 1e-3) / 1e9,
-                         "calls": "one tt_cuda_<name>_dev call per reference function"},
-        "stages_ms": mean_stage,
-        "device_rounds": rounds,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": float(np.mean(e2e_ms)),
-                "path": "tt_cuda_d8_pipeline + tt_cuda_hillshade_fused (host pointers)"},
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "data": "synthetic", "config": head["config"], "roofline": roof,
+        "step": "tt_cuda_d8_pipeline_dev (fill, flats, costs, gwdt, carve, accumulation"
+                + (", hillshade" if head["hillshade"] else "") + ") on device-resident inputs",
+        "pipeline_roofline": pipe_roof, "per_function": head["per_function"],
+        "stages_ms": head["stages_ms"], "device_rounds": head["device_rounds"],
+        "e2e": head["e2e"], "gpu_launches": head["launches"], "clocks": clk.summary(),
     }
+    small = sec_out if sec_out is not None else out
     if not args.no_adjoint:
         line["adjoint"] = adjoint_leg(dev)
     if batched is not None:
         line["batched"] = batched
     if not args.no_edges:
-        line["edges"] = edges_leg(dev, o["node"], o["direction"])
+        line["edges"] = edges_leg(dev, small["node"], small["direction"])
     if not args.no_graphflood:
-        line["graphflood"] = graphflood_leg(dem, cs)
+        line["graphflood"] = graphflood_leg(small["dem"], small["cs"])
     if not args.no_io:
-        line["io"] = io_leg(dem)
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(dem, bc)
+        line["io"] = io_leg(small["dem"])
+    if secondary is not None:
+        sroof, spipe = roofline_of(secondary, SECONDARY)
+        secondary.update({"roofline": sroof, "pipeline_roofline": spipe})
+        if "secondary" in cpu_threads:
+            secondary["cpu_same_config"] = cpu_threads["secondary"].result(
+                "same workload and config as this leg")
+            cv = secondary["cpu_same_config"]["value"]
+            if cv:
+                secondary["speedup_vs_cpu"] = {"device_resident": secondary["value"] / cv,
+                                               "e2e": secondary["e2e"]["value"] / cv}
+        line["secondary"] = secondary
+    if "head" in cpu_threads:
+        line["cpu_baseline"] = cpu_threads["head"].result(
+            "same workload and config as the headline")
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

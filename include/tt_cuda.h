@@ -341,8 +341,12 @@ TT_CUDA_API tt_cuda_status tt_cuda_write_file_dev(const char *path, int64_t offs
  *  array's device address (cudaGetSymbolAddress) with that device current;
  *  make that first call before any stream capture.  All calls share the
  *  array: each call re-initialises it, and calls that overlap on the GPU
- *  (other streams, other threads on the same device) race on it.  The call
- *  synchronises `stream` before it returns. */
+ *  (other streams, other threads on the same device) race on it.  The
+ *  address looked up on the first call is kept for the life of the process:
+ *  do not call this after a cudaDeviceReset of that device.  The fill's
+ *  persistent kernel is a cooperative launch, so all of its blocks run at
+ *  once even beside other work on the device.  The call synchronises
+ *  `stream` before it returns. */
 TT_CUDA_API tt_cuda_status tt_cuda_fillsinks_noalloc_dev(
     float *output, const float *dem, const uint8_t *bc,
     const ptrdiff_t dims[2], void *stream);

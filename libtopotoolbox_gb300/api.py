@@ -95,6 +95,18 @@ def reconstruct(marker, mask):
     return mk
 
 
+def reconstruct_hybrid(marker, mask):
+    """(reconstructed marker, flag) of include/topotoolbox.h:1070; the flag
+    is 1 when the reconstruction did not converge (the input is not
+    modified)."""
+    mk = np.array(marker, dtype=np.float32, order="F", copy=True)
+    mask = _f32(mask)
+    dp, keep = N.dims_arg(_dims(mask))
+    flag = N.lib().tt_cuda_reconstruct_hybrid(_ptr(mk), None, _ptr(mask), dp)
+    _after("reconstruct_hybrid")
+    return mk, int(flag)
+
+
 def identifyflats(dem):
     """(flags, count): bit 0 flat, bit 1 sill, bit 2 presill
     (include/topotoolbox.h:405, src/identifyflats.c:33-121)."""
@@ -349,6 +361,14 @@ class dev:  # namespace
         N.check(N.lib().tt_cuda_fillsinks_dev(dev._p(out), dev._p(dem), dev._p(bc), dp,
                                               dev._stream()), "fillsinks_dev")
         return out
+
+    @staticmethod
+    def reconstruct(marker, mask):
+        """Reconstructs `marker` under `mask` in place and returns it."""
+        dp, keep = N.dims_arg(dev._dims(mask))
+        N.check(N.lib().tt_cuda_reconstruct_dev(dev._p(marker), dev._p(mask), dp,
+                                                dev._stream()), "reconstruct_dev")
+        return marker
 
     @staticmethod
     def identifyflats(dem, out=None):

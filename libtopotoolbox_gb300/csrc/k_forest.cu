@@ -21,11 +21,22 @@
 //     inflow and repeats the in-tile walk to produce every pixel's total.
 //
 // Sums are exact: weights are converted to 64-bit fixed point with a
-// power-of-two scale chosen from max|w| * N so no partial sum can overflow,
-// and integer addition is associative, so the result is independent of the
-// order of the walk and identical from run to run (no float atomics).  Unit
-// weights use scale 1 (exact pixel counts).  Each total is rounded once to
-// float32.
+// power-of-two scale 2^k1 chosen from max|w| * N so no partial sum can
+// overflow, and integer addition is associative, so the result is
+// independent of the order of the walk and identical from run to run (no
+// float atomics).  Unit weights use scale 1 (exact pixel counts).  Each
+// total is rounded once to float32.
+//
+// One scale bounds the rounding of every weight by 2^-(k1+1) in absolute
+// terms, which is too coarse for weights far below max|w| (a 1e-6 headwater
+// weight beside unit weights on 2.7e8 pixels).  When the smallest nonzero
+// |w| asks for a finer scale, the same contraction runs again at scales
+// k1 + d, k1 + 2d, ... with sums taken modulo 2^64 (wrapping integer adds are
+// still exact and associative).  Pass i's total X_i differs from
+// 2^d * X_(i-1) by less than N * 2^d <= 2^61 units, so the 64-bit residue of
+// X_i and that of X_(i-1) determine X_i exactly; the finest total, rebuilt
+// from the exact first total and the per-pass corrections in double-double,
+// is rounded once to float32.
 //
 // The node order sorts pixels by the length of their longest upstream path
 // h (0 at sources): a receiver's h exceeds each donor's, so ascending h is a
@@ -91,6 +102,7 @@ struct UpArgs {
   int *elist;       // per exit id: the exit's pixel
   int *ecount;
   float *acc_out;
+  long long *raw_out;  // when set: the fixed-point totals instead of acc_out
   int *count_out;  // unit weights: the exact count as int (or nullptr)
   int *h_out;
   int *hmax;
@@ -111,13 +123,13 @@ __device__ __forceinline__ long long to_fixed(float w, int k, int *err) {
     mant |= 0x800000u;
   int sh = e - 150 + k;  // value = mant * 2^(e-150)
   long long v;
-  if (sh >= 0)
-    v = sh < 39 ? ((long long)mant << sh) : 0;
+  if (sh >= 0)  // modulo 2^64 (a multiple of 2^64 is 0) at the finer scales
+    v = sh < 64 ? (long long)((unsigned long long)mant << sh) : 0;
   else if (sh > -40)
     v = ((long long)mant + (1LL << (-sh - 1))) >> (-sh);
   else
     v = 0;
-  return (bits >> 31) ? -v : v;
+  return (bits >> 31) ? (long long)(0ULL - (unsigned long long)v) : v;
 }
 
 // Receiver code of tile pixel (ii, jj).
@@ -379,6 +391,8 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
       const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
       if (a.want_acc && a.count_out) {
         a.count_out[gp] = (int)t.acc[e];
+      } else if (a.want_acc && a.raw_out) {
+        a.raw_out[gp] = t.acc[e];
       } else if (a.want_acc) {
         const float v = __ll2float_rn(t.acc[e]);
         a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
@@ -792,16 +806,66 @@ __global__ void down_jump_kernel(const int *__restrict__ ecount,
   if (__any_sync(__activemask(), act) && (threadIdx.x & 31) == 0) atomicAdd(active, 1);
 }
 
-__global__ void maxabs_kernel(const float *__restrict__ w, int64_t N,
-                              unsigned *__restrict__ out) {
-  unsigned mx = 0;
+// out[0] = bits of the largest |w| (NaN/INF sort above every finite
+// value), out[1] = bits of the smallest nonzero |w| (start: all ones).
+__global__ void weight_range_kernel(const float *__restrict__ w, int64_t N,
+                                    unsigned *__restrict__ out) {
+  unsigned mx = 0, mn = 0xffffffffu;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
-    unsigned b = __float_as_uint(w[p]) & 0x7fffffffu;
-    if (b > mx) mx = b;  // NaN/INF sort above every finite value
+    const unsigned b = __float_as_uint(w[p]) & 0x7fffffffu;
+    mx = max(mx, b);
+    if (b) mn = min(mn, b);
   }
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, mx);
+    atomicMin(out + 1, mn);
+  }
+}
+
+// Two-sum of doubles (Knuth): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = __dadd_rn(a, b);
+  const double bb = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
+// Adds the integer x * 2^-k to the double-double (hi, lo): x is split into
+// 32-bit halves, each exact in a double.
+__device__ __forceinline__ void dd_add_scaled(double &hi, double &lo, long long x, int k) {
+  const double a = ldexp((double)(x >> 32), 32 - k);  // exact: |x >> 32| < 2^32
+  const double b = ldexp((double)(unsigned)(x & 0xffffffffLL), -k);
+  double s, e;
+  two_sum(hi, a, s, e);
+  lo = __dadd_rn(lo, e);
+  two_sum(s, b, hi, e);
+  lo = __dadd_rn(lo, e);
+}
+
+// Float totals from the fixed-point residues of `passes` contractions at
+// scales k1, k1 + d, ...: X_1 = R_0 exactly, and pass i adds the
+// correction delta_i = R_i - (R_(i-1) << d) (mod 2^64, signed) at scale
+// 2^-(k1 + i d).
+__global__ void combine_passes_kernel(float *__restrict__ acc, const long long *__restrict__ R,
+                                      int passes, int64_t N, int k1, int d) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    long long prev = R[p];
+    double hi = 0.0, lo = 0.0;
+    dd_add_scaled(hi, lo, prev, k1);
+    for (int i = 1; i < passes; i++) {
+      const long long r = R[(int64_t)i * N + p];
+      const long long delta = (long long)((unsigned long long)r -
+                                          ((unsigned long long)prev << d));
+      dd_add_scaled(hi, lo, delta, k1 + i * d);
+      prev = r;
+    }
+    acc[p] = __double2float_rn(__dadd_rn(hi, lo));
+  }
 }
 
 int list_grid(int64_t n) {
@@ -817,11 +881,12 @@ struct UpWork {
   uint8_t *emask;
   int2 *link;
   int *xmap, *xsteps, *elist, *leaves, *h;
-  int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err, [5] maxabs
+  long long *raw;  // passes * N fixed-point totals (multi-scale sums only)
+  int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err
 };
 
 tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
-                        UpWork &w) {
+                        UpWork &w, int raw_passes = 0) {
   const size_t N = (size_t)g.cells();
   Workspace &ws = workspace();
   // Exits are ring pixels: at most 124 per tile.
@@ -829,7 +894,8 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
   size_t need = 256 + align_up(N * sizeof(CoarseCell)) + align_up(E * sizeof(CoarseCell)) +
                 align_up(E * 8) + 2 * align_up(E * 4) + 2 * align_up(N * 4) +
                 (want_acc ? align_up(N * 8) : 0) + (want_h ? align_up(N * 4) : 0) +
-                align_up(N * 2) + align_up((size_t)g.tiles() * kRing) + 4096;
+                align_up(N * 2) + align_up((size_t)g.tiles() * kRing) +
+                (size_t)raw_passes * align_up(N * 8) + 4096;
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   w.counters = (int *)ws.take(256);
   w.cell = (CoarseCell *)ws.take(N * sizeof(CoarseCell));
@@ -843,6 +909,7 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
   w.xsteps = (int *)ws.take(N * 4);
   w.elist = (int *)ws.take(E * 4);
   w.leaves = (int *)ws.take(E * 4);
+  w.raw = raw_passes ? (long long *)ws.take((size_t)raw_passes * N * 8) : nullptr;
   return TT_CUDA_SUCCESS;
 }
 
@@ -850,7 +917,7 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
 tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
                       const GridDims &g, unsigned order, bool want_acc,
                       bool want_h, float *acc_out, UpWork &w, cudaStream_t st,
-                      int *count_out = nullptr) {
+                      int *count_out = nullptr, long long *raw_out = nullptr) {
   const int T = g.tiles();
   TT_CHECK(cudaMemsetAsync(w.counters, 0, 256, st));
   UpArgs a{};
@@ -875,6 +942,7 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.elist = w.elist;
   a.ecount = w.counters + 0;
   a.acc_out = acc_out;
+  a.raw_out = raw_out;
   a.count_out = count_out;
   a.h_out = w.h;
   a.hmax = w.counters + 3;
@@ -941,29 +1009,75 @@ tt_cuda_status count_dev(int *count, const uint8_t *dir, const GridDims &g, cuda
 
 namespace {
 
-// Fixed-point shift for weighted sums: the largest |w| times the pixel count
-// must stay below 2^62.  Unit weights (nullptr) need none.
-tt_cuda_status weight_shift(const float *weights, const GridDims &g, UpWork &w,
-                            cudaStream_t st, int *wshift) {
-  *wshift = 0;
+// Fixed-point scales of a weighted sum.  The first pass uses 2^k1 with
+// max|w| * N * 2^k1 <= 2^62, so no partial sum overflows.  Rounding a weight
+// to that grid costs at most 2^-(k1+1), so a total over weights of one sign
+// is within 2^-(k1+1) / min|w| of exact, relative; when that exceeds
+// kRelTarget the contraction is repeated at k1 + d, k1 + 2d, ... (at most
+// kMaxPasses scales) with d = 61 - ceil(log2 N), which keeps every pass's
+// total within 2^61 units of 2^d times the previous one.
+constexpr double kRelTarget = 1e-7;
+constexpr int kMaxPasses = 4;
+struct WeightPlan {
+  int k1 = 0;      // scale of the first pass
+  int d = 0;       // scale step between passes
+  int passes = 1;  // contractions to run
+};
+
+tt_cuda_status weight_plan(const float *weights, const GridDims &g, cudaStream_t st,
+                           WeightPlan *plan) {
+  *plan = WeightPlan{};
   if (!weights) return TT_CUDA_SUCCESS;
-  unsigned *mx = (unsigned *)(w.counters + 5);
-  TT_CHECK(cudaMemsetAsync(mx, 0, 4, st));
-  TT_LAUNCH(maxabs_kernel, list_grid(g.cells()), 256, 0, st, weights, g.cells(), mx);
+  Workspace &ws = workspace();
+  if (!ws.reserve(256)) return TT_CUDA_ERR_ALLOC;
+  unsigned *rng = (unsigned *)ws.take(256);
+  TT_CHECK(cudaMemsetAsync(rng, 0, 4, st));
+  TT_CHECK(cudaMemsetAsync(rng + 1, 0xff, 4, st));
+  TT_LAUNCH(weight_range_kernel, list_grid(g.cells()), 256, 0, st, weights, g.cells(), rng);
   unsigned *h = (unsigned *)pinned_scratch();
   if (!h) return TT_CUDA_ERR_ALLOC;
-  TT_CHECK(cudaMemcpyAsync(h, mx, 4, cudaMemcpyDeviceToHost, st));
+  TT_CHECK(cudaMemcpyAsync(h, rng, 8, cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
-  unsigned bits = *h;
-  float mxv;
-  std::memcpy(&mxv, &bits, 4);
-  if (bits >= 0x7f800000u) mxv = 0.0f;  // non-finite weights are flagged per pixel
-  if (mxv > 0.0f) {
-    double bound = (double)mxv * (double)g.cells();
-    int e = (int)std::ceil(std::log2(bound));
-    *wshift = 62 - e;
-  }
+  float mxv, mnv;
+  std::memcpy(&mxv, &h[0], 4);
+  std::memcpy(&mnv, &h[1], 4);
+  if (h[0] >= 0x7f800000u) return TT_CUDA_SUCCESS;  // non-finite: flagged per pixel
+  if (!(mxv > 0.0f)) return TT_CUDA_SUCCESS;        // all weights zero
+  const double N = (double)g.cells();
+  plan->k1 = 62 - (int)std::ceil(std::log2((double)mxv * N));
+  plan->d = 61 - (int)std::ceil(std::log2(std::max(N, 2.0)));
+  const double need = std::ceil(std::log2(0.5 / ((double)mnv * kRelTarget)));
+  if (need > plan->k1 && plan->d > 0)
+    plan->passes = std::min(kMaxPasses,
+                            1 + (int)std::ceil((need - plan->k1) / (double)plan->d));
   return TT_CUDA_SUCCESS;
+}
+
+// Weighted (or unit) accumulation into `acc` following `plan`; `want_h`
+// also leaves the subtree heights of the first pass in w.h and their
+// maximum in h6[3].  w must come from up_alloc with plan.passes raw slots
+// when plan.passes > 1.
+tt_cuda_status accumulate_planned(float *acc, const uint8_t *dir, const float *weights,
+                                  const WeightPlan &plan, const GridDims &g, bool want_h,
+                                  UpWork &w, cudaStream_t st, int h6[6]) {
+  if (plan.passes == 1) {
+    TT_TRY_STATUS(up_run(dir, weights, plan.k1, g, 0, true, want_h, acc, w, st));
+    return up_status(w, st, h6);
+  }
+  const int64_t N = g.cells();
+  tt_cuda_status first = TT_CUDA_SUCCESS;
+  for (int p = 0; p < plan.passes; p++) {
+    TT_TRY_STATUS(up_run(dir, weights, plan.k1 + p * plan.d, g, 0, true, want_h && p == 0,
+                         nullptr, w, st, nullptr, w.raw + (size_t)p * N));
+    if (p == 0) {  // later passes walk the same forest
+      first = up_status(w, st, h6);
+      if (first == TT_CUDA_ERR_CYCLE) return first;
+    }
+  }
+  TT_LAUNCH(combine_passes_kernel, list_grid(N), 256, 0, st, acc, w.raw, plan.passes, N,
+            plan.k1, plan.d);
+  TT_CHECK(cudaGetLastError());
+  return first;
 }
 
 // Node order from the subtree heights of a finished up_run: pixels sorted
@@ -990,13 +1104,12 @@ tt_cuda_status node_scatter(ptrdiff_t *node, UpWork &w, const int h6[6], const G
 tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,
                               cudaStream_t st) {
+  WeightPlan plan;
+  TT_TRY_STATUS(weight_plan(weights, g, st, &plan));
   UpWork w;
-  TT_TRY_STATUS(up_alloc(g, true, false, w));
-  int wshift = 0;
-  TT_TRY_STATUS(weight_shift(weights, g, w, st, &wshift));
-  TT_TRY_STATUS(up_run(dir, weights, wshift, g, 0, true, false, acc, w, st));
+  TT_TRY_STATUS(up_alloc(g, true, false, w, plan.passes > 1 ? plan.passes : 0));
   int h6[6];
-  return up_status(w, st, h6);
+  return accumulate_planned(acc, dir, weights, plan, g, false, w, st, h6);
 }
 
 tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
@@ -1019,13 +1132,12 @@ tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *di
                                   const float *weights, const GridDims &g,
                                   cudaStream_t st, tt_cuda_status (*acc_done)(void *),
                                   void *ctx) {
+  WeightPlan plan;
+  TT_TRY_STATUS(weight_plan(weights, g, st, &plan));
   UpWork w;
-  TT_TRY_STATUS(up_alloc(g, true, true, w));
-  int wshift = 0;
-  TT_TRY_STATUS(weight_shift(weights, g, w, st, &wshift));
-  TT_TRY_STATUS(up_run(dir, weights, wshift, g, 0, true, true, acc, w, st));
+  TT_TRY_STATUS(up_alloc(g, true, true, w, plan.passes > 1 ? plan.passes : 0));
   int h6[6];
-  tt_cuda_status s = up_status(w, st, h6);
+  tt_cuda_status s = accumulate_planned(acc, dir, weights, plan, g, true, w, st, h6);
   if (s == TT_CUDA_ERR_CYCLE) return s;
   if (acc_done) TT_TRY_STATUS(acc_done(ctx));  // acc is complete on `st` here
   TT_TRY_STATUS(node_scatter(node, w, h6, g, st));

@@ -671,6 +671,27 @@ int elementwise_grid(int64_t N) {
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
+// Launches the persistent relaxation as a cooperative kernel: every block
+// of the grid is resident at once or the launch is refused
+// (cudaErrorCooperativeLaunchTooLarge), so no warp waits for a block that
+// cannot be scheduled -- for example while other work holds some SMs.  The
+// grid never exceeds the occupancy bound computed for this kernel.
+template <int KIND>
+cudaError_t launch_relax(int grid, const RelaxArgs &ra, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kWarps * 32);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  note_launch();
+  return cudaLaunchKernelEx(&cfg, relax_persistent_kernel<KIND>, ra);
+}
+
 // Host driver: mark the starting tiles, run one persistent launch, read the
 // status.  `bc` (sink filling only) selects the seeded start: the fill's
 // initial state is written here and only tiles next to a seed start dirty;
@@ -718,7 +739,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   int grid = sm_count() * blocks_per_sm[KIND];
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
-  TT_LAUNCH(relax_persistent_kernel<KIND>, grid, kWarps * 32, 0, st, ra);
+  TT_CHECK(launch_relax<KIND>(grid, ra, st));
   if (KIND == GWDT)
     TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
@@ -780,7 +801,10 @@ tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
 // per 32 x 32 tile -- lives in the file-scope array below, sized for
 // kNoAllocMaxTiles tiles; every device that loads this library holds it
 // until the process exits.  All calls share it: each call clears what must
-// start at zero, and calls that overlap on the GPU race on it.
+// start at zero, and calls that overlap on the GPU race on it.  The array's
+// device address is looked up once per device and kept; a caller that
+// resets the device (cudaDeviceReset, which unloads this module) must not
+// call this entry point afterwards in the same process.
 // ------------------------------------------------------------------
 constexpr int kNoAllocMaxTiles = 65536;  // e.g. 8192 x 8192 pixels
 constexpr int kNoAllocHeaderWords = 64;  // control block, padded to 256 bytes
@@ -834,8 +858,7 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   int grid = sm_count() * (b > 0 ? b : 1);
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
-  TT_LAUNCH(relax_persistent_kernel<FILL>, grid, kWarps * 32, 0, st, ra);
-  TT_CHECK(cudaGetLastError());
+  TT_CHECK(launch_relax<FILL>(grid, ra, st));
   QueueCtl h;  // read back into host stack memory: no pinned allocation
   TT_CHECK(cudaMemcpyAsync(&h, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));

@@ -24,7 +24,6 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libtopotoolbox_ref.so"
-REF_ROOT = Path(os.environ.get("TT_REFERENCE_ROOT", "/root/reference"))
 
 P = C.c_void_p
 PD = C.POINTER(C.c_int64)
@@ -37,10 +36,22 @@ def build_port() -> Path:
     return PORT_LIB
 
 
-def build_ref() -> Path | None:
-    if not (REF_ROOT / "src" / "fillsinks.c").exists():
+def reference_root(root=None) -> Path | None:
+    """The reference checkout: `root`, else $TT_REFERENCE_ROOT; None when
+    neither names a directory holding the reference's sources."""
+    root = root or os.environ.get("TT_REFERENCE_ROOT")
+    if not root or not (Path(root) / "src" / "fillsinks.c").exists():
         return None
-    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+    return Path(root)
+
+
+def build_ref(root=None) -> Path | None:
+    """Compile the reference's hot-path sources (in place, read-only) into
+    oracle/_ref/; None when no reference checkout is given or present."""
+    ref_root = reference_root(root)
+    if ref_root is None:
+        return REF_LIB if REF_LIB.exists() else None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={ref_root}"], check=True)
     return REF_LIB
 
 
@@ -77,6 +88,8 @@ class Oracle:
         sig = {
             "fillsinks": (None, [P, P, P, PD]),
             "fillsinks_hybrid": (C.c_int if kind == "port" else None, [P, P, P, P, PD]),
+            "reconstruct": (None, [P, P, PD]),
+            "reconstruct_hybrid": (C.c_int, [P, P, P, PD]),
             "identifyflats": (C.c_int64, [P, P, PD]),
             "gwdt_computecosts": (None, [P, P, P, P, P, PD]),
             "gwdt": (None, [P, P, P, P, P, P, PD]),
@@ -127,6 +140,23 @@ class Oracle:
         dp, k = _dims(dem.shape)
         self.fn["fillsinks_hybrid"](_ptr(out), _ptr(q), _ptr(dem), _ptr(bc), dp)
         return out
+
+    def reconstruct(self, marker, mask):
+        """Reconstructed marker (src/reconstruct.c:270-278); inputs untouched."""
+        mk = np.array(marker, dtype=np.float32, order="F", copy=True)
+        mask = np.array(mask, dtype=np.float32, order="F", copy=True)
+        dp, k = _dims(mk.shape)
+        self.fn["reconstruct"](_ptr(mk), _ptr(mask), dp)
+        return mk
+
+    def reconstruct_hybrid(self, marker, mask):
+        """(reconstructed marker, flag) of src/reconstruct.c:291-312."""
+        mk = np.array(marker, dtype=np.float32, order="F", copy=True)
+        mask = np.array(mask, dtype=np.float32, order="F", copy=True)
+        q = np.empty(mk.shape, dtype=np.int64, order="F")
+        dp, k = _dims(mk.shape)
+        flag = self.fn["reconstruct_hybrid"](_ptr(mk), _ptr(q), _ptr(mask), dp)
+        return mk, int(flag)
 
     def identifyflats(self, dem):
         dem = _f32(dem)
@@ -306,6 +336,26 @@ class Oracle:
             self.fn["compute_weighted_drainage_area_single_flow"](
                 _ptr(out), _ptr(w), _ptr(rcv), _ptr(stack), C.cast(dim, P), float(dx))
         return out.reshape(shape)
+
+    def run_pipeline(self, dem, bc, hillshade=None):
+        """The pipeline of `pipeline` (hybrid fill) for timing: every
+        intermediate is dropped as soon as the next stage has read it, so a
+        16384 x 16384 run peaks near 35 bytes per pixel.  `hillshade`
+        (azimuth, altitude, cellsize) adds hillshade_fused of `dem`.
+        Returns the accumulation."""
+        filled = self.fillsinks_hybrid(dem, bc)
+        flats, _ = self.identifyflats(filled)
+        costs, cc = self.gwdt_computecosts(flats, dem, filled)
+        del cc
+        dist = self.gwdt(costs, flats, want_prev=False)
+        del costs
+        node, direction = self.flow_routing_d8_carve(filled, dist, flats, 0)
+        del filled, dist, flats
+        acc = self.flow_accumulation(node, direction)
+        del node, direction
+        if hillshade is not None:
+            self.hillshade_fused(dem, *hillshade)
+        return acc
 
     def pipeline(self, dem, bc, weights=None, hybrid=True):
         """fill -> flats -> costs -> gwdt -> carve -> accumulation, the call

@@ -156,6 +156,50 @@ int orc_fillsinks_hybrid(float *output, ptrdiff_t *queue, const float *dem,
   return (scans == 2) && repeat;
 }
 
+/* Grayscale reconstruction by dilation, src/reconstruct.c:270-278 and
+ * :291-312.  Its update marker = min(mask, max(marker, causal neighbours))
+ * is the negation of the fill's update above with f = -marker and
+ * dem = -mask, NaN comparisons included (fminf/fmaxf and `<` are symmetric
+ * under negation), and so are the queue tests of the backward scan
+ * (:179-196) and of the propagation (:207-251).  The scans therefore run on
+ * negated copies; only the sign of a zero may differ. */
+static void negate_copy(float *dst, const float *src, ptrdiff_t n) {
+  for (ptrdiff_t p = 0; p < n; p++) dst[p] = -src[p];
+}
+
+void orc_reconstruct(float *marker, const float *mask, const ptrdiff_t dims[2]) {
+  const ptrdiff_t n = dims[0] * dims[1];
+  float *z = (float *)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
+  negate_copy(z, mask, n);
+  negate_copy(marker, marker, n);
+  ptrdiff_t changed = n;
+  for (int it = 0; it < 1000 && changed > 0; it++) {
+    changed = fill_scan(marker, z, dims, +1, NULL);
+    changed += fill_scan(marker, z, dims, -1, NULL);
+  }
+  negate_copy(marker, marker, n);
+  free(z);
+}
+
+int orc_reconstruct_hybrid(float *marker, ptrdiff_t *queue, const float *mask,
+                           const ptrdiff_t dims[2]) {
+  const ptrdiff_t n = dims[0] * dims[1];
+  float *z = (float *)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
+  negate_copy(z, mask, n);
+  negate_copy(marker, marker, n);
+  orc_fifo q = {queue, n, 0, 0};
+  int scans = 0, repeat = 0;
+  do {
+    fill_scan(marker, z, dims, +1, NULL);
+    repeat = (fill_scan(marker, z, dims, -1, &q) == -1);
+    repeat |= fill_propagate(marker, z, dims, &q);
+    scans++;
+  } while (repeat && scans < 2);
+  negate_copy(marker, marker, n);
+  free(z);
+  return (scans == 2) && repeat;
+}
+
 /* ------------------------------------------------------------------ */
 /* Flats, sills and presills (src/identifyflats.c:33-121)              */
 /* ------------------------------------------------------------------ */

@@ -28,6 +28,11 @@ void orc_fillsinks(float *output, const float *dem, const uint8_t *bc,
  * Returns 1 when the queue overflowed on the last allowed scan. */
 int orc_fillsinks_hybrid(float *output, ptrdiff_t *queue, const float *dem,
                          const uint8_t *bc, const ptrdiff_t dims[2]);
+/* src/reconstruct.c:270-278: `marker` reconstructed under `mask` in place. */
+void orc_reconstruct(float *marker, const float *mask, const ptrdiff_t dims[2]);
+/* src/reconstruct.c:291-312; returns 1 if the queue overflowed twice. */
+int orc_reconstruct_hybrid(float *marker, ptrdiff_t *queue, const float *mask,
+                           const ptrdiff_t dims[2]);
 /* src/identifyflats.c:33-121 */
 ptrdiff_t orc_identifyflats(int32_t *output, const float *dem,
                             const ptrdiff_t dims[2]);

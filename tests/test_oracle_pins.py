@@ -15,7 +15,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import same_float, topo_positions_ok
+from conftest import reconstruct_cases, same_float, topo_positions_ok
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
@@ -201,3 +201,19 @@ def test_port_sfgraph_equals_reference(port, ref, idx, d8):
                                                                      weights),
                               ref.compute_drainage_area_single_flow(rcv, stack, topo.shape, 30.0,
                                                                     weights)), name
+
+
+RECON = reconstruct_cases()
+
+
+@pytest.mark.parametrize("idx", range(len(RECON)))
+def test_port_reconstruct_equals_reference(port, ref, idx):
+    """Grayscale reconstruction with arbitrary markers (src/reconstruct.c:270-312)."""
+    name, marker, mask = RECON[idx]
+    assert same_float(port.reconstruct(marker, mask), ref.reconstruct(marker, mask)), name
+    a, fa = port.reconstruct_hybrid(marker, mask)
+    b, fb = ref.reconstruct_hybrid(marker, mask)
+    assert same_float(a, b), name
+    assert fa == fb == 0, name
+    # both forms reach the same fixpoint
+    assert same_float(a, port.reconstruct(marker, mask)), name
