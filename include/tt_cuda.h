@@ -168,16 +168,30 @@ TT_CUDA_API ptrdiff_t tt_cuda_flow_routing_d8_edgelist(ptrdiff_t *source,
                                                        ptrdiff_t dims[2],
                                                        unsigned int order);
 /** include/topotoolbox.h:1019 flow_accumulation_edgelist
- *  (src/flow_accumulation.c:10-30) for the edge list of a D8 forest (each
- *  pixel the source of at most one edge, to one of its eight neighbours in
- *  the column-major interpretation of `dims`) with unit fractions: the
- *  exact forest sum of tt_cuda_flow_accumulation.  Other edge lists are
- *  refused with TT_CUDA_ERR_INVALID_ARGUMENT. */
+ *  (src/flow_accumulation.c:10-30): acc = weights (or 1), then
+ *  acc[target] += fraction * acc[source] for every edge in list order, for
+ *  any edge list: fractional and multi-target (several edges out of a
+ *  pixel), in any order, with the reference's list-order semantics.  Sums
+ *  are taken in list order in FP64 and rounded once to float32, so the
+ *  result is run-to-run identical and within float32 rounding of an FP64
+ *  sweep.  The edge list of a D8 forest with unit fractions in topological
+ *  order (as flow_routing_d8_edgelist produces) takes the exact forest sum
+ *  of tt_cuda_flow_accumulation instead.  An index outside the grid gives
+ *  TT_CUDA_ERR_INVALID_ARGUMENT. */
 TT_CUDA_API void tt_cuda_flow_accumulation_edgelist(float *acc, ptrdiff_t *source,
                                                     ptrdiff_t *target,
                                                     float *fraction, float *weights,
                                                     ptrdiff_t edge_count,
                                                     ptrdiff_t dims[2]);
+/** include/topotoolbox.h:1755 traverse_down_f32_add_mul
+ *  (src/streamquad.c:171-180): output[target] = output[target] +
+ *  output[source] * input[e] for every edge e in list order, any order,
+ *  FP64 sums in list order rounded once to float32 (run-to-run identical).
+ *  `output` spans nodes 0 .. the largest index the edges name, as in the
+ *  reference. */
+TT_CUDA_API void tt_cuda_traverse_down_f32_add_mul(float *output, float *input,
+                                                   ptrdiff_t *source, ptrdiff_t *target,
+                                                   ptrdiff_t edge_count);
 /** include/topotoolbox.h:2304 drainagebasins (src/drainagebasins.c:6-27).
  *  For a topologically ordered edge list (as flow_routing_d8_edgelist
  *  produces) the labels equal the reference's on the same list. */
@@ -304,6 +318,11 @@ TT_CUDA_API tt_cuda_status tt_cuda_flow_accumulation_edgelist_dev(
     float *acc, const ptrdiff_t *source, const ptrdiff_t *target,
     const float *fraction, const float *weights, ptrdiff_t edge_count,
     const ptrdiff_t dims[2], void *stream);
+/** Device form of tt_cuda_traverse_down_f32_add_mul; `node_count` is the
+ *  length of `output` (every index in the edge list must be below it). */
+TT_CUDA_API tt_cuda_status tt_cuda_traverse_down_f32_add_mul_dev(
+    float *output, const float *input, const ptrdiff_t *source, const ptrdiff_t *target,
+    ptrdiff_t edge_count, ptrdiff_t node_count, void *stream);
 TT_CUDA_API tt_cuda_status tt_cuda_drainagebasins_dev(
     ptrdiff_t *basins, const ptrdiff_t *source, const ptrdiff_t *target,
     ptrdiff_t edge_count, const ptrdiff_t dims[2], void *stream);

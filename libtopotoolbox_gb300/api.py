@@ -236,8 +236,8 @@ def flow_routing_d8_edgelist(node, direction, order=0):
 
 
 def flow_accumulation_edgelist(source, target, fraction, shape, weights=None):
-    """acc (include/topotoolbox.h:1019, src/flow_accumulation.c:10-30) for the
-    edge list of a D8 forest with unit fractions."""
+    """acc (include/topotoolbox.h:1019, src/flow_accumulation.c:10-30) for any
+    edge list: fractions, several edges out of a pixel, any order."""
     src = np.ascontiguousarray(source, dtype=np.int64)
     tgt = np.ascontiguousarray(target, dtype=np.int64)
     fr = np.ascontiguousarray(fraction, dtype=np.float32)
@@ -248,6 +248,20 @@ def flow_accumulation_edgelist(source, target, fraction, shape, weights=None):
                                                _ptr(w), len(src), dp)
     _after("flow_accumulation_edgelist")
     return acc
+
+
+def traverse_down_f32_add_mul(output, input, source, target):
+    """output[target] += output[source] * input[e] for every edge in list
+    order (include/topotoolbox.h:1755, src/streamquad.c:171-180).  Returns
+    the updated copy of `output` (float32 node attribute list)."""
+    out = np.array(output, dtype=np.float32, copy=True)
+    inp = np.ascontiguousarray(input, dtype=np.float32)
+    src = np.ascontiguousarray(source, dtype=np.int64)
+    tgt = np.ascontiguousarray(target, dtype=np.int64)
+    N.lib().tt_cuda_traverse_down_f32_add_mul(_ptr(out), _ptr(inp), _ptr(src), _ptr(tgt),
+                                              len(src))
+    _after("traverse_down_f32_add_mul")
+    return out
 
 
 def drainagebasins(source, target, shape):
@@ -454,6 +468,15 @@ class dev:  # namespace
             dev._p(out), dev._p(source), dev._p(target), dev._p(fraction), dev._p(weights),
             int(source.numel()), dp, dev._stream()), "flow_accumulation_edgelist_dev")
         return out
+
+    @staticmethod
+    def traverse_down_f32_add_mul(output, input, source, target):
+        """In place on the 1-D float32 tensor `output`; returns it."""
+        N.check(N.lib().tt_cuda_traverse_down_f32_add_mul_dev(
+            dev._p(output), dev._p(input), dev._p(source), dev._p(target),
+            int(source.numel()), int(output.numel()), dev._stream()),
+            "traverse_down_f32_add_mul_dev")
+        return output
 
     @staticmethod
     def drainagebasins(source, target, like, out=None):

@@ -4,8 +4,11 @@
 //    (u, receiver(u)) per pixel u with a direction, listed in `node` order.
 //    An order-preserving compaction: per-block counts, one scan, scatter.
 //  * flow_accumulation_edgelist (src/flow_accumulation.c:10-30) on an edge
-//    list of a D8 forest with unit fractions: the edges are turned back into
-//    a direction grid and summed by the exact forest contraction.
+//    list of a D8 forest with unit fractions, listed in topological order:
+//    the edges are turned back into a direction grid and summed by the exact
+//    forest contraction.  Every other list (fractions, several edges out of a
+//    pixel, non-neighbours, any order) takes the general sweep of
+//    k_edgeflow.cu.
 //  * drainagebasins (src/drainagebasins.c:6-27): the reference labels basins
 //    in a reverse sweep over a topologically ordered edge list (every edge
 //    out of a pixel is listed after every edge into it).  Running backwards,
@@ -133,7 +136,8 @@ enum : int {
   EL_NOT_NEIGHBOUR = 2,
   EL_DUPLICATE = 4,
   EL_FRACTION = 8,
-  EL_CYCLE = 16  // a pointer-jumping fixpoint that still has an out-edge
+  EL_CYCLE = 16,  // a pointer-jumping fixpoint that still has an out-edge
+  EL_ORDER = 32   // an edge into a pixel listed after the pixel's out-edge
 };
 
 // Direction bit of each source from its edge (bit k of the column-major
@@ -142,7 +146,8 @@ __global__ void edges_to_dir_kernel(const ptrdiff_t *__restrict__ source,
                                     const ptrdiff_t *__restrict__ target,
                                     const float *__restrict__ fraction, int64_t E,
                                     int64_t m, int64_t n, uint8_t *__restrict__ dir,
-                                    int *__restrict__ seen, int *__restrict__ err) {
+                                    int *__restrict__ seen, int *__restrict__ maxin,
+                                    int *__restrict__ err) {
   const int64_t N = m * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -151,6 +156,7 @@ __global__ void edges_to_dir_kernel(const ptrdiff_t *__restrict__ source,
       atomicOr(err, EL_BAD_INDEX);
       continue;
     }
+    atomicMax(&maxin[v], (int)e);
     if (fraction[e] != 1.0f) atomicOr(err, EL_FRACTION);
     const int64_t i = u % m, j = u / m, vi = v % m, vj = v / m;
     const int64_t di = vi - i, dj = vj - j;
@@ -167,6 +173,17 @@ __global__ void edges_to_dir_kernel(const ptrdiff_t *__restrict__ source,
       continue;
     }
     dir[u] = (uint8_t)(1u << k);
+  }
+}
+
+// The forest sum equals the list-order sweep only when every edge into a
+// pixel is listed before the pixel's own out-edge.
+__global__ void edges_order_kernel(const ptrdiff_t *__restrict__ source, int64_t E, int64_t N,
+                                   const int *__restrict__ maxin, int *__restrict__ err) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = source[e];
+    if (u >= 0 && u < N && maxin[u] > (int)e) atomicOr(err, EL_ORDER);
   }
 }
 
@@ -448,19 +465,28 @@ tt_cuda_status accumulate_edgelist_dev(float *acc, const ptrdiff_t *source,
   // accumulation, which may grow (and so move) the shared workspace: they
   // get a stream-ordered allocation of their own.
   uint8_t *dir = nullptr;
-  int *seen = nullptr, *err = nullptr;
+  int *seen = nullptr, *maxin = nullptr, *err = nullptr;
   TT_CHECK(cudaMallocAsync((void **)&dir, (size_t)N + 256, st));
-  TT_CHECK(cudaMallocAsync((void **)&seen, (size_t)N * 4 + 256, st));
-  err = seen + N;
+  TT_CHECK(cudaMallocAsync((void **)&seen, (size_t)N * 8 + 256, st));
+  maxin = seen + N;
+  err = seen + 2 * N;
   TT_CHECK(cudaMemsetAsync(dir, 0, (size_t)N, st));
-  TT_CHECK(cudaMemsetAsync(seen, 0, (size_t)N * 4 + 4, st));
-  TT_LAUNCH(edges_to_dir_kernel, grid_for(E), 256, 0, st, source, target, fraction, E, g.m,
-            g.n, dir, seen, err);
+  TT_CHECK(cudaMemsetAsync(seen, 0, (size_t)N * 4, st));
+  TT_CHECK(cudaMemsetAsync(maxin, 0xff, (size_t)N * 4, st));  // -1: no edge in
+  TT_CHECK(cudaMemsetAsync(err, 0, 4, st));
+  if (E > 0) {
+    TT_LAUNCH(edges_to_dir_kernel, grid_for(E), 256, 0, st, source, target, fraction, E, g.m,
+              g.n, dir, seen, maxin, err);
+    TT_LAUNCH(edges_order_kernel, grid_for(E), 256, 0, st, source, E, N, maxin, err);
+  }
   TT_CHECK(cudaGetLastError());
   int e = 0;
   tt_cuda_status s = read_err(err, st, &e);
-  if (s == TT_CUDA_SUCCESS && e) s = TT_CUDA_ERR_INVALID_ARGUMENT;
-  if (s == TT_CUDA_SUCCESS) s = accumulate_dev(acc, dir, weights, g, st);
+  if (s == TT_CUDA_SUCCESS && (e & EL_BAD_INDEX)) s = TT_CUDA_ERR_INVALID_ARGUMENT;
+  if (s == TT_CUDA_SUCCESS && e)  // not a D8 forest in topological order
+    s = edge_sweep_dev(acc, weights, source, target, fraction, E, N, st);
+  else if (s == TT_CUDA_SUCCESS)
+    s = accumulate_dev(acc, dir, weights, g, st);
   cudaFreeAsync(dir, st);
   cudaFreeAsync(seen, st);
   return s;

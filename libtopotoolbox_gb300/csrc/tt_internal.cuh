@@ -213,6 +213,16 @@ tt_cuda_status accumulate_edgelist_dev(float *acc, const ptrdiff_t *source,
                                        const ptrdiff_t *target, const float *fraction,
                                        const float *weights, int64_t E, const GridDims &g,
                                        cudaStream_t st);
+// The list-order sweep out[tgt] += frac[e] * out[src] over any edge list
+// of nodes [0, N): out = w (or 1) first, then every edge in list order
+// (FP64 sums, deterministic).  `out` may equal `w`.
+tt_cuda_status edge_sweep_dev(float *out, const float *w, const ptrdiff_t *source,
+                              const ptrdiff_t *target, const float *frac, int64_t E, int64_t N,
+                              cudaStream_t st);
+// 1 + the largest node index named by the edge list (INT64_MAX for a
+// negative index), read back to the host.
+tt_cuda_status edge_node_count_dev(const ptrdiff_t *source, const ptrdiff_t *target, int64_t E,
+                                   int64_t *count, cudaStream_t st);
 tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
                                   const ptrdiff_t *target, int64_t E, const GridDims &g,
                                   cudaStream_t st);

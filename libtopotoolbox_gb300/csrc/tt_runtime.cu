@@ -416,6 +416,20 @@ tt_cuda_status tt_cuda_flow_accumulation_edgelist_dev(float *acc, const ptrdiff_
   });
 }
 
+tt_cuda_status tt_cuda_traverse_down_f32_add_mul_dev(float *output, const float *input,
+                                                     const ptrdiff_t *source,
+                                                     const ptrdiff_t *target,
+                                                     ptrdiff_t edge_count, ptrdiff_t node_count,
+                                                     void *stream) {
+  if (!output || (edge_count > 0 && (!source || !target || !input)) ||
+      !edges_ok(edge_count) || node_count <= 0 || node_count >= (1LL << 31))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  const ptrdiff_t nd[2] = {node_count, 1};
+  return dev_call(nd, stream, [&](const GridDims &g, cudaStream_t st) {
+    return edge_sweep_dev(output, output, source, target, input, edge_count, g.cells(), st);
+  });
+}
+
 tt_cuda_status tt_cuda_drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
                                           const ptrdiff_t *target, ptrdiff_t edge_count,
                                           const ptrdiff_t dims[2], void *stream) {
@@ -936,6 +950,56 @@ void tt_cuda_drainagebasins(ptrdiff_t *basins, ptrdiff_t *source, ptrdiff_t *tar
               return drainagebasins_dev((ptrdiff_t *)a[0].dev, (const ptrdiff_t *)a[1].dev,
                                         (const ptrdiff_t *)a[2].dev, edge_count, g, st);
             });
+}
+
+void tt_cuda_traverse_down_f32_add_mul(float *output, float *input, ptrdiff_t *source,
+                                       ptrdiff_t *target, ptrdiff_t edge_count) {
+  if (!edges_ok(edge_count) ||
+      (edge_count > 0 && (!output || !input || !source || !target))) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return;
+  }
+  if (edge_count == 0) {  // no edge: `output` is unchanged
+    set_status(TT_CUDA_SUCCESS);
+    return;
+  }
+  if (!have_device()) {
+    set_status(TT_CUDA_ERR_NO_DEVICE);
+    return;
+  }
+  DeviceLock lock;
+  cudaStream_t st = 0;
+  const size_t E = (size_t)edge_count;
+  Staging sg;
+  sg.add(E * 8);
+  sg.add(E * 8);
+  sg.add(E * 4);
+  if (!sg.reserve()) {
+    finish(TT_CUDA_ERR_ALLOC, st);
+    return;
+  }
+  auto *dsrc = (ptrdiff_t *)sg.take(E * 8);
+  auto *dtgt = (ptrdiff_t *)sg.take(E * 8);
+  auto *din = (float *)sg.take(E * 4);
+  tt_cuda_status s = h2d(dsrc, source, E * 8, st);
+  if (s == TT_CUDA_SUCCESS) s = h2d(dtgt, target, E * 8, st);
+  if (s == TT_CUDA_SUCCESS) s = h2d(din, input, E * 4, st);
+  // The reference's signature carries no node count: `output` spans the
+  // nodes the edges name.
+  int64_t N = 0;
+  if (s == TT_CUDA_SUCCESS) s = edge_node_count_dev(dsrc, dtgt, edge_count, &N, st);
+  if (s == TT_CUDA_SUCCESS && N >= (1LL << 31)) s = TT_CUDA_ERR_INVALID_ARGUMENT;
+  float *dout = nullptr;
+  if (s == TT_CUDA_SUCCESS && cudaMallocAsync((void **)&dout, (size_t)N * 4, st) != cudaSuccess) {
+    cudaGetLastError();
+    s = TT_CUDA_ERR_ALLOC;
+    dout = nullptr;
+  }
+  if (s == TT_CUDA_SUCCESS) s = h2d(dout, output, (size_t)N * 4, st);
+  if (s == TT_CUDA_SUCCESS) s = edge_sweep_dev(dout, dout, dsrc, dtgt, din, edge_count, N, st);
+  if (s == TT_CUDA_SUCCESS) s = d2h(output, dout, (size_t)N * 4, st);
+  if (dout) cudaFreeAsync(dout, st);
+  finish(s, st);
 }
 
 void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree, ptrdiff_t *source,

@@ -101,6 +101,7 @@ class Oracle:
             "flow_accumulation_edgelist": (None, [P, P, P, P, P, C.c_int64, PD]),
             "drainagebasins": (None, [P, P, P, C.c_int64, PD]),
             "edgelist_degree": (None, [P, P, P, P, C.c_int64, C.c_int64]),
+            "traverse_down_f32_add_mul": (None, [P, P, P, P, C.c_int64]),
             "compute_sfgraph": (None, [P, P, P, P, P, P, P, P, D,
                                        C.c_int if kind == "port" else C.c_bool]),
             "compute_drainage_area_single_flow": (None, [P, P, P, P, D]),
@@ -114,6 +115,7 @@ class Oracle:
                 "hillshade_f64": (None, [P, P, D, D, D, PD]),
                 "hillshade_backward_f64": (None, [P, P, P, D, D, D, PD]),
                 "flow_accumulation_edgelist_f64": (None, [P, P, P, P, P, C.c_int64, PD]),
+                "traverse_down_f64_from_f32": (None, [P, P, P, P, C.c_int64]),
             })
         self.fn = {}
         for name, (res, args) in sig.items():
@@ -295,6 +297,17 @@ class Oracle:
         out = np.empty(shape, dtype=np.int64, order="F")
         dp, k = _dims(shape)
         self.fn["drainagebasins"](_ptr(out), _ptr(src), _ptr(tgt), len(src), dp)
+        return out
+
+    def traverse_down_f32_add_mul(self, output, input, source, target, f64=False):
+        """Updated copy of `output` (src/streamquad.c:171-180); with f64 the
+        same sweep in FP64 (port only)."""
+        out = np.array(output, dtype=np.float64 if f64 else np.float32, copy=True)
+        inp = np.ascontiguousarray(input, dtype=np.float32)
+        src = np.ascontiguousarray(source, dtype=np.int64)
+        tgt = np.ascontiguousarray(target, dtype=np.int64)
+        name = "traverse_down_f64_from_f32" if f64 else "traverse_down_f32_add_mul"
+        self.fn[name](_ptr(out), _ptr(inp), _ptr(src), _ptr(tgt), len(src))
         return out
 
     def edgelist_degree(self, source, target, node_count):

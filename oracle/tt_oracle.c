@@ -750,6 +750,24 @@ void orc_flow_accumulation_edgelist_f64(double *acc, const ptrdiff_t *source,
     acc[target[e]] += (double)fraction[e] * acc[source[e]];
 }
 
+/* src/streamquad.c:171-180: out[v] = out[v] + out[u] * in[e] in list order. */
+void orc_traverse_down_f32_add_mul(float *output, const float *input,
+                                   const ptrdiff_t *source, const ptrdiff_t *target,
+                                   ptrdiff_t edge_count) {
+  for (ptrdiff_t e = 0; e < edge_count; e++) {
+    const float add = output[source[e]] * input[e];
+    output[target[e]] = output[target[e]] + add;
+  }
+}
+
+/* The same sweep in FP64 over a float32 start and float32 edge weights. */
+void orc_traverse_down_f64_from_f32(double *output, const float *input,
+                                    const ptrdiff_t *source, const ptrdiff_t *target,
+                                    ptrdiff_t edge_count) {
+  for (ptrdiff_t e = 0; e < edge_count; e++)
+    output[target[e]] += output[source[e]] * (double)input[e];
+}
+
 /* src/drainagebasins.c:6-27 */
 void orc_drainagebasins(ptrdiff_t *basins, const ptrdiff_t *source,
                         const ptrdiff_t *target, ptrdiff_t edge_count,

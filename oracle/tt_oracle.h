@@ -119,6 +119,14 @@ void orc_drainagebasins(ptrdiff_t *basins, const ptrdiff_t *source,
                         const ptrdiff_t dims[2]);
 /* src/streamquad.c:209-224: in- and out-degree of every node (uint8,
  * wrapping as the reference's counters do). */
+/* src/streamquad.c:171-180 */
+void orc_traverse_down_f32_add_mul(float *output, const float *input,
+                                   const ptrdiff_t *source, const ptrdiff_t *target,
+                                   ptrdiff_t edge_count);
+/* the same sweep in FP64 (start values and edge weights given as float32) */
+void orc_traverse_down_f64_from_f32(double *output, const float *input,
+                                    const ptrdiff_t *source, const ptrdiff_t *target,
+                                    ptrdiff_t edge_count);
 void orc_edgelist_degree(uint8_t *indegree, uint8_t *outdegree,
                          const ptrdiff_t *source, const ptrdiff_t *target,
                          ptrdiff_t node_count, ptrdiff_t edge_count);

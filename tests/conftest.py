@@ -109,3 +109,74 @@ def reconstruct_cases():
     nanm = np.asfortranarray(d)
     out.append(("nodata_640", np.asfortranarray(np.where(np.isnan(d), 0, d) - np.float32(20)), nanm))
     return out
+
+
+def mfd_edges(dem, order="topological", seed=0):
+    """Multiple-flow-direction edge list of a DEM: every pixel drains to each
+    lower neighbour with fraction proportional to the drop over the
+    distance (fractions of a pixel sum to 1).  Sources are listed from the
+    highest pixel down (a topological order); "shuffled" permutes the list."""
+    m, n = dem.shape
+    z = np.asarray(dem, np.float64).ravel(order="F")
+    src, tgt, w = [], [], []
+    ii, jj = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
+    ii, jj = ii.ravel(order="F"), jj.ravel(order="F")
+    for di in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            if di == 0 and dj == 0:
+                continue
+            ok = (ii + di >= 0) & (ii + di < m) & (jj + dj >= 0) & (jj + dj < n)
+            p = np.nonzero(ok)[0]
+            q = (jj[p] + dj) * m + (ii[p] + di)
+            drop = (z[p] - z[q]) / np.hypot(di, dj)
+            keep = drop > 0
+            src.append(p[keep])
+            tgt.append(q[keep])
+            w.append(drop[keep])
+    src, tgt, w = np.concatenate(src), np.concatenate(tgt), np.concatenate(w)
+    tot = np.bincount(src, weights=w, minlength=m * n)
+    frac = (w / tot[src]).astype(np.float32)
+    key = np.lexsort((tgt, -z[src]))
+    src, tgt, frac = src[key], tgt[key], frac[key]
+    if order == "shuffled":
+        perm = np.random.default_rng(seed).permutation(src.size)
+        src, tgt, frac = src[perm], tgt[perm], frac[perm]
+    return src.astype(np.int64), tgt.astype(np.int64), frac
+
+
+def edge_list_cases(port):
+    """(name, source, target, fraction, shape) edge lists for
+    flow_accumulation_edgelist / traverse_down_f32_add_mul."""
+    from libtopotoolbox_gb300 import dems
+
+    out = []
+    d = dems.pcg4d_dem((100, 200), 3)
+    r = port.pipeline(d, dems.border_bc(d.shape))
+    s, t = port.flow_routing_d8_edgelist(r["node"], r["direction"])
+    out.append(("d8_unit", s, t, np.ones(len(s), np.float32), d.shape))
+    rng = np.random.default_rng(17)
+    out.append(("d8_fractions", s, t, rng.uniform(0.2, 1.0, len(s)).astype(np.float32), d.shape))
+    perm = rng.permutation(len(s))
+    out.append(("d8_unit_shuffled", s[perm], t[perm], np.ones(len(s), np.float32), d.shape))
+    for shp, sd in [((64, 48), 1), ((37, 53), 2), ((1, 40), 3)]:
+        z = dems.pcg4d_dem(shp, sd)
+        a, b, f = mfd_edges(z)
+        out.append((f"mfd_{shp[0]}x{shp[1]}", a, b, f, shp))
+    z = dems.pcg4d_dem((80, 90), 4)
+    a, b, f = mfd_edges(z, "shuffled", seed=5)
+    out.append(("mfd_shuffled", a, b, f, z.shape))
+    # repeated edges and self-loops among 50 nodes, random order
+    a = rng.integers(0, 50, 400)
+    b = rng.integers(0, 50, 400)
+    b[:20] = a[:20]
+    out.append(("random_dups_loops", a.astype(np.int64), b.astype(np.int64),
+                rng.uniform(0, 0.5, 400).astype(np.float32), (10, 5)))
+    # a fan: one edge into node 1, then 300 edges out of it, then onwards
+    # (more ready edges at once than a walker's private stack holds)
+    fa = [0] + [1] * 300 + list(range(2, 302))
+    fb = [1] + list(range(2, 302)) + [302] * 300
+    out.append(("fan_300", np.array(fa, np.int64), np.array(fb, np.int64),
+                np.full(len(fa), 0.5, np.float32), (303, 1)))
+    out.append(("empty", np.zeros(0, np.int64), np.zeros(0, np.int64),
+                np.zeros(0, np.float32), (7, 9)))
+    return out

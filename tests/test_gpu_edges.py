@@ -6,7 +6,9 @@ the same edge list is bit-identical to the oracle's reverse sweep
 (src/drainagebasins.c:6-27); edgelist_degree equals the oracle's counters
 (src/streamquad.c:209-224); flow_accumulation_edgelist of a D8 forest with
 unit fractions is within 1e-5 of the FP64 sweep and equal, bit for bit, to
-flow_accumulation of the same forest.  Both memory orders.
+flow_accumulation of the same forest; any other edge list (fractions,
+several targets, any order) is within 1e-5 of the FP64 list-order sweep, as
+is traverse_down_f32_add_mul.  Both memory orders.
 """
 import numpy as np
 import pytest
@@ -84,26 +86,68 @@ def test_device_forms_match_host(gpu, port):
     assert np.array_equal(b, port.drainagebasins(hs, hg, dem.shape))
 
 
-def test_edge_lists_the_forest_cannot_take(gpu):
-    """Refused with TT_CUDA_ERR_INVALID_ARGUMENT (1) or TT_CUDA_ERR_CYCLE (5)."""
+def test_edge_list_errors(gpu):
+    """Indices outside the grid are refused with TT_CUDA_ERR_INVALID_ARGUMENT
+    (1); a cycle in drainagebasins' parents with TT_CUDA_ERR_CYCLE (5)."""
     from libtopotoolbox_gb300 import _native, api
 
     shape = (8, 8)
-    src = np.array([0, 1], np.int64)
-    with pytest.raises(_native.TTCudaError) as e:  # a source listed twice
-        api.flow_accumulation_edgelist(np.array([0, 0]), np.array([1, 8]),
-                                       np.ones(2, np.float32), shape)
-    assert e.value.status == 1
-    with pytest.raises(_native.TTCudaError) as e:  # not a neighbour
-        api.flow_accumulation_edgelist(src, np.array([5, 30]), np.ones(2, np.float32), shape)
-    assert e.value.status == 1
-    with pytest.raises(_native.TTCudaError) as e:  # a fraction other than 1
-        api.flow_accumulation_edgelist(src, np.array([1, 2]),
-                                       np.array([1.0, 0.5], np.float32), shape)
-    assert e.value.status == 1
+    for s, t in [([0, 1], [1, 64]), ([-1, 1], [1, 2])]:
+        with pytest.raises(_native.TTCudaError) as e:
+            api.flow_accumulation_edgelist(np.array(s), np.array(t), np.ones(2, np.float32), shape)
+        assert e.value.status == 1
     with pytest.raises(_native.TTCudaError) as e:  # a two-cycle
         api.drainagebasins(np.array([0, 1]), np.array([1, 0]), shape)
     assert e.value.status == 5
+
+
+def test_accumulation_edgelist_general(gpu, port):
+    """Fractional, multi-target, shuffled and degenerate edge lists through
+    the list-order sweep (src/flow_accumulation.c:10-30,
+    src/streamquad.c:171-180): within 1e-5 relative of the FP64 sweep in the
+    same list order (|a - b| / |b| per cell, all values positive) and
+    identical from run to run; the oracle is pinned to the reference on
+    these lists (tests/test_oracle_pins.py)."""
+    from conftest import edge_list_cases
+
+    from libtopotoolbox_gb300 import api
+
+    rng = np.random.default_rng(5)
+    for name, s, t, f, shape in edge_list_cases(port):
+        w = np.asfortranarray(rng.uniform(0.5, 2.0, shape).astype(np.float32))
+        for weights in (None, w):
+            got = api.flow_accumulation_edgelist(s, t, f, shape, weights)
+            exp = port.flow_accumulation_edgelist(s, t, f, shape, weights, f64=True)
+            assert rel_err(got, exp, tau=1e-30) <= REL_TOL, name
+            again = api.flow_accumulation_edgelist(s, t, f, shape, weights)
+            assert np.array_equal(got, again), name
+        start = w.ravel(order="F")
+        got = api.traverse_down_f32_add_mul(start, f, s, t)
+        exp = port.traverse_down_f32_add_mul(start, f, s, t, f64=True)
+        n = int(max(s.max(initial=-1), t.max(initial=-1))) + 1
+        assert rel_err(got[:n], exp[:n], tau=1e-30) <= REL_TOL, name
+        assert np.array_equal(got[n:], start[n:]), name  # nodes no edge names
+
+
+def test_traverse_dev_and_mfd_1024(gpu, port):
+    """Device form on a 1024 x 1024 multiple-flow-direction edge list
+    (about 3.5 million edges, sources listed from the highest pixel down),
+    against the FP64 sweep."""
+    from conftest import mfd_edges
+
+    from libtopotoolbox_gb300 import dems
+    from libtopotoolbox_gb300.api import dev
+
+    torch = gpu
+    z = dems.plain_512(seed=6, size=1024)[0]
+    s, t, f = mfd_edges(z)
+    start = np.ones(z.size, np.float32)
+    out = torch.from_numpy(start.copy()).cuda()
+    dev.traverse_down_f32_add_mul(out, torch.from_numpy(f).cuda(), torch.from_numpy(s).cuda(),
+                                  torch.from_numpy(t).cuda())
+    got = out.cpu().numpy()
+    exp = port.traverse_down_f32_add_mul(start, f, s, t, f64=True)
+    assert rel_err(got, exp, tau=1e-30) <= REL_TOL
 
 
 def test_edgelist_full_size_properties(gpu):

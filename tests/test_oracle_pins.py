@@ -15,7 +15,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import reconstruct_cases, same_float, topo_positions_ok
+from conftest import edge_list_cases, reconstruct_cases, same_float, topo_positions_ok
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
@@ -217,3 +217,19 @@ def test_port_reconstruct_equals_reference(port, ref, idx):
     assert fa == fb == 0, name
     # both forms reach the same fixpoint
     assert same_float(a, port.reconstruct(marker, mask)), name
+
+
+def test_port_edge_sweeps_equal_reference(port, ref):
+    """flow_accumulation_edgelist (src/flow_accumulation.c:10-30) and
+    traverse_down_f32_add_mul (src/streamquad.c:171-180) on fractional,
+    multi-target, shuffled and degenerate edge lists."""
+    rng = np.random.default_rng(3)
+    for name, s, t, f, shape in edge_list_cases(port):
+        w = rng.uniform(0.5, 2.0, shape).astype(np.float32)
+        for weights in (None, w):
+            a = port.flow_accumulation_edgelist(s, t, f, shape, weights)
+            b = ref.flow_accumulation_edgelist(s, t, f, shape, weights)
+            assert same_float(a, b), name
+        start = w.ravel(order="F")
+        assert same_float(port.traverse_down_f32_add_mul(start, f, s, t),
+                          ref.traverse_down_f32_add_mul(start, f, s, t)), name
