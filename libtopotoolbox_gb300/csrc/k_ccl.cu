@@ -173,6 +173,47 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         if (lane == jj) my_mask = b;
       }
     }
+    // Tiles without flats (most of them) and tiles that are flat throughout
+    // (inside large flats) take short paths with the same results as the
+    // general one below.
+    const bool full = i0 + kTile <= m && j0 + kTile <= n;
+    if (!__any_sync(0xffffffffu, my_mask != 0)) {
+      if (i < m)
+        for (int jj = 0; jj < kTile && j0 + jj < n; jj++) L[(j0 + jj) * m + i] = -1;
+      __syncwarp();
+      continue;
+    }
+    if (full && __all_sync(0xffffffffu, my_mask == 0xffffffffu)) {
+      // one component; its root is run 0 (column 0, row 0) at pixel (i0, j0)
+      int kmax = INT_MIN;
+      for (int jj = 0; jj < kTile; jj++) kmax = max(kmax, t.key[jj * kTile + lane]);
+      kmax = __reduce_max_sync(0xffffffffu, kmax);
+      int first = INT_MAX;  // smallest tile index attaining the maximum
+      if (kmax != INT_MIN)
+        for (int jj = 0; jj < kTile; jj++)
+          if (t.key[jj * kTile + lane] == kmax) {
+            first = jj * kTile + lane;
+            break;
+          }
+      first = __reduce_min_sync(0xffffffffu, first);
+      const int64_t rootp = j0 * m + i0;
+      for (int jj = 0; jj < kTile; jj++) {
+        const int64_t gp = (j0 + jj) * m + i;
+        L[gp] = (int)rootp;
+        if (jj || lane) larg[gp] = -1;
+      }
+      if (lane == 0) {
+        lmax[rootp] = kmax;
+        larg[rootp] = first == INT_MAX
+                          ? INT_MAX
+                          : (int)((j0 + first / kTile) * m + (i0 + first % kTile));
+        maxkey[rootp] = INT_MIN;
+        argmax[rootp] = INT_MAX;
+        roots[atomicAdd(nroots, 1)] = (int)rootp;
+      }
+      __syncwarp();
+      continue;
+    }
     // lane = column c from here to the unions
     const uint32_t M = my_mask, S = M & ~(M << 1);
     t.starts[lane] = S;
@@ -345,6 +386,11 @@ __global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ l
   }
 }
 
+// Four pixels per thread: each level of the dependent gather (a pixel's
+// local root, its global root, the root's maximum and argmax) is issued for
+// all four before any result is used.
+constexpr int kCostPer = 4;
+
 __global__ void costs_kernel(float *__restrict__ costs,
                              ptrdiff_t *__restrict__ conncomps, int *__restrict__ L,
                              const int *__restrict__ maxkey,
@@ -352,21 +398,43 @@ __global__ void costs_kernel(float *__restrict__ costs,
                              const int32_t *__restrict__ flats,
                              const float *__restrict__ orig,
                              const float *__restrict__ filled, int64_t N) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    float c = 0.0f;
-    ptrdiff_t lab = 0;
-    if (flats[p] & 1) {
-      const int R = L[L[p]];
-      const float maxd = key_to_float(maxkey[R]);
-      const float depth = __fsub_rn(filled[p], orig[p]);
-      const float diff = __fsub_rn(maxd, depth);
-      c = __double2float_rn(__dadd_rn((double)diff, 0.1));
-      const int a = argmax[R];
-      lab = (a == INT_MAX) ? R : a;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N;
+       p0 += kCostPer * stride) {
+    int fv[kCostPer], l1[kCostPer], R[kCostPer], mk[kCostPer], am[kCostPer];
+    float fl[kCostPer], og[kCostPer];
+#pragma unroll
+    for (int u = 0; u < kCostPer; u++) {
+      const int64_t p = p0 + u * stride;
+      const bool in = p < N;
+      fv[u] = in ? flats[p] : 0;
+      fl[u] = in ? filled[p] : 0.f;
+      og[u] = in ? orig[p] : 0.f;
+      l1[u] = in ? L[p] : -1;
     }
-    costs[p] = c;
-    conncomps[p] = lab;
+#pragma unroll
+    for (int u = 0; u < kCostPer; u++) R[u] = ((fv[u] & 1) && l1[u] >= 0) ? L[l1[u]] : -1;
+#pragma unroll
+    for (int u = 0; u < kCostPer; u++) {
+      mk[u] = R[u] >= 0 ? maxkey[R[u]] : 0;
+      am[u] = R[u] >= 0 ? argmax[R[u]] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kCostPer; u++) {
+      const int64_t p = p0 + u * stride;
+      if (p >= N) continue;
+      float c = 0.0f;
+      ptrdiff_t lab = 0;
+      if (R[u] >= 0) {
+        const float maxd = key_to_float(mk[u]);
+        const float depth = __fsub_rn(fl[u], og[u]);
+        const float diff = __fsub_rn(maxd, depth);
+        c = __double2float_rn(__dadd_rn((double)diff, 0.1));
+        lab = (am[u] == INT_MAX) ? R[u] : am[u];
+      }
+      costs[p] = c;
+      conncomps[p] = lab;
+    }
   }
 }
 
@@ -405,10 +473,8 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
   TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
             maxkey, argmax);
-  // One pixel per thread: each pixel's root lookup is a chain of dependent
-  // loads, best overlapped across many threads.
-  TT_LAUNCH(costs_kernel, (int)std::min<int64_t>((N + 255) / 256, INT_MAX), 256, 0, st,
-            costs, conncomps, L, maxkey, argmax, flats, orig, filled, N);
+  TT_LAUNCH(costs_kernel, (int)std::min<int64_t>((N + 1023) / 1024, (int64_t)sm_count() * 32),
+            256, 0, st, costs, conncomps, L, maxkey, argmax, flats, orig, filled, N);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

@@ -110,7 +110,7 @@ __global__ void ef_pend_kernel(FlowArgs a, int *__restrict__ starts, int *__rest
     const int lo = a.in_off[u];
     const int p = first_after(a.in_list, lo, a.in_off[u + 1], (int)e - 1) - lo;
     a.pend[e] = p;
-    if (p == 0) starts[atomicAdd(nstart, 1)] = (int)e;
+    if (p == 0) starts[append_slot(nstart)] = (int)e;
   }
 }
 

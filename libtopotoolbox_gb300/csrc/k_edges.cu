@@ -273,7 +273,7 @@ basins_tile_kernel(const int *__restrict__ parent, int64_t m, int64_t n, int tm,
       if (t == e) {  // a terminal: root, or exit with its parent outside
         const int q = parent[p];
         J[p] = q;
-        if (q != (int)p) exits[atomicAdd(nexits, 1)] = (int)p;
+        if (q != (int)p) exits[append_slot(nexits)] = (int)p;
       }
     }
     __syncthreads();

@@ -174,12 +174,15 @@ constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
 struct UpTile {
   uint8_t dir[kHalo][36];   // [c][r], one-pixel halo
   int16_t rl[kTileCells];   // local receiver or an RL_* code
+  int16_t leaf[kTileCells];  // in-tile leaves, in the order the walks take them
   int pend[kTileCells];     // in-tile donors not yet arrived
   long long acc[kTileCells];
   int h[kTileCells];
   int nvalid;
   int owned;
   int bad;
+  int nleaf;
+  int next;  // next entry of `leaf` to walk
 };
 
 // Pixel index (jj * 32 + ii) of ring pixel k, 0 <= k < 124.
@@ -218,6 +221,8 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       t.nvalid = 0;
       t.owned = 0;
       t.bad = 0;
+      t.nleaf = 0;
+      t.next = 0;
     }
     __syncthreads();
 
@@ -262,29 +267,44 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       }
       a.emask[(size_t)tile * kRing + tid] = (uint8_t)ne;
     }
-    // Leaves, taken before any walk starts (a walk empties counts).
-    unsigned leaves = 0;
+    // Leaves, listed before any walk starts (a walk empties counts).
 #pragma unroll
     for (int u = 0; u < kTileCells / kUpThreads; u++) {
       const int e = tid + u * kUpThreads;
-      if (t.rl[e] != RL_NONE && t.pend[e] == 0) leaves |= 1u << u;
+      if (t.rl[e] != RL_NONE && t.pend[e] == 0) t.leaf[atomicAdd(&t.nleaf, 1)] = (int16_t)e;
     }
     __syncthreads();
 
-    // Last arriver continues.
+    // Last arriver continues.  A thread whose walk ends takes the next leaf
+    // from the list, so the threads of a warp stay busy until the list is
+    // empty instead of each stepping through its own leaves' walks.
     int owned = 0;
-    for (; leaves; leaves &= leaves - 1) {
-      int cur = tid + (__ffs(leaves) - 1) * kUpThreads;
-      long long v = t.acc[cur];
-      int hv = t.h[cur];
-      owned++;
-      for (int guard = 0; guard < kTileCells; guard++) {
+    {
+      const int nleaf = t.nleaf;
+      int cur = -1;
+      long long v = 0;
+      int hv = 0;
+      for (int guard = 0; guard < 2 * kTileCells + 2; guard++) {
+        if (cur < 0) {
+          const int k = atomicAdd(&t.next, 1);
+          if (k >= nleaf) break;
+          cur = t.leaf[k];
+          v = t.acc[cur];
+          hv = t.h[cur];
+          owned++;
+        }
         const int q = t.rl[cur];
-        if (q < 0) break;  // exit, outlet or grid edge: nothing further in-tile
+        if (q < 0) {  // exit, outlet or grid edge: nothing further in-tile
+          cur = -1;
+          continue;
+        }
         if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
         if (a.want_h) atomicMax(&t.h[q], hv + 1);
         cuda::atomic_ref<int, cuda::thread_scope_block> pend(t.pend[q]);
-        if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) break;
+        if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) {
+          cur = -1;
+          continue;
+        }
         cur = q;  // every donor of q has arrived: q is complete
         owned++;
         if (a.want_acc) v = t.acc[cur];
@@ -304,7 +324,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       if (a.want_h) a.h_out[gp] = t.h[e];
       a.lrl[gp] = t.rl[e];
       if (t.rl[e] != RL_EXIT) continue;
-      const int id = atomicAdd(a.ecount, 1);  // dense exit ids
+      const int id = append_slot(a.ecount);  // dense exit ids
       a.ccell[id] = CoarseCell{a.want_acc ? t.acc[e] : 0LL, a.want_h ? t.h[e] : 0, 0};
       a.elist[id] = (int)gp;
       t.pend[e] = id;  // the counts are spent: keep the exit's id there
@@ -439,7 +459,7 @@ __global__ void coarse_leaves_kernel(const int *__restrict__ ecount,
                                      int *__restrict__ lcount) {
   const int E = *ecount;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x)
-    if (ccell[a].pend == 0) leaves[atomicAdd(lcount, 1)] = a;
+    if (ccell[a].pend == 0) leaves[append_slot(lcount)] = a;
 }
 
 // Relaxed 128-bit compare-and-swap: (lo, hi) holds the expected value on
@@ -730,7 +750,7 @@ __global__ void __launch_bounds__(kDownThreads) forest_down_kernel(DownArgs a) {
       if (t.rl[x] == RL_EXIT) ge = (j0 + x / kTile) * a.m + (i0 + x % kTile);
       if (a.phase == 1) {
         if (t.rl[e] == RL_EXIT) {
-          const int slot = atomicAdd(a.ecount, 1);
+          const int slot = append_slot(a.ecount);
           a.eidx[gp] = slot;
           a.elist[slot] = (int)gp;
         }

@@ -546,21 +546,40 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
 // whose pixels or halo hold such a seed start dirty: every other tile is
 // +INF throughout and already at its local fixpoint until a neighbour
 // publishes a change (plain stores: idempotent).
+// Marks dirty the tiles whose pixels or halo hold pixel (i, j).
+__device__ __forceinline__ void mark_tiles_around(int *dirty, int tm, int64_t i, int64_t j,
+                                                  int64_t m, int64_t n) {
+  const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
+  const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
+  for (int tj = tj0; tj <= tj1; tj++)
+    for (int ti = ti0; ti <= ti1; ti++) dirty[tj * tm + ti] = DIRTY_FULL;
+}
+
+// Elements per thread and loop trip of the elementwise kernels: their loads
+// are all issued before any is used.
+constexpr int kEw = 4;
+
 __global__ void fill_init_kernel(float *__restrict__ f, const float *__restrict__ dem,
                                  const uint8_t *__restrict__ bc, int64_t m, int64_t n,
                                  int *__restrict__ dirty, int tm) {
   const int64_t N = m * n;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    float z = dem[p];
-    const bool seed = bc[p] == 1 || isnan(z);
-    f[p] = seed ? z : INFINITY;
-    if (seed && dirty) {
-      const int64_t i = p % m, j = p / m;
-      const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
-      const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
-      for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) dirty[tj * tm + ti] = DIRTY_FULL;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N; p0 += kEw * stride) {
+    float z[kEw];
+    uint8_t b[kEw];
+#pragma unroll
+    for (int u = 0; u < kEw; u++) {
+      const int64_t p = p0 + u * stride;
+      z[u] = p < N ? dem[p] : 0.f;
+      b[u] = p < N ? bc[p] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kEw; u++) {
+      const int64_t p = p0 + u * stride;
+      if (p >= N) continue;
+      const bool seed = b[u] == 1 || isnan(z[u]);
+      f[p] = seed ? z[u] : INFINITY;
+      if (seed && dirty) mark_tiles_around(dirty, tm, p % m, p / m, m, n);
     }
   }
 }
@@ -600,17 +619,24 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ w
                                  const int32_t *__restrict__ flats, int64_t m,
                                  int64_t n, RelaxArgs qa) {
   const int64_t N = m * n;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    int32_t f = flats[p];
-    dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
-    wcost[p] = (f & 1) ? costs[p] : NAN;
-    if ((f & 5) == 5) {
-      int64_t i = p % m, j = p / m;
-      int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
-      int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
-      for (int tj = tj0; tj <= tj1; tj++)
-        for (int ti = ti0; ti <= ti1; ti++) qa.dirty[tj * qa.tm + ti] = DIRTY_FULL;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N; p0 += kEw * stride) {
+    int32_t fv[kEw];
+    float cv[kEw];
+#pragma unroll
+    for (int u = 0; u < kEw; u++) {
+      const int64_t p = p0 + u * stride;
+      fv[u] = p < N ? flats[p] : 0;
+      cv[u] = p < N ? costs[p] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kEw; u++) {
+      const int64_t p = p0 + u * stride;
+      if (p >= N) continue;
+      const int32_t f = fv[u];
+      dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
+      wcost[p] = (f & 1) ? cv[u] : NAN;
+      if ((f & 5) == 5) mark_tiles_around(qa.dirty, qa.tm, p % m, p / m, m, n);
     }
   }
 }
@@ -618,9 +644,15 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ w
 // Non-flat pixels: distance 0 (src/gwdt.c:300-302).
 __global__ void gwdt_fix_kernel(float *__restrict__ dist, const int32_t *__restrict__ flats,
                                 int64_t N) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
-       p += (int64_t)gridDim.x * blockDim.x)
-    if (!(flats[p] & 1)) dist[p] = 0.0f;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N; p0 += kEw * stride) {
+    int32_t fv[kEw];
+#pragma unroll
+    for (int u = 0; u < kEw; u++) fv[u] = p0 + u * stride < N ? flats[p0 + u * stride] : 1;
+#pragma unroll
+    for (int u = 0; u < kEw; u++)
+      if (!(fv[u] & 1)) dist[p0 + u * stride] = 0.0f;
+  }
 }
 
 // A valid back-link for every reached flat: the first flat neighbour u (in

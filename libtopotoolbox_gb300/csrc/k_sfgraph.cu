@@ -202,7 +202,7 @@ rw_tile_kernel(const int *__restrict__ parent, const int *__restrict__ val, int6
           const int64_t qi = q % m, qj = q / m;
           if (qi >= i0 && qi < i0 + kTile && qj >= j0 && qj < j0 + kTile)
             atomicOr(err, 1);  // a terminal whose parent is in-tile: a cycle
-          exits[atomicAdd(nexits, 1)] = (int)p;
+          exits[append_slot(nexits)] = (int)p;
         }
       }
     }

@@ -4,6 +4,7 @@
 // Every kernel is HBM-bound.  Tiles of 32 x 32 pixels (plus a halo) are
 // staged in shared memory with coalesced 128-byte column segments, so each
 // input byte is read from DRAM about once.
+#include <algorithm>
 #include <cmath>
 
 #include "tt_internal.cuh"
@@ -23,98 +24,108 @@ constexpr int kBlockY = 8;   // along j
 // presill(f) =  flat(f) && exists non-flat neighbour s with z_s == z_f
 // (the scatter at src/identifyflats.c:83-119 restated as a gather).
 //
-// Streamed by warps: a warp owns a strip of 28 output rows (lane l carries
-// row strip*28 - 2 + l; lanes 0..1 and 30..31 are halo) and walks 128
-// columns.  Each column is loaded once, coalesced; the rows above and below
-// come from the neighbouring lanes by shuffles; a window of four columns
-// lives in registers, and the flat bits of a column are one ballot mask.
-// Flat bits of column j - 1 are known once column j is loaded, and the
-// sill/presill gather of column j - 2 then needs only registers and masks.
-// Loads are issued eight columns ahead.
+// One 32 x 32 output tile per step of a 32 x 8 thread block, looping over
+// tiles (a persistent grid): the DEM is staged with a two-pixel halo (NaN
+// off the grid), flat bits are computed for the tile plus a one-pixel ring,
+// then each output pixel gathers from its eight neighbours.  The flat count
+// is kept per block and added once.
 // ------------------------------------------------------------------
-constexpr int kFlatRows = 28;   // output rows per warp
-constexpr int kFlatSeg = 128;   // output columns per warp
-constexpr int kFlatAhead = 8;   // columns loaded per batch
-
 __device__ __forceinline__ float nan_to_neg_inf(float v) { return v != v ? -INFINITY : v; }
 
-__global__ void __launch_bounds__(128)
-identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
-                     int64_t m, int64_t n, int nstrips, int nsegs,
-                     unsigned long long *count) {
-  const int lane = threadIdx.x & 31;
-  const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
-  if (wid >= nstrips * nsegs) return;  // whole warps only
-  const int strip = wid % nstrips, seg = wid / nstrips;
-  const int64_t i = (int64_t)strip * kFlatRows - 2 + lane;
-  const bool row_in = i >= 0 && i < m;
-  const bool row_int = i >= 1 && i < m - 1;  // interior rows may be flat
-  const bool row_out = lane >= 2 && lane < 2 + kFlatRows && row_in;
-  const int64_t ic = row_in ? i : (i < 0 ? 0 : m - 1);  // clamped for loads
-  const int64_t js = (int64_t)seg * kFlatSeg;
-  const int64_t je = (js + kFlatSeg < n ? js + kFlatSeg : n) - 1;  // last output column
-  // window of columns jl-3..jl: z, the row above (u) and below (d)
-  float Z[4], U[4], D[4];
-#pragma unroll
-  for (int w = 0; w < 4; w++) Z[w] = U[w] = D[w] = NAN;
-  unsigned F0 = 0, F1 = 0, F2 = 0;  // flat masks of columns jl-3, jl-2, jl-1
+constexpr int kFz = kTile + 4;  // staged DEM side (two-pixel halo)
+constexpr int kFf = kTile + 2;  // flat bits side (one-pixel ring)
+
+__global__ void __launch_bounds__(kBlockX * kBlockY)
+identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, int64_t m,
+                     int64_t n, int tm, int tn, unsigned long long *count) {
+  __shared__ float zs[kFz][kFz + 1];      // [c][r]: dem at (i0 - 2 + r, j0 - 2 + c)
+  __shared__ uint8_t fs[kFf][kFf + 2];    // [c][r]: flat bit at (i0 - 1 + r, j0 - 1 + c)
+  __shared__ unsigned wsum[kBlockY];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  constexpr int kC = (kFz + kBlockY - 1) / kBlockY;  // 5
   unsigned cnt = 0;
-  for (int64_t jb = js - 2; jb <= je + 2; jb += kFlatAhead) {
-    float buf[kFlatAhead];
+  for (int tile = blockIdx.x; tile < tm * tn; tile += gridDim.x) {
+    const int64_t i0 = (int64_t)(tile % tm) * kTile, j0 = (int64_t)(tile / tm) * kTile;
+    const bool inner = i0 >= 2 && j0 >= 2 && i0 + kTile + 2 <= m && j0 + kTile + 2 <= n;
+    float v[kC][2];
+    if (inner) {
+      const float *base = dem + (j0 - 2) * m + (i0 - 2);
 #pragma unroll
-    for (int u = 0; u < kFlatAhead; u++) {
-      const int64_t j = jb + u;
-      const int64_t jc = j < 0 ? 0 : (j >= n ? n - 1 : j);
-      buf[u] = dem[jc * m + ic];
-    }
+      for (int k = 0; k < kC; k++)
 #pragma unroll
-    for (int u = 0; u < kFlatAhead; u++) {
-      const int64_t jl = jb + u;
-      if (jl > je + 2) break;
-      const float zn = (row_in && jl >= 0 && jl < n) ? buf[u] : NAN;
-      const float un = __shfl_up_sync(0xffffffffu, zn, 1);
-      const float dn = __shfl_down_sync(0xffffffffu, zn, 1);
-#pragma unroll
-      for (int w = 0; w < 3; w++) {
-        Z[w] = Z[w + 1];
-        U[w] = U[w + 1];
-        D[w] = D[w + 1];
-      }
-      Z[3] = zn;
-      U[3] = un;
-      D[3] = dn;
-      // flat bit of column jl - 1 (window column 2)
-      const float zc = Z[2];
-      const float lo = fminf(
-          fminf(fminf(nan_to_neg_inf(U[1]), nan_to_neg_inf(Z[1])),
-                fminf(nan_to_neg_inf(D[1]), nan_to_neg_inf(U[2]))),
-          fminf(fminf(nan_to_neg_inf(D[2]), nan_to_neg_inf(U[3])),
-                fminf(nan_to_neg_inf(Z[3]), nan_to_neg_inf(D[3]))));
-      const bool col_int = jl - 1 >= 1 && jl - 1 < n - 1;
-      const bool f = row_int && col_int && zc == zc && !(lo < zc);
-      F0 = F1;
-      F1 = F2;
-      F2 = __ballot_sync(0xffffffffu, f);
-      // sill / presill of column jl - 2 (window column 1)
-      const int64_t jo = jl - 2;
-      if (jo >= js && jo <= je) {
-        const float z1 = Z[1];
-        const unsigned fc = (F1 >> lane) & 1u;
-        const unsigned lm = (lane + 31) & 31, lp = (lane + 1) & 31;  // rows above, below
-        const bool hit =
-            ((((F0 >> lm) & 1u) != fc) & (U[0] == z1)) | ((((F0 >> lane) & 1u) != fc) & (Z[0] == z1)) |
-            ((((F0 >> lp) & 1u) != fc) & (D[0] == z1)) | ((((F1 >> lm) & 1u) != fc) & (U[1] == z1)) |
-            ((((F1 >> lp) & 1u) != fc) & (D[1] == z1)) | ((((F2 >> lm) & 1u) != fc) & (U[2] == z1)) |
-            ((((F2 >> lane) & 1u) != fc) & (Z[2] == z1)) | ((((F2 >> lp) & 1u) != fc) & (D[2] == z1));
-        if (row_out) {
-          out[jo * m + i] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
-          cnt += fc;
+        for (int h = 0; h < 2; h++) {
+          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+          const bool ok = c < kFz && r < kFz;
+          v[k][h] = base[(int64_t)(ok ? c : 0) * m + (ok ? r : 0)];
         }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kC; k++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+          const int64_t i = i0 - 2 + r, j = j0 - 2 + c;
+          v[k][h] = (c < kFz && r < kFz && i >= 0 && i < m && j >= 0 && j < n) ? dem[j * m + i]
+                                                                             : NAN;
+        }
+    }
+    __syncthreads();  // the previous tile's reads of zs and fs are done
+#pragma unroll
+    for (int k = 0; k < kC; k++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+        if (c < kFz && r < kFz) zs[c][r] = v[k][h];
+      }
+    __syncthreads();
+    // flat bits of the tile and its ring: interior pixel, not NaN, and no
+    // neighbour lower (a NaN neighbour counts as -INF)
+    for (int c = ty; c < kFf; c += kBlockY)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = tx + h * kBlockX;
+        if (r >= kFf) continue;
+        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+        const float zc = zs[c + 1][r + 1];
+        const float lo = fminf(
+            fminf(fminf(nan_to_neg_inf(zs[c][r]), nan_to_neg_inf(zs[c][r + 1])),
+                  fminf(nan_to_neg_inf(zs[c][r + 2]), nan_to_neg_inf(zs[c + 1][r]))),
+            fminf(fminf(nan_to_neg_inf(zs[c + 1][r + 2]), nan_to_neg_inf(zs[c + 2][r])),
+                  fminf(nan_to_neg_inf(zs[c + 2][r + 1]), nan_to_neg_inf(zs[c + 2][r + 2]))));
+        const bool f = i >= 1 && i < m - 1 && j >= 1 && j < n - 1 && zc == zc && !(lo < zc);
+        fs[c][r] = (uint8_t)f;
+      }
+    __syncthreads();
+    // sill / presill: a neighbour of the other kind at the same elevation
+    const int64_t i = i0 + tx;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int c = ty + k * kBlockY;
+      const int64_t j = j0 + c;
+      const unsigned fc = fs[c + 1][tx + 1];
+      const float z1 = zs[c + 2][tx + 2];
+      bool hit = false;
+#pragma unroll
+      for (int dc = -1; dc <= 1; dc++)
+#pragma unroll
+        for (int dr = -1; dr <= 1; dr++) {
+          if (dc == 0 && dr == 0) continue;
+          hit |= (fs[c + 1 + dc][tx + 1 + dr] != fc) & (zs[c + 2 + dc][tx + 2 + dr] == z1);
+        }
+      if (i < m && j < n) {
+        out[j * m + i] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
+        cnt += fc;
       }
     }
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-  if (lane == 0 && cnt) atomicAdd(count, (unsigned long long)cnt);
+  if (tx == 0) wsum[ty] = cnt;
+  __syncthreads();
+  if (tx == 0 && ty == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < kBlockY; w++) tot += wsum[w];
+    if (tot) atomicAdd(count, tot);
+  }
 }
 
 // ------------------------------------------------------------------
@@ -126,38 +137,64 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem,
 // division are written with explicit round-to-nearest intrinsics so that no
 // contraction changes a bit.
 // ------------------------------------------------------------------
+//
+// One 32 x 32 tile per block of 32 x 8 threads.  The neighbour order is a
+// template parameter, so every offset is a compile-time constant; the
+// division by sqrt(2) of a diagonal runs only when the difference itself
+// beats the best slope so far (fl(diff / sqrt(2)) <= diff, so otherwise it
+// cannot win).  Tiles clear of the grid edges stage their halo without
+// bounds tests.
+template <unsigned ORDER>
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
                   const float *__restrict__ dist,
-                  const int32_t *__restrict__ flats, int64_t m, int64_t n,
-                  unsigned order) {
+                  const int32_t *__restrict__ flats, int64_t m, int64_t n) {
   __shared__ float zs[kTile + 2][kTile + 3];
   __shared__ float ds[kTile + 2][kTile + 3];
-  __shared__ uint8_t fs[kTile + 2][kTile + 3];
+  __shared__ uint8_t fs[kTile][kTile + 4];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
-  {  // stage dem, dist and flats with every load in flight at once
-    constexpr int kH = kTile + 2;
-    constexpr int kC = (kH + kBlockY - 1) / kBlockY;
+  constexpr int kH = kTile + 2;
+  constexpr int kC = (kH + kBlockY - 1) / kBlockY;  // 5 halo columns per thread row
+  const bool inner = i0 >= 1 && j0 >= 1 && i0 + kTile + 1 <= m && j0 + kTile + 1 <= n;
+  {  // stage dem and dist (with halo) and the centre flats, every load in flight
     float va[kC][2], vb[kC][2];
-    int vf[kC][2];
+    int vf[4];
+    if (inner) {
+      const float *pd = dem + (j0 - 1) * m + (i0 - 1);
+      const float *pt = dist + (j0 - 1) * m + (i0 - 1);
 #pragma unroll
-    for (int k = 0; k < kC; k++)
+      for (int k = 0; k < kC; k++)
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int c = ty + k * kBlockY, r = tx + h * kBlockX;
-        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
-        va[k][h] = NAN;
-        vb[k][h] = NAN;
-        vf[k][h] = 0;
-        if (c < kH && r < kH && i >= 0 && i < m && j >= 0 && j < n) {
-          const int64_t p = j * m + i;
-          va[k][h] = dem[p];
-          vb[k][h] = dist[p];
-          vf[k][h] = flats[p];
+        for (int h = 0; h < 2; h++) {
+          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+          const bool ok = c < kH && r < kH;
+          const int64_t o = (int64_t)(ok ? c : 0) * m + (ok ? r : 0);
+          va[k][h] = pd[o];
+          vb[k][h] = pt[o];
         }
-      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kC; k++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
+          const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+          va[k][h] = NAN;
+          vb[k][h] = NAN;
+          if (c < kH && r < kH && i >= 0 && i < m && j >= 0 && j < n) {
+            const int64_t p = j * m + i;
+            va[k][h] = dem[p];
+            vb[k][h] = dist[p];
+          }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int64_t i = i0 + tx, j = j0 + ty + k * kBlockY;
+      vf[k] = (i < m && j < n) ? flats[j * m + i] : 0;
+    }
 #pragma unroll
     for (int k = 0; k < kC; k++)
 #pragma unroll
@@ -166,40 +203,43 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
         if (c < kH && r < kH) {
           zs[c][r] = va[k][h];
           ds[c][r] = vb[k][h];
-          fs[c][r] = (uint8_t)(vf[k][h] & 1);
         }
       }
+#pragma unroll
+    for (int k = 0; k < 4; k++) fs[ty + k * kBlockY][tx] = (uint8_t)(vf[k] & 1);
   }
   __syncthreads();
   // Off-grid neighbours hold NaN: their slope is NaN and never selected,
   // exactly as the reference skips them, so no bounds checks are needed.
-  // Odd bits divide by sqrtf(2) with IEEE rounding; even bits divide by 1,
-  // which is exact.
   const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
-  for (int c = ty; c < kTile; c += kBlockY) {
+  const int64_t i = i0 + tx;
+#pragma unroll
+  for (int k4 = 0; k4 < 4; k4++) {
+    const int c = ty + k4 * kBlockY;
     const int64_t j = j0 + c;
-    const int64_t i = i0 + tx;
     if (j >= n || i >= m) continue;
     const int r = tx;
-    const bool fl = fs[c + 1][r + 1] != 0;
+    const bool fl = fs[c][r] != 0;
     const float zc = zs[c + 1][r + 1];
     const float z = fl ? ds[c + 1][r + 1] : zc;
     float best = 0.0f;
-    uint8_t d = 0;
+    unsigned d = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      const int di = d8_di(k, order), dj = d8_dj(k, order);
+      constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+      const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
       const float zn = zs[c + 1 + dj][r + 1 + di];
       if (zn > zc) continue;
       const float zz = fl ? ds[c + 1 + dj][r + 1 + di] : zn;
       const float diff = __fsub_rn(z, zz);
+      if (!(diff > best)) continue;  // also NaN; a diagonal's quotient is <= diff
       const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
       if (g > best) {
         best = g;
-        d = (uint8_t)(1u << k);
+        d = 1u << k;
       }
     }
-    dir[j * m + i] = d;
+    dir[j * m + i] = (uint8_t)d;
   }
 }
 
@@ -573,11 +613,10 @@ tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
     cnt = (unsigned long long *)ws.take(8);
   }
   TT_CHECK(cudaMemsetAsync(cnt, 0, 8, st));
-  const int nstrips = (int)((g.m + kFlatRows - 1) / kFlatRows);
-  const int nsegs = (int)((g.n + kFlatSeg - 1) / kFlatSeg);
-  const int64_t warps = (int64_t)nstrips * nsegs;
-  TT_LAUNCH(identifyflats_kernel, (int)((warps + 3) / 4), 128, 0, st, flags, dem, g.m, g.n,
-            nstrips, nsegs, cnt);
+  // a persistent grid: eight resident blocks of 256 threads per SM
+  const int grid = (int)std::min<int64_t>((int64_t)g.tiles(), (int64_t)sm_count() * 8);
+  TT_LAUNCH(identifyflats_kernel, grid, dim3(kBlockX, kBlockY), 0, st, flags, dem, g.m, g.n,
+            g.tm, g.tn, cnt);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
@@ -585,8 +624,12 @@ tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
 tt_cuda_status directions_dev(uint8_t *dir, const float *dem, const float *dist,
                               const int32_t *flats, const GridDims &g,
                               unsigned order, cudaStream_t st) {
-  TT_LAUNCH(directions_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st, dir,
-            dem, dist, flats, g.m, g.n, order);
+  if (order & 1)
+    TT_LAUNCH(directions_kernel<1>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st, dir, dem,
+              dist, flats, g.m, g.n);
+  else
+    TT_LAUNCH(directions_kernel<0>, tile_grid(g), dim3(kBlockX, kBlockY), 0, st, dir, dem,
+              dist, flats, g.m, g.n);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

@@ -6,6 +6,7 @@
 // column-major: tile (ti, tj) has id tj * tiles_m + ti.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -57,6 +58,18 @@ __host__ __device__ __forceinline__ int d8_dj(int k, unsigned order) {
 // Index of the highest set bit, as the reference decodes a direction byte
 // (src/flow_accumulation.c:63-67).
 __device__ __forceinline__ int d8_bit(unsigned d) { return 31 - __clz(d); }
+
+// Slot in a list appended to by many threads: the threads that call it
+// together take consecutive slots with one atomic on the shared counter
+// (one per group of converged threads, not one per element, so a counter
+// that millions of elements append to does not serialise at one address).
+__device__ __forceinline__ int append_slot(int *counter) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+  return g.shfl(base, 0) + (int)g.thread_rank();
+}
 
 // ------------------------------------------------------------------
 // Status, launch accounting, workspace
