@@ -24,40 +24,45 @@ constexpr int kBlockY = 8;   // along j
 // presill(f) =  flat(f) && exists non-flat neighbour s with z_s == z_f
 // (the scatter at src/identifyflats.c:83-119 restated as a gather).
 //
-// One 32 x 32 output tile per step of a 32 x 8 thread block, looping over
-// tiles (a persistent grid): the DEM is staged with a two-pixel halo (NaN
-// off the grid), flat bits are computed for the tile plus a one-pixel ring,
-// then each output pixel gathers from its eight neighbours.  The flat count
-// is kept per block and added once.
+// One 32 x 32 output tile per block of 32 x 8 threads: the DEM is staged
+// with a two-pixel halo (NaN off the grid), flat bits are computed for the
+// tile plus a one-pixel ring, then thread (tx, ty) gathers for column tx,
+// rows 4 ty .. 4 ty + 3 from a 3 x 6 neighbourhood read once into
+// registers; the flags go out through shared memory in coalesced columns.
+// Each block adds its flat count to one of kCountSlots counters (spread so
+// that blocks do not queue on one address), which a last step sums.
 // ------------------------------------------------------------------
 __device__ __forceinline__ float nan_to_neg_inf(float v) { return v != v ? -INFINITY : v; }
 
 constexpr int kFz = kTile + 4;  // staged DEM side (two-pixel halo)
 constexpr int kFf = kTile + 2;  // flat bits side (one-pixel ring)
+constexpr int kCountSlots = 64;
 
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, int64_t m,
-                     int64_t n, int tm, int tn, unsigned long long *count) {
-  __shared__ float zs[kFz][kFz + 1];      // [c][r]: dem at (i0 - 2 + r, j0 - 2 + c)
-  __shared__ uint8_t fs[kFf][kFf + 2];    // [c][r]: flat bit at (i0 - 1 + r, j0 - 1 + c)
+                     int64_t n, unsigned long long *slots) {
+  __shared__ float zs[kFz][kFz + 1];                 // [c][r]: dem at (i0 - 2 + r, j0 - 2 + c)
+  __shared__ __align__(4) uint8_t fs[kFf][kFf + 2];  // [c][r]: flat at (i0 - 1 + r, j0 - 1 + c)
+  __shared__ int32_t os[kTile][kTile + 1];
   __shared__ unsigned wsum[kBlockY];
   const int tx = threadIdx.x, ty = threadIdx.y;
   constexpr int kC = (kFz + kBlockY - 1) / kBlockY;  // 5
-  unsigned cnt = 0;
-  for (int tile = blockIdx.x; tile < tm * tn; tile += gridDim.x) {
-    const int64_t i0 = (int64_t)(tile % tm) * kTile, j0 = (int64_t)(tile / tm) * kTile;
-    const bool inner = i0 >= 2 && j0 >= 2 && i0 + kTile + 2 <= m && j0 + kTile + 2 <= n;
+  const int64_t i0 = (int64_t)blockIdx.x * kTile, j0 = (int64_t)blockIdx.y * kTile;
+  const bool inner = i0 >= 2 && j0 >= 2 && i0 + kTile + 2 <= m && j0 + kTile + 2 <= n;
+  {
     float v[kC][2];
     if (inner) {
       const float *base = dem + (j0 - 2) * m + (i0 - 2);
 #pragma unroll
-      for (int k = 0; k < kC; k++)
+      for (int k = 0; k < kC; k++) {
+        const int c = ty + k * kBlockY;
+        const int64_t co = (int64_t)(c < kFz ? c : 0) * m;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
-          const bool ok = c < kFz && r < kFz;
-          v[k][h] = base[(int64_t)(ok ? c : 0) * m + (ok ? r : 0)];
+          const int r = tx + h * kBlockX;
+          v[k][h] = base[co + (r < kFz ? r : 0)];
         }
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < kC; k++)
@@ -69,7 +74,6 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
                                                                              : NAN;
         }
     }
-    __syncthreads();  // the previous tile's reads of zs and fs are done
 #pragma unroll
     for (int k = 0; k < kC; k++)
 #pragma unroll
@@ -77,46 +81,69 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
         const int c = ty + k * kBlockY, r = tx + h * kBlockX;
         if (c < kFz && r < kFz) zs[c][r] = v[k][h];
       }
-    __syncthreads();
-    // flat bits of the tile and its ring: interior pixel, not NaN, and no
-    // neighbour lower (a NaN neighbour counts as -INF)
-    for (int c = ty; c < kFf; c += kBlockY)
+  }
+  __syncthreads();
+  // flat bits of the tile and its ring: interior pixel, not NaN, and no
+  // neighbour lower (a NaN neighbour counts as -INF)
+  const int64_t ilo = 1 - (i0 - 1), ihi = (m - 1) - (i0 - 1);  // interior rows: ilo <= r < ihi
+  const int64_t jlo = 1 - (j0 - 1), jhi = (n - 1) - (j0 - 1);
+  for (int c = ty; c < kFf; c += kBlockY)
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int r = tx + h * kBlockX;
-        if (r >= kFf) continue;
-        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
-        const float zc = zs[c + 1][r + 1];
-        const float lo = fminf(
-            fminf(fminf(nan_to_neg_inf(zs[c][r]), nan_to_neg_inf(zs[c][r + 1])),
-                  fminf(nan_to_neg_inf(zs[c][r + 2]), nan_to_neg_inf(zs[c + 1][r]))),
-            fminf(fminf(nan_to_neg_inf(zs[c + 1][r + 2]), nan_to_neg_inf(zs[c + 2][r])),
-                  fminf(nan_to_neg_inf(zs[c + 2][r + 1]), nan_to_neg_inf(zs[c + 2][r + 2]))));
-        const bool f = i >= 1 && i < m - 1 && j >= 1 && j < n - 1 && zc == zc && !(lo < zc);
-        fs[c][r] = (uint8_t)f;
-      }
-    __syncthreads();
-    // sill / presill: a neighbour of the other kind at the same elevation
-    const int64_t i = i0 + tx;
+    for (int h = 0; h < 2; h++) {
+      const int r = tx + h * kBlockX;
+      if (r >= kFf) continue;
+      const float zc = zs[c + 1][r + 1];
+      const float lo = fminf(
+          fminf(fminf(nan_to_neg_inf(zs[c][r]), nan_to_neg_inf(zs[c][r + 1])),
+                fminf(nan_to_neg_inf(zs[c][r + 2]), nan_to_neg_inf(zs[c + 1][r]))),
+          fminf(fminf(nan_to_neg_inf(zs[c + 1][r + 2]), nan_to_neg_inf(zs[c + 2][r])),
+                fminf(nan_to_neg_inf(zs[c + 2][r + 1]), nan_to_neg_inf(zs[c + 2][r + 2]))));
+      const bool f = r >= ilo && r < ihi && c >= jlo && c < jhi && zc == zc && !(lo < zc);
+      fs[c][r] = (uint8_t)f;
+    }
+  __syncthreads();
+  // sill / presill: a neighbour of the other kind at the same elevation
+  unsigned cnt = 0;
+  {
+    const int c = tx, r0 = 4 * ty;
+    uint32_t f[3][2];
+    float z[3][6];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int c = ty + k * kBlockY;
-      const int64_t j = j0 + c;
-      const unsigned fc = fs[c + 1][tx + 1];
-      const float z1 = zs[c + 2][tx + 2];
+    for (int dc = 0; dc < 3; dc++) {
+      f[dc][0] = *reinterpret_cast<const uint32_t *>(&fs[c + dc][r0]);
+      f[dc][1] = *reinterpret_cast<const uint32_t *>(&fs[c + dc][r0 + 4]);
+#pragma unroll
+      for (int u = 0; u < 6; u++) z[dc][u] = zs[c + 1 + dc][r0 + 1 + u];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int uc = u + 1;  // centre row in the 6-row window
+      const unsigned fc = (f[1][uc >> 2] >> (8 * (uc & 3))) & 1u;
+      const float z1 = z[1][uc];
       bool hit = false;
 #pragma unroll
-      for (int dc = -1; dc <= 1; dc++)
+      for (int dc = 0; dc < 3; dc++)
 #pragma unroll
-        for (int dr = -1; dr <= 1; dr++) {
-          if (dc == 0 && dr == 0) continue;
-          hit |= (fs[c + 1 + dc][tx + 1 + dr] != fc) & (zs[c + 2 + dc][tx + 2 + dr] == z1);
+        for (int du = -1; du <= 1; du++) {
+          if (dc == 1 && du == 0) continue;
+          const int w = uc + du;
+          const unsigned fn = (f[dc][w >> 2] >> (8 * (w & 3))) & 1u;
+          hit |= (fn != fc) & (z[dc][w] == z1);
         }
-      if (i < m && j < n) {
-        out[j * m + i] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
-        cnt += fc;
-      }
+      os[c][r0 + u] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
+      if (i0 + r0 + u < m && j0 + c < n) cnt += fc;
     }
+  }
+  __syncthreads();
+  {
+    const int64_t i = i0 + tx;
+    if (i < m)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int c = ty + k * kBlockY;
+        const int64_t j = j0 + c;
+        if (j < n) out[j * m + i] = os[c][tx];
+      }
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
   if (tx == 0) wsum[ty] = cnt;
@@ -124,8 +151,15 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
   if (tx == 0 && ty == 0) {
     unsigned long long tot = 0;
     for (int w = 0; w < kBlockY; w++) tot += wsum[w];
-    if (tot) atomicAdd(count, tot);
+    if (tot) atomicAdd(&slots[(blockIdx.x + blockIdx.y * 7) % kCountSlots], tot);
   }
+}
+
+__global__ void sum_slots_kernel(const unsigned long long *__restrict__ slots,
+                                 unsigned long long *__restrict__ count) {
+  unsigned long long v = slots[threadIdx.x] + slots[threadIdx.x + 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (threadIdx.x == 0) *count = v;
 }
 
 // ------------------------------------------------------------------
@@ -138,12 +172,15 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
 // contraction changes a bit.
 // ------------------------------------------------------------------
 //
-// One 32 x 32 tile per block of 32 x 8 threads.  The neighbour order is a
+// One 32 x 32 tile per block of 32 x 8 threads.  Staging: dem and dist with
+// a one-pixel halo (NaN off the grid) and the centre flat bits.  Compute:
+// thread (tx, ty) takes column tx, rows 4 ty .. 4 ty + 3, reading the 3 x 6
+// neighbourhood of its strip once into registers.  The neighbour order is a
 // template parameter, so every offset is a compile-time constant; the
-// division by sqrt(2) of a diagonal runs only when the difference itself
-// beats the best slope so far (fl(diff / sqrt(2)) <= diff, so otherwise it
-// cannot win).  Tiles clear of the grid edges stage their halo without
-// bounds tests.
+// division of a diagonal difference by sqrt(2) (div_by_sqrt2, bit-identical
+// to the IEEE division) runs only when the difference itself beats the best
+// slope so far (fl(diff / sqrt(2)) <= diff, so otherwise it cannot win).
+// The direction bytes go out through shared memory in coalesced rows.
 template <unsigned ORDER>
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
@@ -151,29 +188,32 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
                   const int32_t *__restrict__ flats, int64_t m, int64_t n) {
   __shared__ float zs[kTile + 2][kTile + 3];
   __shared__ float ds[kTile + 2][kTile + 3];
-  __shared__ uint8_t fs[kTile][kTile + 4];
+  __shared__ __align__(4) uint8_t fs[kTile][kTile + 4];
+  __shared__ __align__(4) uint8_t os[kTile][kTile + 4];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kTile;
   const int64_t j0 = (int64_t)blockIdx.y * kTile;
   constexpr int kH = kTile + 2;
   constexpr int kC = (kH + kBlockY - 1) / kBlockY;  // 5 halo columns per thread row
   const bool inner = i0 >= 1 && j0 >= 1 && i0 + kTile + 1 <= m && j0 + kTile + 1 <= n;
-  {  // stage dem and dist (with halo) and the centre flats, every load in flight
+  {  // every load in flight at once
     float va[kC][2], vb[kC][2];
     int vf[4];
     if (inner) {
       const float *pd = dem + (j0 - 1) * m + (i0 - 1);
       const float *pt = dist + (j0 - 1) * m + (i0 - 1);
 #pragma unroll
-      for (int k = 0; k < kC; k++)
+      for (int k = 0; k < kC; k++) {
+        const int c = ty + k * kBlockY;
+        const int64_t co = (int64_t)(c < kH ? c : 0) * m;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-          const int c = ty + k * kBlockY, r = tx + h * kBlockX;
-          const bool ok = c < kH && r < kH;
-          const int64_t o = (int64_t)(ok ? c : 0) * m + (ok ? r : 0);
-          va[k][h] = pd[o];
-          vb[k][h] = pt[o];
+          const int r = tx + h * kBlockX;
+          const int rr = r < kH ? r : 0;
+          va[k][h] = pd[co + rr];
+          vb[k][h] = pt[co + rr];
         }
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < kC; k++)
@@ -190,10 +230,11 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
           }
         }
     }
+    const bool row_ok = i0 + tx < m;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int64_t i = i0 + tx, j = j0 + ty + k * kBlockY;
-      vf[k] = (i < m && j < n) ? flats[j * m + i] : 0;
+      const int64_t j = j0 + ty + k * kBlockY;
+      vf[k] = (row_ok && j < n) ? flats[j * m + i0 + tx] : 0;
     }
 #pragma unroll
     for (int k = 0; k < kC; k++)
@@ -211,36 +252,54 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
   __syncthreads();
   // Off-grid neighbours hold NaN: their slope is NaN and never selected,
   // exactly as the reference skips them, so no bounds checks are needed.
-  const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
-  const int64_t i = i0 + tx;
+  {
+    const int c = tx, r0 = 4 * ty;  // centre (c + 1, r0 + 1 + u) in halo coordinates
+    float z[3][6], d[3][6];
 #pragma unroll
-  for (int k4 = 0; k4 < 4; k4++) {
-    const int c = ty + k4 * kBlockY;
-    const int64_t j = j0 + c;
-    if (j >= n || i >= m) continue;
-    const int r = tx;
-    const bool fl = fs[c][r] != 0;
-    const float zc = zs[c + 1][r + 1];
-    const float z = fl ? ds[c + 1][r + 1] : zc;
-    float best = 0.0f;
-    unsigned d = 0;
+    for (int dc = 0; dc < 3; dc++)
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
-      const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
-      const float zn = zs[c + 1 + dj][r + 1 + di];
-      if (zn > zc) continue;
-      const float zz = fl ? ds[c + 1 + dj][r + 1 + di] : zn;
-      const float diff = __fsub_rn(z, zz);
-      if (!(diff > best)) continue;  // also NaN; a diagonal's quotient is <= diff
-      const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
-      if (g > best) {
-        best = g;
-        d = 1u << k;
+      for (int u = 0; u < 6; u++) {
+        z[dc][u] = zs[c + dc][r0 + u];
+        d[dc][u] = ds[c + dc][r0 + u];
       }
+    const uint32_t fl4 = *reinterpret_cast<const uint32_t *>(&fs[c][r0]);
+    uint32_t out4 = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const bool fl = (fl4 >> (8 * u)) & 1u;
+      const float zc = z[1][u + 1];
+      const float zz0 = fl ? d[1][u + 1] : zc;
+      float best = 0.0f;
+      unsigned dv = 0;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+        const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
+        const float zn = z[1 + dj][u + 1 + di];
+        const float zz = fl ? d[1 + dj][u + 1 + di] : zn;
+        const float diff = __fsub_rn(zz0, zz);
+        // skip higher neighbours; a difference that does not beat the best
+        // (or is NaN) cannot win, since a diagonal's quotient is <= diff
+        if (zn > zc || !(diff > best)) continue;
+        const float g = (k & 1) ? div_by_sqrt2(diff) : diff;
+        if (g > best) {
+          best = g;
+          dv = 1u << k;
+        }
+      }
+      out4 |= dv << (8 * u);
     }
-    dir[j * m + i] = (uint8_t)d;
+    *reinterpret_cast<uint32_t *>(&os[c][r0]) = out4;
   }
+  __syncthreads();
+  const int64_t i = i0 + tx;
+  if (i < m)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int c = ty + k * kBlockY;
+      const int64_t j = j0 + c;
+      if (j < n) dir[j * m + i] = os[c][tx];
+    }
 }
 
 // ------------------------------------------------------------------
@@ -606,17 +665,14 @@ tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
                                  const GridDims &g,
                                  unsigned long long *count_dev,
                                  cudaStream_t st) {
-  unsigned long long *cnt = count_dev;
-  if (!cnt) {
-    Workspace &ws = workspace();
-    if (!ws.reserve(256)) return TT_CUDA_ERR_ALLOC;
-    cnt = (unsigned long long *)ws.take(8);
-  }
-  TT_CHECK(cudaMemsetAsync(cnt, 0, 8, st));
-  // a persistent grid: eight resident blocks of 256 threads per SM
-  const int grid = (int)std::min<int64_t>((int64_t)g.tiles(), (int64_t)sm_count() * 8);
-  TT_LAUNCH(identifyflats_kernel, grid, dim3(kBlockX, kBlockY), 0, st, flags, dem, g.m, g.n,
-            g.tm, g.tn, cnt);
+  Workspace &ws = workspace();
+  if (!ws.reserve(1024)) return TT_CUDA_ERR_ALLOC;
+  unsigned long long *slots = (unsigned long long *)ws.take(kCountSlots * 8);
+  unsigned long long *cnt = count_dev ? count_dev : (unsigned long long *)ws.take(8);
+  TT_CHECK(cudaMemsetAsync(slots, 0, kCountSlots * 8, st));
+  TT_LAUNCH(identifyflats_kernel, tile_grid(g), dim3(kBlockX, kBlockY), 0, st, flags, dem, g.m,
+            g.n, slots);
+  TT_LAUNCH(sum_slots_kernel, 1, 32, 0, st, slots, cnt);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

@@ -1,4 +1,5 @@
-"""Batched form: every DEM of a batch gets exactly what a separate call gives.
+"""Batched form: every DEM of a batch gets exactly what a separate call gives,
+and exactly what the oracle gives on DEMs of the batched workload itself.
 
 Uneven tiles (sides 37-300, aspect 0.5-2, quantised to 0.1 m, as in the
 batched workload but smaller), run through one mosaic with NaN gutters and a
@@ -60,4 +61,37 @@ def test_batch_matches_single_calls(gpu, tmp_path, monkeypatch):
                     assert same_float(got, r), (k, name)
                 else:
                     assert np.array_equal(got, r), (k, name)
+    bt.close()
+
+
+def test_batch_workload_sample_vs_oracle(gpu, port, tmp_path, monkeypatch):
+    """DEMs drawn from the batched workload itself (512 DEMs, sides
+    log-uniform 128-2048, aspect 0.5-2, fractal, quantised to 0.1 m): its
+    three largest and five others at random, run as one batch; every output
+    of every DEM against the oracle's pipeline on that DEM (which is pinned
+    to the reference): filled, flats, dist and directions bit-exact, unit
+    accumulation exact."""
+    torch = gpu
+    monkeypatch.setenv("TT_CUDA_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    from libtopotoolbox_gb300 import dems
+    from libtopotoolbox_gb300.batch import Batch
+
+    shapes = dems.batch_tile_shapes()
+    area = np.array([a * b for a, b in shapes])
+    big = list(np.argsort(-area)[:3])
+    rng = np.random.default_rng(4)
+    rest = [k for k in rng.permutation(len(shapes)) if k not in big][:5]
+    pick = sorted(int(k) for k in big + rest)
+    tiles = dems.batch_tiles(only=set(pick))
+    assert max(max(d.shape) for d, _ in tiles) >= 1800
+    bt = Batch([d.shape for d, _ in tiles])
+    out = bt.run([_t(d, torch) for d, _ in tiles], [_t(b, torch) for _, b in tiles])
+    torch.cuda.synchronize()
+    for k, (dem, bc) in enumerate(tiles):
+        r = port.pipeline(dem, bc)
+        assert same_float(out["filled"][k].cpu().numpy().T, r["filled"]), (pick[k], "filled")
+        assert np.array_equal(out["flats"][k].cpu().numpy().T, r["flats"]), (pick[k], "flats")
+        assert same_float(out["dist"][k].cpu().numpy().T, r["dist"]), (pick[k], "dist")
+        assert np.array_equal(out["direction"][k].cpu().numpy().T, r["direction"]), (pick[k], "dir")
+        assert np.array_equal(out["acc"][k].cpu().numpy().T, r["acc"]), (pick[k], "acc")
     bt.close()
