@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(kCclWarps * 32)
 ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ larg,
                 int *__restrict__ maxkey, int *__restrict__ argmax,
                 int *__restrict__ roots, int *__restrict__ nroots,
+                uint4 *__restrict__ edges,
                 const int32_t *__restrict__ flats, const float *__restrict__ orig,
                 const float *__restrict__ filled, int64_t m, int64_t n, int tm, int tn) {
   __shared__ CclTile tiles[kCclWarps];
@@ -172,6 +173,14 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         const uint32_t b = __ballot_sync(0xffffffffu, f);
         if (lane == jj) my_mask = b;
       }
+    }
+    {  // the tile's edge flat masks for the border pass: top and bottom row
+       // (bit = column), left and right column (bit = row)
+      const uint32_t top = __ballot_sync(0xffffffffu, my_mask & 1u);
+      const uint32_t bottom = __ballot_sync(0xffffffffu, (my_mask >> 31) & 1u);
+      const uint32_t left = __shfl_sync(0xffffffffu, my_mask, 0);
+      const uint32_t right = __shfl_sync(0xffffffffu, my_mask, kTile - 1);
+      if (lane == 0) edges[tile] = make_uint4(top, bottom, left, right);
     }
     // Tiles without flats (most of them) and tiles that are flat throughout
     // (inside large flats) take short paths with the same results as the
@@ -323,35 +332,53 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
   }
 }
 
-// Edges that cross tile borders: from the last row, the last column and the
-// first column of every tile to the neighbours (i+1,j), (i,j+1), (i+1,j+1),
-// (i+1,j-1) lying in another tile.
-__global__ void ccl_border_kernel(int *__restrict__ L,
-                                  const int32_t *__restrict__ flats, int64_t m,
-                                  int64_t n, int tm, int tn) {
+// Edges that cross tile borders, from the tiles' edge masks (one thread per
+// tile; bit k of a row mask is column k, of a column mask row k).  Flat
+// pixels next to each other along one tile edge are already connected
+// inside the tile, so a border needs one union per pair of touching runs
+// (8-connectivity: a run on one side touches the other side's pixels from
+// one position before its start to one after its end), not one per pixel.
+// Per tile: the border with the tile below (its bottom row against their
+// top row), the border with the tile to the right (right column against
+// their left column), and the two corners: (31, 31) against (0, 0) of the
+// tile below-right, (31, 0) against (0, 31) of the tile below-left.
+__device__ void unite_runs(int *L, uint32_t a, uint32_t b, int64_t pa0, int64_t pa_step,
+                           int64_t pb0, int64_t pb_step) {
+  const uint32_t sb = b & ~(b << 1);  // run starts of b
+  for (uint32_t ra = a & ~(a << 1); ra; ra &= ra - 1) {
+    const int s0 = __ffs(ra) - 1;
+    const uint32_t rm = run_mask(a, s0);
+    uint32_t ov = b & (rm | (rm << 1) | (rm >> 1));
+    while (ov) {
+      const int t0 = run_start(sb, __ffs(ov) - 1);
+      uf_union(L, (int)(pa0 + s0 * pa_step), (int)(pb0 + t0 * pb_step));
+      ov &= ~run_mask(b, t0);
+    }
+  }
+}
+
+__global__ void ccl_border_kernel(int *__restrict__ L, const uint4 *__restrict__ edges,
+                                  int64_t m, int tm, int tn) {
   const int T = tm * tn;
-  const int64_t total = (int64_t)T * 96;
-  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
-       w += (int64_t)gridDim.x * blockDim.x) {
-    const int tile = (int)(w / 96), k = (int)(w % 96);
+  for (int tile = blockIdx.x * blockDim.x + threadIdx.x; tile < T;
+       tile += gridDim.x * blockDim.x) {
     const int ti = tile % tm, tj = tile / tm;
-    int ii, jj;
-    if (k < 32) { ii = kTile - 1; jj = k; }
-    else if (k < 64) { ii = k - 32; jj = kTile - 1; }
-    else { ii = k - 64; jj = 0; }
-    const int64_t i = (int64_t)ti * kTile + ii, j = (int64_t)tj * kTile + jj;
-    if (i >= m || j >= n) continue;
-    const int64_t p = j * m + i;
-    if (!(flats[p] & 1)) continue;
-    const int di[4] = {1, 0, 1, 1};
-    const int dj[4] = {0, 1, 1, -1};
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      int64_t qi = i + di[e], qj = j + dj[e];
-      if (qi >= m || qj < 0 || qj >= n) continue;
-      if (qi / kTile == ti && qj / kTile == tj) continue;  // internal edge
-      int64_t q = qj * m + qi;
-      if (flats[q] & 1) uf_union(L, (int)p, (int)q);
+    const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
+    const uint4 e = edges[tile];  // top, bottom, left, right
+    if (ti + 1 < tm) {
+      const uint4 d = edges[tile + 1];  // the tile below
+      if (e.y && d.x)  // bottom row (i0 + 31, j0 + k) against row i0 + 32
+        unite_runs(L, e.y, d.x, j0 * m + i0 + kTile - 1, m, j0 * m + i0 + kTile, m);
+      if (tj + 1 < tn && (e.y >> 31) && (edges[tile + 1 + tm].x & 1u))
+        uf_union(L, (int)((j0 + kTile - 1) * m + i0 + kTile - 1),
+                 (int)((j0 + kTile) * m + i0 + kTile));
+      if (tj > 0 && (e.y & 1u) && (edges[tile + 1 - tm].x >> 31))
+        uf_union(L, (int)(j0 * m + i0 + kTile - 1), (int)((j0 - 1) * m + i0 + kTile));
+    }
+    if (tj + 1 < tn) {
+      const uint4 r = edges[tile + tm];  // the tile to the right
+      if (e.w && r.z)  // right column (i0 + k, j0 + 31) against column j0 + 32
+        unite_runs(L, e.w, r.z, (j0 + kTile - 1) * m + i0, 1, (j0 + kTile) * m + i0, 1);
     }
   }
 }
@@ -452,8 +479,11 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
                          cudaStream_t st) {
   const int64_t N = g.cells();
   Workspace &ws = workspace();
-  if (!ws.reserve(7 * align_up((size_t)N * 4) + 256)) return TT_CUDA_ERR_ALLOC;
+  const int T = g.tiles();
+  if (!ws.reserve(7 * align_up((size_t)N * 4) + align_up((size_t)T * 16) + 256))
+    return TT_CUDA_ERR_ALLOC;
   int *nroots = (int *)ws.take(256);
+  uint4 *edges = (uint4 *)ws.take((size_t)T * 16);
   int *roots = (int *)ws.take((size_t)N * 4);
   int *rootR = (int *)ws.take((size_t)N * 4);
   int *L = (int *)ws.take((size_t)N * 4);
@@ -462,14 +492,12 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   int *maxkey = (int *)ws.take((size_t)N * 4);
   int *argmax = (int *)ws.take((size_t)N * 4);
   const int grid = ew_grid(N);
-  const int T = g.tiles();
   const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
                                            (int64_t)sm_count() * 16);
   TT_CHECK(cudaMemsetAsync(nroots, 0, sizeof(int), st));
   TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, maxkey, argmax,
-            roots, nroots, flats, orig, filled, g.m, g.n, g.tm, g.tn);
-  TT_LAUNCH(ccl_border_kernel, ew_grid((int64_t)T * 96), 256, 0, st, L, flats, g.m,
-            g.n, g.tm, g.tn);
+            roots, nroots, edges, flats, orig, filled, g.m, g.n, g.tm, g.tn);
+  TT_LAUNCH(ccl_border_kernel, ew_grid(T), 256, 0, st, L, edges, g.m, g.tm, g.tn);
   TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
   TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
             maxkey, argmax);

@@ -3,7 +3,7 @@
 The direction kernels divide diagonal drops by sqrtf(2) with a
 three-instruction correctly rounded division (Markstein's correction step
 for a constant divisor) instead of the IEEE division of the reference
-(src/flow_routing.c:57-61).  It must give the same bits as the IEEE
+(src/flow_routing.c:42-43,69).  It must give the same bits as the IEEE
 division for every float32 input, which this test checks exhaustively
 (2^32 inputs, on the GPU).
 """
