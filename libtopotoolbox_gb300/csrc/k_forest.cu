@@ -167,8 +167,8 @@ constexpr int kUpThreads = 128;
 // thread, no spills; shared memory allows 10 and 15): walks wait at block
 // barriers for the block's longest chain, so more resident blocks keep the
 // SM busy meanwhile.
-constexpr int kUpBlocks = 10;
-constexpr int kFinBlocks = 12;
+constexpr int kUpBlocks = 9;
+constexpr int kFinBlocks = 11;
 constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
 
 struct UpTile {
@@ -193,30 +193,67 @@ __device__ __forceinline__ int ring_pixel(int k) {
   return (kTile - 1) * kTile + (k - 3 * kTile + 3);     // jj = 31, ii = 1..30
 }
 
+// Receiver code of the pixel at tile position (ii, jj) with direction byte
+// d, neighbour order ORDER.  `inner`: the tile and its one-pixel halo lie in
+// the grid, so every receiver is on the grid.
+template <unsigned ORDER>
+__device__ __forceinline__ int tile_receiver(unsigned d, int ii, int jj, bool inner,
+                                             int64_t i0, int64_t j0, int64_t m, int64_t n) {
+  if (d == 0) return RL_ROOT;
+  constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+  const int k = d8_bit(d);
+  const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
+  const int ni = ii + di, nj = jj + dj;
+  if (!inner) {
+    const int64_t gi = i0 + ni, gj = j0 + nj;
+    if (gi < 0 || gi >= m || gj < 0 || gj >= n) return RL_BADDIR;
+  }
+  if ((unsigned)ni < (unsigned)kTile && (unsigned)nj < (unsigned)kTile) return nj * kTile + ni;
+  return RL_EXIT;
+}
+
+// Stages the tile's directions with a one-pixel halo (0 off the grid).
+__device__ __forceinline__ void stage_dirs(uint8_t (*dir)[36], const uint8_t *__restrict__ g,
+                                           int64_t i0, int64_t j0, int64_t m, int64_t n,
+                                           bool inner, int tid) {
+  constexpr int kL = (kHalo * kHalo + kUpThreads - 1) / kUpThreads;
+  uint8_t v[kL];
+  const uint8_t *base = g + (j0 - 1) * m + (i0 - 1);  // only dereferenced in the grid
+#pragma unroll
+  for (int u = 0; u < kL; u++) {
+    const int e = tid + u * kUpThreads;
+    const int c = e / kHalo, r = e % kHalo;
+    if (inner) {
+      v[u] = e < kHalo * kHalo ? base[(int64_t)c * m + r] : 0;
+    } else {
+      const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
+      v[u] = (e < kHalo * kHalo && i >= 0 && i < m && j >= 0 && j < n) ? g[j * m + i] : 0;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kL; u++) {
+    const int e = tid + u * kUpThreads;
+    if (e < kHalo * kHalo) dir[e / kHalo][e % kHalo] = v[u];
+  }
+}
+
+// Thread tid owns tile pixels e = tid + 128 u (u = 0..7): row ii = tid % 32,
+// columns jj = tid / 32 + 4 u, so its global indices advance by 4 m.
+constexpr int kPerThread = kTileCells / kUpThreads;  // 8
+
+template <bool ACC, bool H, unsigned ORDER>
 __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs a) {
   __shared__ UpTile t;
   const int tid = threadIdx.x;
+  const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-    {  // stage the directions with every load in flight at once
-      constexpr int kL = (kHalo * kHalo + kUpThreads - 1) / kUpThreads;
-      uint8_t v[kL];
+    const bool inner = i0 >= 1 && j0 >= 1 && i0 + kTile + 1 <= a.m && j0 + kTile + 1 <= a.n;
+    stage_dirs(t.dir, a.dir, i0, j0, a.m, a.n, inner, tid);
 #pragma unroll
-      for (int u = 0; u < kL; u++) {
-        const int e = tid + u * kUpThreads;
-        const int c = e / kHalo, r = e % kHalo;
-        const int64_t i = i0 - 1 + r, j = j0 - 1 + c;
-        v[u] = (e < kHalo * kHalo && i >= 0 && i < a.m && j >= 0 && j < a.n) ? a.dir[j * a.m + i] : 0;
-      }
-#pragma unroll
-      for (int u = 0; u < kL; u++) {
-        const int e = tid + u * kUpThreads;
-        if (e < kHalo * kHalo) t.dir[e / kHalo][e % kHalo] = v[u];
-      }
-    }
-    for (int e = tid; e < kTileCells; e += kUpThreads) t.pend[e] = 0;
+    for (int u = 0; u < kPerThread; u++) t.pend[tid + u * kUpThreads] = 0;
     if (tid == 0) {
       t.nvalid = 0;
       t.owned = 0;
@@ -226,21 +263,23 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
     }
     __syncthreads();
 
+    const int64_t g0 = (j0 + jb) * a.m + i0 + ii;  // global index of u = 0
+    const int64_t gstep = 4 * a.m;
+    const bool row_in = i0 + ii < a.m;
     int nvalid = 0, bad = 0;
-    for (int e = tid; e < kTileCells; e += kUpThreads) {
-      const int ii = e % kTile, jj = e / kTile;
-      const int64_t i = i0 + ii, j = j0 + jj;
-      const int rl = local_receiver(t.dir, ii, jj, i, j, a.m, a.n, a.order);
+#pragma unroll
+    for (int u = 0; u < kPerThread; u++) {
+      const int jj = jb + 4 * u, e = tid + u * kUpThreads;
+      const bool in = inner || (row_in && j0 + jj < a.n);
+      const int rl = in ? tile_receiver<ORDER>(t.dir[jj + 1][ii + 1], ii, jj, inner, i0, j0,
+                                               a.m, a.n)
+                        : RL_NONE;
       t.rl[e] = (int16_t)rl;
       bad |= rl == RL_BADDIR;
       if (rl >= 0) atomicAdd(&t.pend[rl], 1);
-      long long w0 = 0;
-      if (rl != RL_NONE) {
-        nvalid++;
-        if (a.want_acc) w0 = a.w ? to_fixed(a.w[j * a.m + i], a.wshift, a.err) : 1LL;
-      }
-      t.acc[e] = w0;
-      t.h[e] = 0;
+      if (ACC) t.acc[e] = in ? (a.w ? to_fixed(a.w[g0 + u * gstep], a.wshift, a.err) : 1LL) : 0LL;
+      if (H) t.h[e] = 0;
+      nvalid += in;
     }
     if (nvalid) atomicAdd(&t.nvalid, nvalid);
     if (bad) t.bad = 1;
@@ -251,17 +290,17 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
     int re = 0;
     if (tid < kRing) {
       re = ring_pixel(tid);
-      const int ii = re % kTile, jj = re / kTile;
+      const int ri = re % kTile, rj = re / kTile;
       unsigned ne = 0;
       if (t.rl[re] != RL_NONE) {
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-          const int di = d8_di(k, a.order), dj = d8_dj(k, a.order);
-          const int qr = ii + 1 - di, qc = jj + 1 - dj;  // halo coordinates of q
+          constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+          const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
+          const int qr = ri + 1 - di, qc = rj + 1 - dj;  // halo coordinates of q
           if (qr >= 1 && qr <= kTile && qc >= 1 && qc <= kTile) continue;
           const unsigned dq = t.dir[qc][qr];
-          if (dq == 0 || d8_bit(dq) != k) continue;
-          ne |= 1u << k;
+          if (dq != 0 && d8_bit(dq) == k) ne |= 1u << k;
         }
         entry = ne != 0;
       }
@@ -269,7 +308,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
     }
     // Leaves, listed before any walk starts (a walk empties counts).
 #pragma unroll
-    for (int u = 0; u < kTileCells / kUpThreads; u++) {
+    for (int u = 0; u < kPerThread; u++) {
       const int e = tid + u * kUpThreads;
       if (t.rl[e] != RL_NONE && t.pend[e] == 0) t.leaf[atomicAdd(&t.nleaf, 1)] = (int16_t)e;
     }
@@ -289,8 +328,8 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
           const int k = atomicAdd(&t.next, 1);
           if (k >= nleaf) break;
           cur = t.leaf[k];
-          v = t.acc[cur];
-          hv = t.h[cur];
+          if (ACC) v = t.acc[cur];
+          if (H) hv = t.h[cur];
           owned++;
         }
         const int q = t.rl[cur];
@@ -298,8 +337,8 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
           cur = -1;
           continue;
         }
-        if (a.want_acc) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
-        if (a.want_h) atomicMax(&t.h[q], hv + 1);
+        if (ACC) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
+        if (H) atomicMax(&t.h[q], hv + 1);
         cuda::atomic_ref<int, cuda::thread_scope_block> pend(t.pend[q]);
         if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) {
           cur = -1;
@@ -307,25 +346,26 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
         }
         cur = q;  // every donor of q has arrived: q is complete
         owned++;
-        if (a.want_acc) v = t.acc[cur];
-        if (a.want_h) hv = t.h[cur];
+        if (ACC) v = t.acc[cur];
+        if (H) hv = t.h[cur];
       }
     }
     if (owned) atomicAdd(&t.owned, owned);
     __syncthreads();
     if (tid == 0 && t.owned != t.nvalid) atomicOr(a.err, ERR_CYCLE);
 
-    for (int e = tid; e < kTileCells; e += kUpThreads) {
-      const int ii = e % kTile, jj = e / kTile;
-      const int64_t i = i0 + ii, j = j0 + jj;
-      if (i >= a.m || j >= a.n) continue;
-      const int64_t gp = j * a.m + i;
-      if (a.want_acc) a.lacc[gp] = t.acc[e];  // local totals for the final pass
-      if (a.want_h) a.h_out[gp] = t.h[e];
-      a.lrl[gp] = t.rl[e];
-      if (t.rl[e] != RL_EXIT) continue;
+#pragma unroll
+    for (int u = 0; u < kPerThread; u++) {
+      const int jj = jb + 4 * u, e = tid + u * kUpThreads;
+      if (!(inner || (row_in && j0 + jj < a.n))) continue;
+      const int64_t gp = g0 + u * gstep;
+      if (ACC) a.lacc[gp] = t.acc[e];  // local totals for the final pass
+      if (H) a.h_out[gp] = t.h[e];
+      const int rl = t.rl[e];
+      a.lrl[gp] = (int16_t)rl;
+      if (rl != RL_EXIT) continue;
       const int id = append_slot(a.ecount);  // dense exit ids
-      a.ccell[id] = CoarseCell{a.want_acc ? t.acc[e] : 0LL, a.want_h ? t.h[e] : 0, 0};
+      a.ccell[id] = CoarseCell{ACC ? t.acc[e] : 0LL, H ? t.h[e] : 0, 0};
       a.elist[id] = (int)gp;
       t.pend[e] = id;  // the counts are spent: keep the exit's id there
     }
@@ -356,23 +396,26 @@ struct FinTile {
   int16_t rl[kTileCells];
 };
 
+template <bool ACC, bool H, unsigned ORDER>
 __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpArgs a) {
   __shared__ FinTile t;
   const int tid = threadIdx.x;
+  const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
-  constexpr int kP = kTileCells / kUpThreads;
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
-    const int64_t ilim = a.m - i0, jlim = a.n - j0;  // in-grid: ii < ilim, jj < jlim
+    const bool full = i0 + kTile <= a.m && j0 + kTile <= a.n;
+    const bool row_in = i0 + ii < a.m;
+    const int64_t g0 = (j0 + jb) * a.m + i0 + ii;
+    const int64_t gstep = 4 * a.m;
 #pragma unroll
-    for (int u = 0; u < kP; u++) {  // local totals and receivers
+    for (int u = 0; u < kPerThread; u++) {  // local totals and receivers
       const int e = tid + u * kUpThreads;
-      const int ii = e % kTile, jj = e / kTile;
-      const bool in = ii < ilim && jj < jlim;
-      const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
-      if (a.want_acc) t.acc[e] = in ? a.lacc[gp] : 0LL;
-      if (a.want_h) t.h[e] = in ? a.h_out[gp] : 0;
+      const bool in = full || (row_in && j0 + jb + 4 * u < a.n);
+      const int64_t gp = g0 + u * gstep;
+      if (ACC) t.acc[e] = in ? a.lacc[gp] : 0LL;
+      if (H) t.h[e] = in ? a.h_out[gp] : 0;
       t.rl[e] = in ? a.lrl[gp] : (int16_t)RL_NONE;
     }
     unsigned mask = 0;
@@ -381,20 +424,22 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
 
     if (mask) {  // an entry pixel: carry its inflow down its path
       const int re = ring_pixel(tid);
-      const int64_t i = i0 + re % kTile, j = j0 + re / kTile;
+      const int64_t p = (j0 + re / kTile) * a.m + (i0 + re % kTile);
       long long inflow = 0;
       int hin = 0;
       for (unsigned mk = mask; mk; mk &= mk - 1) {
         const int k = __ffs(mk) - 1;
-        const CoarseCell cq = a.cell[(j - d8_dj(k, a.order)) * a.m + (i - d8_di(k, a.order))];
-        inflow += cq.sum;
-        hin = max(hin, cq.h + 1);
+        constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+        const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
+        const CoarseCell cq = a.cell[p - dj * a.m - di];
+        if (ACC) inflow += cq.sum;
+        if (H) hin = max(hin, cq.h + 1);
       }
       int cur = re;
       for (int d = 0; d < kTileCells; d++) {
-        if (a.want_acc && inflow)
+        if (ACC && inflow)
           atomicAdd((unsigned long long *)&t.acc[cur], (unsigned long long)inflow);
-        if (a.want_h) atomicMax(&t.h[cur], hin + d);
+        if (H) atomicMax(&t.h[cur], hin + d);
         const int q = t.rl[cur];
         if (q < 0) break;
         cur = q;
@@ -404,25 +449,26 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
 
     int hm = 0;
 #pragma unroll
-    for (int u = 0; u < kP; u++) {
+    for (int u = 0; u < kPerThread; u++) {
       const int e = tid + u * kUpThreads;
-      const int ii = e % kTile, jj = e / kTile;
-      if (ii >= ilim || jj >= jlim) continue;
-      const int64_t gp = (j0 + jj) * a.m + (i0 + ii);
-      if (a.want_acc && a.count_out) {
-        a.count_out[gp] = (int)t.acc[e];
-      } else if (a.want_acc && a.raw_out) {
-        a.raw_out[gp] = t.acc[e];
-      } else if (a.want_acc) {
-        const float v = __ll2float_rn(t.acc[e]);
-        a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
+      if (!(full || (row_in && j0 + jb + 4 * u < a.n))) continue;
+      const int64_t gp = g0 + u * gstep;
+      if (ACC) {
+        if (a.count_out) {
+          a.count_out[gp] = (int)t.acc[e];
+        } else if (a.raw_out) {
+          a.raw_out[gp] = t.acc[e];
+        } else {
+          const float v = __ll2float_rn(t.acc[e]);
+          a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
+        }
       }
-      if (a.want_h) {
+      if (H) {
         a.h_out[gp] = t.h[e];
         hm = max(hm, t.h[e]);
       }
     }
-    if (a.want_h && hm) atomicMax(a.hmax, hm);
+    if (H && hm) atomicMax(a.hmax, hm);
     __syncthreads();
   }
 }
@@ -453,13 +499,18 @@ __global__ void coarse_link_kernel(const int *__restrict__ elist,
   }
 }
 
+// Lists the exits without coarse donors and packs every exit's coarse
+// in-degree into the high half of its link's hop count (hops <= 1025).
 __global__ void coarse_leaves_kernel(const int *__restrict__ ecount,
                                      const CoarseCell *__restrict__ ccell,
-                                     int *__restrict__ leaves,
+                                     int2 *__restrict__ link, int *__restrict__ leaves,
                                      int *__restrict__ lcount) {
   const int E = *ecount;
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x)
-    if (ccell[a].pend == 0) leaves[append_slot(lcount)] = a;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < E; a += gridDim.x * blockDim.x) {
+    const int pend = ccell[a].pend;
+    link[a].y |= pend << 16;
+    if (pend == 0) leaves[append_slot(lcount)] = a;
+  }
 }
 
 // Relaxed 128-bit compare-and-swap: (lo, hi) holds the expected value on
@@ -478,7 +529,10 @@ __device__ __forceinline__ void cas128(CoarseCell *p, unsigned long long &lo,
 // Last-arriver walk over the exits: a walker owns a complete exit, folds its
 // totals into the next exit downstream with one compare-and-swap, and
 // continues only if it was the last donor to arrive.  The next exit's link
-// is loaded together with its cell, so a hop costs two dependent accesses.
+// is loaded together with its cell, so a hop costs two dependent accesses;
+// into an exit with a single coarse donor (most hops along a river) the
+// walker is the only arrival, so it combines and stores without the swap:
+// one dependent access per hop.
 __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
                                    const int *__restrict__ lcount,
                                    const int2 *__restrict__ link,
@@ -498,12 +552,23 @@ __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
       if (nx < 0) break;
       const longlong2 g = __ldcg(reinterpret_cast<const longlong2 *>(&ccell[nx]));
       const int2 ln = link[nx];
+      const int hops = l.y & 0xffff;
+      if ((ln.y >> 16) == 1) {  // the only coarse donor of nx: no other writer
+        const long long sum = g.x + v;
+        const int h = max((int)(unsigned)(unsigned long long)g.y, hv + hops);
+        __stcg(reinterpret_cast<longlong2 *>(&ccell[nx]),
+               make_longlong2(sum, (long long)(unsigned long long)(unsigned)h));
+        v = sum;
+        hv = h;
+        l = ln;
+        continue;
+      }
       unsigned long long lo = (unsigned long long)g.x, hi = (unsigned long long)g.y;
       unsigned long long nlo, nhi;
       for (;;) {
         const int oh = (int)(unsigned)hi, op = (int)(unsigned)(hi >> 32);
         nlo = lo + (unsigned long long)v;
-        nhi = (unsigned long long)(unsigned)max(oh, hv + l.y) |
+        nhi = (unsigned long long)(unsigned)max(oh, hv + hops) |
               ((unsigned long long)(unsigned)(op - 1) << 32);
         const unsigned long long elo = lo, ehi = hi;
         cas128(&ccell[nx], lo, hi, nlo, nhi);
@@ -969,19 +1034,31 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.err = w.counters + 4;
   // one resident wave of blocks, each looping over tiles
   const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kUpBlocks);
-  TT_LAUNCH(forest_up_kernel, tgrid, kUpThreads, 0, st, a);
+  const int fgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks);
+  void (*up)(UpArgs) = nullptr;
+  void (*fin)(UpArgs) = nullptr;
+  if (want_acc && want_h) {
+    up = order ? forest_up_kernel<true, true, 1> : forest_up_kernel<true, true, 0>;
+    fin = order ? forest_fin_kernel<true, true, 1> : forest_fin_kernel<true, true, 0>;
+  } else if (want_acc) {
+    up = order ? forest_up_kernel<true, false, 1> : forest_up_kernel<true, false, 0>;
+    fin = order ? forest_fin_kernel<true, false, 1> : forest_fin_kernel<true, false, 0>;
+  } else {
+    up = order ? forest_up_kernel<false, true, 1> : forest_up_kernel<false, true, 0>;
+    fin = order ? forest_fin_kernel<false, true, 1> : forest_fin_kernel<false, true, 0>;
+  }
+  TT_LAUNCH(up, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(coarse_link_kernel, lg, 256, 0, st, w.elist, w.counters + 0, dir,
             g.m, order, w.xmap, w.xsteps, w.link, w.ccell);
-  TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.counters + 0, w.ccell, w.leaves,
+  TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.counters + 0, w.ccell, w.link, w.leaves,
             w.counters + 1);
   TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1, w.link,
             w.ccell, w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
   TT_LAUNCH(coarse_scatter_kernel, lg, 256, 0, st, w.counters + 0, w.elist, w.ccell,
             w.cell);
   a.phase = 3;
-  TT_LAUNCH(forest_fin_kernel, (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks),
-            kUpThreads, 0, st, a);
+  TT_LAUNCH(fin, fgrid, kUpThreads, 0, st, a);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
