@@ -317,7 +317,8 @@ def batch_leg(dev, reps=3, rank=0, world=1, dist=None):
            "batched_ms": batched, "per_dem_ms": per, "speedup": per / batched,
            "batched_gcells_s": cells / (batched * 1e-3) / 1e9,
            "canvas": [info["canvas_rows"], info["canvas_cols"]],
-           "graph_nodes": info["graph_nodes"], "tuned_canvas_cols": best["canvas_cols"]}
+           "graph_nodes": info["graph_nodes"], "tuned_canvas_cols": best["canvas_cols"],
+           "tuned_schedule": best["schedule"], "tuning": cands}
     if world > 1:
         res["sharding"] = {"ranks": world, "rule": "largest first to least loaded rank",
                            "pixels_per_rank": shard.loads(all_shapes, world),

@@ -83,6 +83,15 @@ TT_CUDA_API void tt_cuda_release_workspace(void);
 TT_CUDA_API int64_t tt_cuda_launch_count(int reset);
 /** Device rounds used by the last fill / gwdt call on this thread. */
 TT_CUDA_API int64_t tt_cuda_last_rounds(void);
+/** Sweep schedule of the tile relaxations (fill, reconstruct, gwdt) for this
+ *  thread's later calls; no counterpart in the reference.  Bit 0 runs each
+ *  round's row sweeps before its column sweeps, bit 1 ends a tile visit
+ *  after 8 sweeps (the tile publishes what changed and queues itself
+ *  again).  Results are identical for every schedule; only the time
+ *  differs.  A value outside 0..3 restores the default (the environment
+ *  variable TT_CUDA_RELAX_SCHEDULE, else 0).  A batch takes the schedule in
+ *  effect when its graph is captured (its first run). */
+TT_CUDA_API void tt_cuda_set_relax_schedule(int schedule);
 /** Self-check (no counterpart in the reference): the three-instruction
  *  division by sqrtf(2) that the direction kernels use against the IEEE
  *  division, over every float32 input.  *mismatches receives the number of

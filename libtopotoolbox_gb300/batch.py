@@ -9,9 +9,13 @@ directions -> unit accumulation with one launch per stage for the whole
 batch; the first run with a set of tensors is captured into a CUDA graph
 that later runs with the same tensors replay.
 
-The tuning parameter is the mosaic width.  `tune()` times a few candidate
-widths on the actual batch and stores the fastest, keyed by the batch's
-shapes, in a JSON cache (``TT_CUDA_AUTOTUNE_CACHE`` or
+The tuning parameters are the mosaic width (the shape of the canvas the
+DEMs are packed into) and the sweep schedule of the tile relaxations (fill
+and gwdt: column or row sweeps first, visits run to local convergence or
+capped at 8 sweeps; see tt_cuda_set_relax_schedule).  `tune()` times
+candidate widths on the actual batch, then every schedule at the best
+width, and stores the fastest pair, keyed by the batch's shapes, in a JSON
+cache (``TT_CUDA_AUTOTUNE_CACHE`` or
 ``~/.cache/libtopotoolbox_gb300/autotune.json``).
 """
 from __future__ import annotations
@@ -26,6 +30,7 @@ from pathlib import Path
 from . import _native as N
 
 CANDIDATE_SCALES = (0.8, 1.0, 1.25, 1.6)
+SCHEDULES = (0, 1, 2, 3)
 
 
 def cache_path() -> Path:
@@ -61,11 +66,15 @@ def _store_cache(key, value):
 class Batch:
     """A planned batch.  `shapes` are (nrows, ncols) per DEM."""
 
-    def __init__(self, shapes, canvas_cols: int | None = None):
+    def __init__(self, shapes, canvas_cols: int | None = None, schedule: int | None = None):
         self.shapes = [(int(a), int(b)) for a, b in shapes]
+        tuned = _load_cache().get(signature(self.shapes), {})
         if canvas_cols is None:
-            canvas_cols = _load_cache().get(signature(self.shapes), {}).get("canvas_cols", 0)
+            canvas_cols = tuned.get("canvas_cols", 0)
+        if schedule is None:
+            schedule = tuned.get("schedule", 0)
         self.canvas_cols = int(canvas_cols)
+        self.schedule = int(schedule)
         lib = N.lib()
         dims = (C.c_int64 * (2 * len(self.shapes)))(*[v for s in self.shapes for v in s])
         h = C.c_void_p()
@@ -110,23 +119,28 @@ class Batch:
         keep = [arr(dems), arr(bcs)] + [arr(outputs.get(k)) for k in
                                         ("filled", "flats", "dist", "direction", "acc")]
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        N.check(N.lib().tt_cuda_batch_run(self._h, *[C.cast(a, C.c_void_p) if a is not None
+        lib = N.lib()
+        lib.tt_cuda_set_relax_schedule(self.schedule)  # taken when the graph is captured
+        try:
+            N.check(lib.tt_cuda_batch_run(self._h, *[C.cast(a, C.c_void_p) if a is not None
                                                      else None for a in keep],
                                           C.c_void_p(st)), "batch_run")
+        finally:
+            lib.tt_cuda_set_relax_schedule(-1)
         return outputs
 
 
-def tune(shapes, dems, bcs, reps: int = 2, scales=CANDIDATE_SCALES):
-    """Time candidate mosaic widths on this batch; cache and return the best."""
+def tune(shapes, dems, bcs, reps: int = 2, scales=CANDIDATE_SCALES, schedules=SCHEDULES):
+    """Time candidate mosaic widths (schedule 0), then every sweep schedule
+    at the best width, on this batch; cache and return the fastest."""
     import torch
 
     area = sum((a + 1) * (b + 1) for a, b in shapes)
     base = math.sqrt(area * 1.15)
-    best = None
     results = []
-    for sc in scales:
-        cols = int(base * sc)
-        bt = Batch(shapes, canvas_cols=cols)
+
+    def measure(cols, sched):
+        bt = Batch(shapes, canvas_cols=cols, schedule=sched)
         out = bt.run(dems, bcs)  # plain run + capture
         torch.cuda.synchronize()
         ts = []
@@ -137,13 +151,24 @@ def tune(shapes, dems, bcs, reps: int = 2, scales=CANDIDATE_SCALES):
             b.record()
             torch.cuda.synchronize()
             ts.append(a.elapsed_time(b))
-        ms = min(ts)
         info = bt.info()
-        results.append({"canvas_cols": info["canvas_cols"], "ms": ms,
-                        "canvas_pixels": info["canvas_rows"] * info["canvas_cols"]})
-        if best is None or ms < best["ms"]:
-            best = results[-1]
         bt.close()
-    _store_cache(signature(shapes), {"canvas_cols": best["canvas_cols"], "ms": best["ms"],
+        results.append({"canvas_cols": info["canvas_cols"], "schedule": sched, "ms": min(ts),
+                        "canvas_pixels": info["canvas_rows"] * info["canvas_cols"]})
+        return results[-1]
+
+    best = None
+    for sc in scales:
+        r = measure(int(base * sc), 0)
+        if best is None or r["ms"] < best["ms"]:
+            best = r
+    for sched in schedules:
+        if sched == 0:
+            continue
+        r = measure(best["canvas_cols"], sched)
+        if r["ms"] < best["ms"]:
+            best = r
+    _store_cache(signature(shapes), {"canvas_cols": best["canvas_cols"],
+                                     "schedule": best["schedule"], "ms": best["ms"],
                                      "candidates": results})
     return best, results

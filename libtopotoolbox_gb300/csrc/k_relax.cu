@@ -295,7 +295,15 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
     sweep_gwdt_run<ALONG_C>(t, lane, dir, nd, dm_all);
 }
 
-template <int KIND>
+// Sweep schedules (a template parameter, picked at run time): bit 0 runs the
+// row sweeps (right, left) of a round before the column sweeps (down, up);
+// bit 1 caps a visit at kCapSweeps sweeps, after which the tile publishes
+// what changed and queues itself again, so that neighbours see partial
+// results sooner.
+constexpr int kSchedules = 4;
+constexpr int kCapSweeps = 8;
+
+template <int KIND, int SCHED>
 __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
 
 // The warp that made every warp idle (idle word `seen` after its arrival):
@@ -308,7 +316,7 @@ __device__ void check_done(const RelaxArgs &a, int lane, int T, unsigned long lo
   if (*(volatile unsigned long long *)&a.ctl->idle == seen) atomicExch(&a.ctl->done, 1);
 }
 
-template <int KIND>
+template <int KIND, int SCHED>
 __global__ void __launch_bounds__(kWarps * 32)
 relax_persistent_kernel(RelaxArgs a) {
   __shared__ WarpTile tiles[kWarps];
@@ -360,7 +368,7 @@ relax_persistent_kernel(RelaxArgs a) {
         got = __shfl_sync(0xffffffffu, got, 0);
         if (!got) continue;
         did = true;
-        relax_tile<KIND>(a, t, lane, tile, got);
+        relax_tile<KIND, SCHED>(a, t, lane, tile, got);
       }
     }
     if (did) {
@@ -395,7 +403,7 @@ relax_persistent_kernel(RelaxArgs a) {
 }
 
 // Relaxes one tile to its local fixpoint and marks changed neighbours dirty.
-template <int KIND>
+template <int KIND, int SCHED>
 __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode) {
   const int ti = tile % a.tm, tj = tile / a.tm;
   const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
@@ -464,25 +472,10 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
   // Sweep until no pixel is marked for re-evaluation: the local fixpoint.
   // Down and up run in the column layout, right and left in the row layout
   // (the marks are transposed between the two).
+  constexpr int kCap = (SCHED & 2) ? kCapSweeps : kMaxSweeps;
   bool done = false;
   int sweeps = 0;
-  while (sweeps < kMaxSweeps) {
-    if (!__any_sync(0xffffffffu, nd != 0)) {
-      done = true;
-      break;
-    }
-    sweep<KIND, false>(t, lane, +1, nd, dm);
-    sweeps++;
-    if (!__any_sync(0xffffffffu, nd != 0)) {
-      done = true;
-      break;
-    }
-    sweep<KIND, false>(t, lane, -1, nd, dm);
-    sweeps++;
-    if (!__any_sync(0xffffffffu, nd != 0)) {
-      done = true;
-      break;
-    }
+  auto rows = [&]() {  // right and left in the row layout
     uint32_t ndr = transpose32(nd, lane), dmr = 0;
     sweep<KIND, true>(t, lane, +1, ndr, dmr);
     sweeps++;
@@ -492,6 +485,34 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
     }
     nd = transpose32(ndr, lane);
     dm |= transpose32(dmr, lane);
+  };
+  while (sweeps < kCap) {
+    if (!__any_sync(0xffffffffu, nd != 0)) {
+      done = true;
+      break;
+    }
+    if (SCHED & 1) {
+      rows();
+      if (!__any_sync(0xffffffffu, nd != 0)) {
+        done = true;
+        break;
+      }
+    }
+    sweep<KIND, false>(t, lane, +1, nd, dm);
+    sweeps++;
+    if (!__any_sync(0xffffffffu, nd != 0)) {
+      done = true;
+      break;
+    }
+    sweep<KIND, false>(t, lane, -1, nd, dm);
+    sweeps++;
+    if (!(SCHED & 1)) {
+      if (!__any_sync(0xffffffffu, nd != 0)) {
+        done = true;
+        break;
+      }
+      rows();
+    }
   }
 
   // Write back changed cells (coalesced per column: lane = row).
@@ -708,7 +729,7 @@ int elementwise_grid(int64_t N) {
 // (cudaErrorCooperativeLaunchTooLarge), so no warp waits for a block that
 // cannot be scheduled -- for example while other work holds some SMs.  The
 // grid never exceeds the occupancy bound computed for this kernel.
-template <int KIND>
+template <int KIND, int SCHED>
 cudaError_t launch_relax(int grid, const RelaxArgs &ra, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
@@ -721,7 +742,7 @@ cudaError_t launch_relax(int grid, const RelaxArgs &ra, cudaStream_t st) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   note_launch();
-  return cudaLaunchKernelEx(&cfg, relax_persistent_kernel<KIND>, ra);
+  return cudaLaunchKernelEx(&cfg, relax_persistent_kernel<KIND, SCHED>, ra);
 }
 
 // Host driver: mark the starting tiles, run one persistent launch, read the
@@ -760,18 +781,28 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
               flats, g.m, g.n, ra);
   }
   TT_CHECK(cudaGetLastError());
-  static int blocks_per_sm[2] = {0, 0};
-  if (!blocks_per_sm[KIND]) {
+  const int sched = relax_schedule();
+  static int blocks_per_sm[2][kSchedules] = {};
+  if (!blocks_per_sm[KIND][sched]) {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND>,
-                                                  kWarps * 32, 0);
-    blocks_per_sm[KIND] = b > 0 ? b : 1;
+    switch (sched) {
+      case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 1>, kWarps * 32, 0); break;
+      case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 2>, kWarps * 32, 0); break;
+      case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 3>, kWarps * 32, 0); break;
+      default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 0>, kWarps * 32, 0); break;
+    }
+    blocks_per_sm[KIND][sched] = b > 0 ? b : 1;
   }
   // No more warps than tiles (each warp owns at least one tile).
-  int grid = sm_count() * blocks_per_sm[KIND];
+  int grid = sm_count() * blocks_per_sm[KIND][sched];
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
-  TT_CHECK(launch_relax<KIND>(grid, ra, st));
+  switch (sched) {
+    case 1: TT_CHECK((launch_relax<KIND, 1>(grid, ra, st))); break;
+    case 2: TT_CHECK((launch_relax<KIND, 2>(grid, ra, st))); break;
+    case 3: TT_CHECK((launch_relax<KIND, 3>(grid, ra, st))); break;
+    default: TT_CHECK((launch_relax<KIND, 0>(grid, ra, st))); break;
+  }
   if (KIND == GWDT)
     TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
@@ -885,12 +916,12 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   ra.max_visits = (unsigned long long)T *
                   (unsigned long long)std::min<int64_t>(max_rounds(), 1LL << 20);
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<FILL>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<FILL, 0>,
                                                 kWarps * 32, 0);
   int grid = sm_count() * (b > 0 ? b : 1);
   grid = std::max(1, std::min(grid, (T + kWarps - 1) / kWarps));
   ra.visit_flush = visit_flush(ra.max_visits, grid * kWarps);
-  TT_CHECK(launch_relax<FILL>(grid, ra, st));
+  TT_CHECK((launch_relax<FILL, 0>(grid, ra, st)));
   QueueCtl h;  // read back into host stack memory: no pinned allocation
   TT_CHECK(cudaMemcpyAsync(&h, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));

@@ -159,6 +159,8 @@ Workspace &workspace();          // of the current device (or the override)
 void set_workspace_override(Workspace *ws);
 void *pinned_scratch();          // 4 KiB of pinned host memory per device
 int64_t max_rounds();
+// Sweep schedule of the relaxations (0..3) for this thread's calls.
+int relax_schedule();
 void set_last_rounds(int64_t r);
 
 // RAII lock of the current device's call mutex.

@@ -18,6 +18,7 @@ thread_local int64_t g_launches = 0;
 thread_local int64_t g_last_rounds = 0;
 thread_local StatusSink *g_sink = nullptr;
 thread_local Workspace *g_ws_override = nullptr;
+thread_local int g_relax_schedule = -1;  // -1: the environment's or 0
 int64_t g_max_rounds_override = 0;
 
 constexpr int kMaxDevices = 64;
@@ -48,6 +49,15 @@ void set_status(tt_cuda_status s) { g_status = s; }
 tt_cuda_status get_status() { return g_status; }
 void note_launch(int count) { g_launches += count; }
 void set_last_rounds(int64_t r) { g_last_rounds = r; }
+int relax_schedule() {
+  if (g_relax_schedule >= 0) return g_relax_schedule;
+  static const int env = [] {
+    const char *s = std::getenv("TT_CUDA_RELAX_SCHEDULE");
+    const int v = s ? std::atoi(s) : 0;
+    return (v >= 0 && v < 4) ? v : 0;
+  }();
+  return env;
+}
 
 StatusSink *status_sink() { return g_sink; }
 void set_status_sink(StatusSink *sink) { g_sink = sink; }
@@ -279,6 +289,10 @@ int64_t tt_cuda_launch_count(int reset) {
 }
 
 int64_t tt_cuda_last_rounds(void) { return g_last_rounds; }
+
+void tt_cuda_set_relax_schedule(int schedule) {
+  g_relax_schedule = (schedule >= 0 && schedule < 4) ? schedule : -1;
+}
 
 }  // extern "C"
 

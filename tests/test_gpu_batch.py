@@ -35,9 +35,10 @@ def test_batch_matches_single_calls(gpu, tmp_path, monkeypatch):
     dems = [_t(d, torch) for d, _ in tiles]
     bcs = [_t(b, torch) for _, b in tiles]
     best, results = tune(shapes, dems, bcs, reps=1, scales=(0.9, 1.3))
-    assert len(results) == 2
-    bt = Batch(shapes)  # picks the tuned width from the cache
+    assert len(results) == 2 + 3  # two widths, then the other three schedules
+    bt = Batch(shapes)  # picks the tuned width and schedule from the cache
     assert bt.info()["canvas_cols"] == best["canvas_cols"]
+    assert bt.schedule == best["schedule"]
     first = bt.run(dems, bcs)
     torch.cuda.synchronize()
     snap = {k: [t.clone() for t in v] for k, v in first.items()}
@@ -95,3 +96,32 @@ def test_batch_workload_sample_vs_oracle(gpu, port, tmp_path, monkeypatch):
         assert np.array_equal(out["direction"][k].cpu().numpy().T, r["direction"]), (pick[k], "dir")
         assert np.array_equal(out["acc"][k].cpu().numpy().T, r["acc"]), (pick[k], "acc")
     bt.close()
+
+
+def test_batch_every_schedule_same_bits(gpu, tmp_path, monkeypatch):
+    """The sweep schedules the tuner chooses between change only the time:
+    every schedule gives the same outputs, bit for bit."""
+    torch = gpu
+    monkeypatch.setenv("TT_CUDA_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    from libtopotoolbox_gb300.batch import Batch
+
+    tiles = _tiles(count=10, seed=21)
+    shapes = [d.shape for d, _ in tiles]
+    dems = [_t(d, torch) for d, _ in tiles]
+    bcs = [_t(b, torch) for _, b in tiles]
+    ref = None
+    for sched in range(4):
+        bt = Batch(shapes, schedule=sched)
+        out = bt.run(dems, bcs)
+        torch.cuda.synchronize()
+        got = {k: [t.cpu().numpy() for t in v] for k, v in out.items()}
+        bt.close()
+        if ref is None:
+            ref = got
+            continue
+        for k in ref:
+            for a, b in zip(ref[k], got[k]):
+                if a.dtype.kind == "f":
+                    assert same_float(a, b), (sched, k)
+                else:
+                    assert np.array_equal(a, b), (sched, k)
