@@ -92,14 +92,6 @@ TT_CUDA_API int64_t tt_cuda_last_rounds(void);
  *  variable TT_CUDA_RELAX_SCHEDULE, else 0).  A batch takes the schedule in
  *  effect when its graph is captured (its first run). */
 TT_CUDA_API void tt_cuda_set_relax_schedule(int schedule);
-/** Self-check (no counterpart in the reference): the three-instruction
- *  division by sqrtf(2) that the direction kernels use against the IEEE
- *  division, over every float32 input.  *mismatches receives the number of
- *  inputs whose bits differ (0 expected), *first_bad the smallest such bit
- *  pattern (0xffffffff when none). */
-TT_CUDA_API tt_cuda_status tt_cuda_selftest_div_sqrt2(unsigned long long *mismatches,
-                                                      unsigned *first_bad);
-
 /* ------------------------------------------------------------------ */
 /* Drop-in host-pointer entry points                                    */
 /* ------------------------------------------------------------------ */

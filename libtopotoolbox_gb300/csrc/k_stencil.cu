@@ -176,10 +176,10 @@ __global__ void sum_slots_kernel(const unsigned long long *__restrict__ slots,
 // a one-pixel halo (NaN off the grid) and the centre flat bits.  Compute:
 // thread (tx, ty) takes column tx, rows 4 ty .. 4 ty + 3, reading the 3 x 6
 // neighbourhood of its strip once into registers.  The neighbour order is a
-// template parameter, so every offset is a compile-time constant; the
-// division of a diagonal difference by sqrt(2) (div_by_sqrt2, bit-identical
-// to the IEEE division) runs only when the difference itself beats the best
-// slope so far (fl(diff / sqrt(2)) <= diff, so otherwise it cannot win).
+// template parameter, so every offset is a compile-time constant; the IEEE
+// division of a diagonal difference by sqrt(2) runs only when the
+// difference itself beats the best slope so far (fl(diff / sqrt(2)) <= diff,
+// so otherwise it cannot win).
 // The direction bytes go out through shared memory in coalesced rows.
 template <unsigned ORDER>
 __global__ void __launch_bounds__(kBlockX * kBlockY)
@@ -252,6 +252,7 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
   __syncthreads();
   // Off-grid neighbours hold NaN: their slope is NaN and never selected,
   // exactly as the reference skips them, so no bounds checks are needed.
+  const float sq2 = 1.41421353816986083984375f;  // sqrtf(2.0f) = 0x3FB504F3
   {
     const int c = tx, r0 = 4 * ty;  // centre (c + 1, r0 + 1 + u) in halo coordinates
     float z[3][6], d[3][6];
@@ -281,7 +282,7 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
         // skip higher neighbours; a difference that does not beat the best
         // (or is NaN) cannot win, since a diagonal's quotient is <= diff
         if (zn > zc || !(diff > best)) continue;
-        const float g = (k & 1) ? div_by_sqrt2(diff) : diff;
+        const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
         if (g > best) {
           best = g;
           dv = 1u << k;

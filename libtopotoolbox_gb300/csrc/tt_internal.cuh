@@ -59,25 +59,6 @@ __host__ __device__ __forceinline__ int d8_dj(int k, unsigned order) {
 // (src/flow_accumulation.c:63-67).
 __device__ __forceinline__ int d8_bit(unsigned d) { return 31 - __clz(d); }
 
-// x / sqrtf(2) rounded to nearest, bit-identical to __fdiv_rn(x, sqrtf(2))
-// (verified for every float32 input by tt_cuda_selftest_div_sqrt2), in three
-// instructions instead of a full IEEE division: Markstein's correction step
-// for division by a constant (P. Markstein, "IA-64 and Elementary
-// Functions", 2000, ch. 8): with r = RN(1/s), q0 = RN(x r) is within an ulp
-// of x / s, the residual x - q0 s is exact in one fused multiply-add, and
-// q1 = RN(q0 + r (x - q0 s)) is the correctly rounded quotient.  Infinite x
-// keep q0 (the residual would be NaN); below 2^-120 the quotient or the
-// residual can leave the normal range, where the residual is no longer
-// exact, so those rare inputs take the IEEE division.
-__device__ __forceinline__ float div_by_sqrt2(float x) {
-  constexpr float s = 1.41421353816986083984375f;   // sqrtf(2.0f) = 0x3FB504F3
-  constexpr float r = 0.707106769084930419921875f;  // RN(1 / s)   = 0x3F3504F3
-  if (fabsf(x) < 0x1p-120f) return __fdiv_rn(x, s);
-  const float q0 = __fmul_rn(x, r);
-  const float q1 = __fmaf_rn(__fmaf_rn(-q0, s, x), r, q0);
-  return isinf(x) ? q0 : q1;
-}
-
 // Slot in a list appended to by many threads: the threads that call it
 // together take consecutive slots with one atomic on the shared counter
 // (one per group of converged threads, not one per element, so a counter
