@@ -84,13 +84,17 @@ TT_CUDA_API int64_t tt_cuda_launch_count(int reset);
 /** Device rounds used by the last fill / gwdt call on this thread. */
 TT_CUDA_API int64_t tt_cuda_last_rounds(void);
 /** Sweep schedule of the tile relaxations (fill, reconstruct, gwdt) for this
- *  thread's later calls; no counterpart in the reference.  Bit 0 runs each
- *  round's row sweeps before its column sweeps, bit 1 ends a tile visit
- *  after 8 sweeps (the tile publishes what changed and queues itself
- *  again).  Results are identical for every schedule; only the time
- *  differs.  A value outside 0..3 restores the default (the environment
- *  variable TT_CUDA_RELAX_SCHEDULE, else 0).  A batch takes the schedule in
- *  effect when its graph is captured (its first run). */
+ *  thread's later calls; no counterpart in the reference.  0..3: bit 0 runs
+ *  each round's row sweeps before its column sweeps, bit 1 ends a tile
+ *  visit after 8 sweeps (the tile publishes what changed and queues itself
+ *  again).  4 and 5 order tile visits by value: only tiles whose lowest
+ *  incoming value is at or below a global threshold run, and the threshold
+ *  rises band by band (bands of 1/8 and 1/2 of the value, at least 1 and 4
+ *  units) when every warp has run out of eligible tiles.  Results are
+ *  identical for every schedule; only the time differs.  A value outside
+ *  0..5 restores the default (the environment variable
+ *  TT_CUDA_RELAX_SCHEDULE, else 0).  A batch takes the schedule in effect
+ *  when its graph is captured (its first run). */
 TT_CUDA_API void tt_cuda_set_relax_schedule(int schedule);
 /* ------------------------------------------------------------------ */
 /* Drop-in host-pointer entry points                                    */

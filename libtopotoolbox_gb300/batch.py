@@ -12,7 +12,8 @@ that later runs with the same tensors replay.
 The tuning parameters are the mosaic width (the shape of the canvas the
 DEMs are packed into) and the sweep schedule of the tile relaxations (fill
 and gwdt: column or row sweeps first, visits run to local convergence or
-capped at 8 sweeps; see tt_cuda_set_relax_schedule).  `tune()` times
+capped at 8 sweeps, or visits ordered by value in bands; see
+tt_cuda_set_relax_schedule).  `tune()` times
 candidate widths on the actual batch, then every schedule at the best
 width, and stores the fastest pair, keyed by the batch's shapes, in a JSON
 cache (``TT_CUDA_AUTOTUNE_CACHE`` or
@@ -30,7 +31,7 @@ from pathlib import Path
 from . import _native as N
 
 CANDIDATE_SCALES = (0.8, 1.0, 1.25, 1.6)
-SCHEDULES = (0, 1, 2, 3)
+SCHEDULES = (0, 1, 2, 3, 4, 5)
 
 
 def cache_path() -> Path:

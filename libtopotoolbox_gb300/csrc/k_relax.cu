@@ -68,6 +68,7 @@ struct QueueCtl {
   unsigned long long idle;    // wakes << 32 | warps that found nothing to do
   int done;                   // set once every warp is idle and no flag is set
   int abort;                  // ABORT_* bits
+  int thresh;                 // ordered schedules: tiles with priority <= thresh run
 };
 
 enum : int { ABORT_SPIN = 1, ABORT_VISITS = 2 };
@@ -83,7 +84,22 @@ struct RelaxArgs {
   int *dirty;  // per tile: nonzero while waiting to be relaxed
   unsigned long long max_visits;
   int visit_flush;  // a warp adds its visits to ctl->visits in batches of this
+  int *prio;        // ordered schedules: per tile, the key of the lowest value
+                    // published into it since it was last taken (kClean: none)
+  int *wmin;        // ordered schedules: per warp, the lowest priority among
+                    // its waiting tiles at its last pass (kClean: none)
 };
+
+// Order-preserving integer key of a float (key order == value order).
+__device__ __forceinline__ int value_key(float x) {
+  const int b = __float_as_int(x);
+  return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float key_value(int k) {
+  return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff);
+}
+constexpr int kClean = 0x7f7f7f7f;        // no priority (above every finite key)
+constexpr int kUrgent = (int)0x80000000;  // below every key: runs at any threshold
 
 // Dirty flag bits: 1 = a halo pixel changed (re-evaluate the edge ring),
 // 2 = evaluate every pixel (first visit, or a visit that hit its sweep cap).
@@ -299,12 +315,42 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
 // row sweeps (right, left) of a round before the column sweeps (down, up);
 // bit 1 caps a visit at kCapSweeps sweeps, after which the tile publishes
 // what changed and queues itself again, so that neighbours see partial
-// results sooner.
-constexpr int kSchedules = 4;
+// results sooner.  Schedules 4 and 5 order the visits by value (delta
+// stepping over tiles): a tile carries the lowest value published into it,
+// and only tiles at or below a global threshold run; when every warp is
+// idle and some tile is still waiting, the threshold rises to the lowest
+// waiting value plus a band (a fraction of that value, at least a fixed
+// step: 1/8 and 1 for schedule 4, 1/2 and 4 for schedule 5).  Both updates
+// only lower values and any order reaches the same fixpoint, so every
+// schedule gives the same bits; ordering trades idle time at band
+// boundaries for fewer repeated lowerings of the same pixels.
+constexpr int kSchedules = 6;
 constexpr int kCapSweeps = 8;
+constexpr bool ordered_sched(int s) { return s >= 4; }
+__device__ __forceinline__ int band_above(int key, int sched) {
+  const float v = key_value(key);
+  if (!(v > -INFINITY)) return value_key(-3.4028234663852886e38f);  // -INF or NaN
+  const float rel = sched == 5 ? 0.5f : 0.125f, step = sched == 5 ? 4.0f : 1.0f;
+  const float nv = v + fmaxf(fabsf(v) * rel, step);
+  return value_key(nv);
+}
 
 template <int KIND, int SCHED>
 __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, int mode);
+
+// Ordered schedules: with every warp idle, raise the threshold above the
+// lowest priority any warp reported waiting.  Returns false when no warp
+// reported waiting work.
+template <int SCHED>
+__device__ bool raise_threshold(const RelaxArgs &a, int lane, int W, int thr) {
+  int g = kClean;
+  for (int w = lane; w < W; w += 32) g = min(g, *(volatile int *)&a.wmin[w]);
+  g = __reduce_min_sync(0xffffffffu, g);
+  if (g == kClean) return false;
+  const int nt = band_above(g, SCHED);
+  if (lane == 0 && nt > thr) atomicMax(&a.ctl->thresh, nt);
+  return true;
+}
 
 // The warp that made every warp idle (idle word `seen` after its arrival):
 // finish the run if no flag is set and no warp has woken since.
@@ -328,8 +374,12 @@ relax_persistent_kernel(RelaxArgs a) {
   long long spins = 0;
   bool idle = false;                 // counted in ctl->idle (warp-uniform)
   unsigned long long unflushed = 0;  // lane 0: visits not yet added to ctl
+  int posted = kClean;               // ordered: this warp's last wmin entry
+  int raised_at = kUrgent;           // ordered: threshold this warp last raised from
   for (;;) {
     if (*(volatile int *)&a.ctl->abort || *(volatile int *)&a.ctl->done) break;
+    const int thr = ordered_sched(SCHED) ? *(volatile int *)&a.ctl->thresh : 0;
+    int lane_wait = kClean;  // ordered: lowest priority of this lane's waiting tiles
     if (lane == 0) {
       if (unflushed >= (unsigned long long)a.visit_flush) {
         atomicAdd(&a.ctl->visits, unflushed);
@@ -342,7 +392,15 @@ relax_persistent_kernel(RelaxArgs a) {
     for (int base = wid; base < T; base += W * 32) {
       const int mine = base + lane * W;
       int f = (mine < T) ? *(volatile int *)&a.dirty[mine] : 0;
-      unsigned mask = __ballot_sync(0xffffffffu, f != 0);
+      bool elig = f != 0;
+      if (ordered_sched(SCHED) && elig) {
+        const int pr = *(volatile int *)&a.prio[mine];
+        elig = pr <= thr;
+        // a flag whose priority was cleared by a take racing its publication
+        // waits with the highest priority short of "none"
+        if (!elig) lane_wait = min(lane_wait, pr == kClean ? kClean - 1 : pr);
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, elig);
       if (mask && idle) {  // wake: leave the idle count before taking a flag
         if (lane == 0) {
           const unsigned long long before =
@@ -359,6 +417,9 @@ relax_persistent_kernel(RelaxArgs a) {
         const int tile = base + l * W;
         int got = 0;
         if (lane == 0) {
+          // ordered: clear the priority before taking the flag, so a value
+          // published in between keeps a priority (at worst a stale one)
+          if (ordered_sched(SCHED)) atomicExch(&a.prio[tile], kClean);
           got = atomicExch(&a.dirty[tile], 0);
           if (got) {
             unflushed++;
@@ -371,13 +432,19 @@ relax_persistent_kernel(RelaxArgs a) {
         relax_tile<KIND, SCHED>(a, t, lane, tile, got);
       }
     }
+    int wait_min = kClean;
+    if (ordered_sched(SCHED)) {  // report this warp's waiting work
+      wait_min = __reduce_min_sync(0xffffffffu, lane_wait);
+      if (lane == 0 && wait_min != posted) *(volatile int *)&a.wmin[wid] = wait_min;
+      posted = wait_min;
+    }
     if (did) {
       spins = 0;
       continue;
     }
     if (!idle) {
       idle = true;
-      fence_acq_rel_gpu();  // every lane: its flags before the idle mark
+      fence_acq_rel_gpu();  // every lane: its flags (and wait report) before the idle mark
       __syncwarp();
       unsigned long long seen = 0;
       if (lane == 0) {
@@ -385,8 +452,18 @@ relax_persistent_kernel(RelaxArgs a) {
         if ((unsigned)seen == (unsigned)W) fence_acq_rel_gpu();  // all flags visible
       }
       seen = __shfl_sync(0xffffffffu, seen, 0);
-      if ((unsigned)seen == (unsigned)W) check_done(a, lane, T, seen);
+      if ((unsigned)seen == (unsigned)W) {
+        if (!ordered_sched(SCHED) || !raise_threshold<SCHED>(a, lane, W, thr))
+          check_done(a, lane, T, seen);
+        raised_at = thr;
+      }
       continue;
+    }
+    if (ordered_sched(SCHED) && wait_min != kClean && raised_at != thr &&
+        (unsigned)*(volatile unsigned long long *)&a.ctl->idle == (unsigned)W) {
+      // every warp idle and this one still waiting: open the next band
+      raise_threshold<SCHED>(a, lane, W, thr);
+      raised_at = thr;
     }
     int stop = 0;
     if (lane == 0) {
@@ -472,7 +549,7 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
   // Sweep until no pixel is marked for re-evaluation: the local fixpoint.
   // Down and up run in the column layout, right and left in the row layout
   // (the marks are transposed between the two).
-  constexpr int kCap = (SCHED & 2) ? kCapSweeps : kMaxSweeps;
+  constexpr int kCap = (!ordered_sched(SCHED) && (SCHED & 2)) ? kCapSweeps : kMaxSweeps;
   bool done = false;
   int sweeps = 0;
   auto rows = [&]() {  // right and left in the row layout
@@ -491,7 +568,7 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
       done = true;
       break;
     }
-    if (SCHED & 1) {
+    if (!ordered_sched(SCHED) && (SCHED & 1)) {
       rows();
       if (!__any_sync(0xffffffffu, nd != 0)) {
         done = true;
@@ -506,7 +583,7 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
     }
     sweep<KIND, false>(t, lane, -1, nd, dm);
     sweeps++;
-    if (!(SCHED & 1)) {
+    if (ordered_sched(SCHED) || !(SCHED & 1)) {
       if (!__any_sync(0xffffffffu, nd != 0)) {
         done = true;
         break;
@@ -557,9 +634,22 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
   // pattern): a warp that takes a flag and fences sees every store made
   // before it.
   if (!__any_sync(0xffffffffu, tgt >= 0)) return;
+  int key = kUrgent;
+  if (ordered_sched(SCHED)) {  // the lowest changed value on the tile's edges
+    float v = INFINITY;
+    if (dm & 1u) v = fminf(v, t.s[lane + 1][1]);
+    if ((dm >> 31) & 1u) v = fminf(v, t.s[lane + 1][kTile]);
+    if ((left >> lane) & 1u) v = fminf(v, t.s[1][lane + 1]);
+    if ((right >> lane) & 1u) v = fminf(v, t.s[kTile][lane + 1]);
+    key = __reduce_min_sync(0xffffffffu, value_key(v));
+    if (tgt >= 0 && val == DIRTY_FULL) key = kUrgent;  // a capped visit resumes at once
+  }
   fence_acq_rel_gpu();
   __syncwarp();
-  if (tgt >= 0) atomicOr(&a.dirty[tgt], val);
+  if (tgt >= 0) {
+    if (ordered_sched(SCHED)) atomicMin(&a.prio[tgt], key);
+    atomicOr(&a.dirty[tgt], val);
+  }
 }
 
 // f = dem where bc == 1 (and where dem is NaN), +INF elsewhere
@@ -568,12 +658,16 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
 // +INF throughout and already at its local fixpoint until a neighbour
 // publishes a change (plain stores: idempotent).
 // Marks dirty the tiles whose pixels or halo hold pixel (i, j).
-__device__ __forceinline__ void mark_tiles_around(int *dirty, int tm, int64_t i, int64_t j,
-                                                  int64_t m, int64_t n) {
+// (Ordered schedules: those tiles also get the most urgent priority.)
+__device__ __forceinline__ void mark_tiles_around(int *dirty, int *prio, int tm, int64_t i,
+                                                  int64_t j, int64_t m, int64_t n) {
   const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
   const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
   for (int tj = tj0; tj <= tj1; tj++)
-    for (int ti = ti0; ti <= ti1; ti++) dirty[tj * tm + ti] = DIRTY_FULL;
+    for (int ti = ti0; ti <= ti1; ti++) {
+      dirty[tj * tm + ti] = DIRTY_FULL;
+      if (prio) prio[tj * tm + ti] = kUrgent;
+    }
 }
 
 // Elements per thread and loop trip of the elementwise kernels: their loads
@@ -582,7 +676,7 @@ constexpr int kEw = 4;
 
 __global__ void fill_init_kernel(float *__restrict__ f, const float *__restrict__ dem,
                                  const uint8_t *__restrict__ bc, int64_t m, int64_t n,
-                                 int *__restrict__ dirty, int tm) {
+                                 int *__restrict__ dirty, int *__restrict__ prio, int tm) {
   const int64_t N = m * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N; p0 += kEw * stride) {
@@ -600,7 +694,7 @@ __global__ void fill_init_kernel(float *__restrict__ f, const float *__restrict_
       if (p >= N) continue;
       const bool seed = b[u] == 1 || isnan(z[u]);
       f[p] = seed ? z[u] : INFINITY;
-      if (seed && dirty) mark_tiles_around(dirty, tm, p % m, p / m, m, n);
+      if (seed && dirty) mark_tiles_around(dirty, prio, tm, p % m, p / m, m, n);
     }
   }
 }
@@ -625,10 +719,12 @@ __global__ void negate_kernel(float *__restrict__ out, const float *__restrict__
     out[p] = -in[p];
 }
 
-// Mark every tile dirty (fill starts everywhere).
-__global__ void dirty_all_kernel(int *dirty, int n) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+// Mark every tile dirty (fill starts everywhere), most urgent.
+__global__ void dirty_all_kernel(int *dirty, int *prio, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     dirty[t] = DIRTY_FULL;
+    if (prio) prio[t] = kUrgent;
+  }
 }
 
 // gwdt working arrays: distance 1 at presills and +INF at other flats, as
@@ -657,7 +753,7 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ w
       const int32_t f = fv[u];
       dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
       wcost[p] = (f & 1) ? cv[u] : NAN;
-      if ((f & 5) == 5) mark_tiles_around(qa.dirty, qa.tm, p % m, p / m, m, n);
+      if ((f & 5) == 5) mark_tiles_around(qa.dirty, qa.prio, qa.tm, p % m, p / m, m, n);
     }
   }
 }
@@ -753,18 +849,29 @@ template <int KIND>
 tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
                          const GridDims &g, cudaStream_t st, const uint8_t *bc = nullptr) {
   const int T = g.tiles();
+  const int sched = relax_schedule();
+  const bool ordered = sched >= 4;
+  const int wmax = sm_count() * 32 * kWarps;  // more warp slots than any grid has warps
   Workspace &ws = workspace();
   size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
   if (KIND == GWDT) need += align_up((size_t)g.cells() * 4);
+  if (ordered) need += align_up((size_t)T * 4) + align_up((size_t)wmax * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
   int *dirty = (int *)ws.take((size_t)T * 4);
   // gwdt relaxes over a copy of the costs with NaN at non-flat pixels
   float *wcost = KIND == GWDT ? (float *)ws.take((size_t)g.cells() * 4) : nullptr;
+  int *prio = ordered ? (int *)ws.take((size_t)T * 4) : nullptr;
+  int *wmin = ordered ? (int *)ws.take((size_t)wmax * 4) : nullptr;
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
   if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  RelaxArgs ra{state, KIND == GWDT ? wcost : aux, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
+  RelaxArgs ra{state, KIND == GWDT ? wcost : aux, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1,
+               prio, wmin};
+  if (ordered) {  // no priorities, no waiting work (kClean = 0x7f7f7f7f)
+    TT_CHECK(cudaMemsetAsync(prio, 0x7f, (size_t)T * 4, st));
+    TT_CHECK(cudaMemsetAsync(wmin, 0x7f, (size_t)wmax * 4, st));
+  }
   const int64_t cap_rounds = max_rounds();
   ra.max_visits = (unsigned long long)T * (unsigned long long)std::min<int64_t>(cap_rounds, 1LL << 20);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
@@ -772,16 +879,15 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   if (KIND == FILL && bc) {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, aux, bc, g.m,
-              g.n, dirty, g.tm);
+              g.n, dirty, prio, g.tm);
   } else if (KIND == FILL) {
-    TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, T);
+    TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, prio, T);
   } else {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, wcost, aux,
               flats, g.m, g.n, ra);
   }
   TT_CHECK(cudaGetLastError());
-  const int sched = relax_schedule();
   static int blocks_per_sm[2][kSchedules] = {};
   if (!blocks_per_sm[KIND][sched]) {
     int b = 0;
@@ -789,6 +895,8 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
       case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 1>, kWarps * 32, 0); break;
       case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 2>, kWarps * 32, 0); break;
       case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 3>, kWarps * 32, 0); break;
+      case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 4>, kWarps * 32, 0); break;
+      case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 5>, kWarps * 32, 0); break;
       default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, relax_persistent_kernel<KIND, 0>, kWarps * 32, 0); break;
     }
     blocks_per_sm[KIND][sched] = b > 0 ? b : 1;
@@ -801,6 +909,8 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
     case 1: TT_CHECK((launch_relax<KIND, 1>(grid, ra, st))); break;
     case 2: TT_CHECK((launch_relax<KIND, 2>(grid, ra, st))); break;
     case 3: TT_CHECK((launch_relax<KIND, 3>(grid, ra, st))); break;
+    case 4: TT_CHECK((launch_relax<KIND, 4>(grid, ra, st))); break;
+    case 5: TT_CHECK((launch_relax<KIND, 5>(grid, ra, st))); break;
     default: TT_CHECK((launch_relax<KIND, 0>(grid, ra, st))); break;
   }
   if (KIND == GWDT)
@@ -908,11 +1018,11 @@ tt_cuda_status fill_noalloc(float *f, const float *dem, const uint8_t *bc,
   int *dirty = (int *)base + kNoAllocHeaderWords;
   const int T = g.tiles();
   TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, f, dem, bc, g.m,
-            g.n, nullptr, g.tm);
+            g.n, nullptr, nullptr, g.tm);
   TT_CHECK(cudaMemsetAsync(ctl, 0, sizeof(QueueCtl), st));
-  TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, T);
+  TT_LAUNCH(dirty_all_kernel, (T + 255) / 256, 256, 0, st, dirty, (int *)nullptr, T);
   TT_CHECK(cudaGetLastError());
-  RelaxArgs ra{f, dem, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1};
+  RelaxArgs ra{f, dem, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1, nullptr, nullptr};
   ra.max_visits = (unsigned long long)T *
                   (unsigned long long)std::min<int64_t>(max_rounds(), 1LL << 20);
   int b = 0;

@@ -25,24 +25,41 @@ constexpr int kBlockY = 8;   // along j
 // (the scatter at src/identifyflats.c:83-119 restated as a gather).
 //
 // One 32 x 32 output tile per block of 32 x 8 threads: the DEM is staged
-// with a two-pixel halo (NaN off the grid), flat bits are computed for the
-// tile plus a one-pixel ring, then thread (tx, ty) gathers for column tx,
-// rows 4 ty .. 4 ty + 3 from a 3 x 6 neighbourhood read once into
-// registers; the flags go out through shared memory in coalesced columns.
-// Each block adds its flat count to one of kCountSlots counters (spread so
-// that blocks do not queue on one address), which a last step sums.
+// with a two-pixel halo (NaN off the grid).  Thread (tx, ty) takes column
+// tx, rows 4 ty .. 4 ty + 3, and reads the 3 x 6 neighbourhood of that strip
+// once into registers: it serves both the flat test of the four pixels and
+// their sill / presill gather.  The flat bits of the one-pixel ring around
+// the tile (132 pixels) are computed one per thread.  A strip with no flat
+// pixel in its neighbourhood is all zeros (a non-flat pixel needs a flat
+// neighbour to be a sill).  The flags go out through shared memory in
+// coalesced columns, and each block adds its flat count to one of
+// kCountSlots counters (spread so that blocks do not queue on one address),
+// which a last step sums.
 // ------------------------------------------------------------------
 __device__ __forceinline__ float nan_to_neg_inf(float v) { return v != v ? -INFINITY : v; }
 
 constexpr int kFz = kTile + 4;  // staged DEM side (two-pixel halo)
-constexpr int kFf = kTile + 2;  // flat bits side (one-pixel ring)
+constexpr int kFr = 4;          // flat-bit row r of the tile is stored at r + kFr
+constexpr int kFp = 44;         // flat-bit column pitch (bytes): rows -1 .. 32 at 3 .. 36,
+                                // conflict-free 32-bit reads (44 / 4 = 11 is odd)
 constexpr int kCountSlots = 64;
+
+// Flat test of the pixel whose 3 x 3 neighbourhood is (a0 a1 a2 | b0 b1 b2 |
+// c0 c1 c2), centre b1: not NaN and no neighbour lower (NaN counts as -INF).
+__device__ __forceinline__ bool is_flat(float a0, float a1, float a2, float b0, float b1,
+                                        float b2, float c0, float c1, float c2) {
+  const float lo = fminf(fminf(fminf(nan_to_neg_inf(a0), nan_to_neg_inf(a1)),
+                               fminf(nan_to_neg_inf(a2), nan_to_neg_inf(b0))),
+                         fminf(fminf(nan_to_neg_inf(b2), nan_to_neg_inf(c0)),
+                               fminf(nan_to_neg_inf(c1), nan_to_neg_inf(c2))));
+  return b1 == b1 && !(lo < b1);
+}
 
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, int64_t m,
                      int64_t n, unsigned long long *slots) {
-  __shared__ float zs[kFz][kFz + 1];                 // [c][r]: dem at (i0 - 2 + r, j0 - 2 + c)
-  __shared__ __align__(4) uint8_t fs[kFf][kFf + 2];  // [c][r]: flat at (i0 - 1 + r, j0 - 1 + c)
+  __shared__ float zs[kFz][kFz + 1];                   // [c][r]: dem at (i0 - 2 + r, j0 - 2 + c)
+  __shared__ __align__(4) uint8_t fs[kTile + 2][kFp];  // [c + 1][r + kFr]: flat at (i0 + r, j0 + c)
   __shared__ int32_t os[kTile][kTile + 1];
   __shared__ unsigned wsum[kBlockY];
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -83,55 +100,77 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
       }
   }
   __syncthreads();
-  // flat bits of the tile and its ring: interior pixel, not NaN, and no
-  // neighbour lower (a NaN neighbour counts as -INF)
-  const int64_t ilo = 1 - (i0 - 1), ihi = (m - 1) - (i0 - 1);  // interior rows: ilo <= r < ihi
-  const int64_t jlo = 1 - (j0 - 1), jhi = (n - 1) - (j0 - 1);
-  for (int c = ty; c < kFf; c += kBlockY)
+  // interior pixels may be flat: global row 1 .. m - 2, column 1 .. n - 2
+  auto interior = [&](int r, int c) {  // tile coordinates
+    const int64_t i = i0 + r, j = j0 + c;
+    return i >= 1 && i < m - 1 && j >= 1 && j < n - 1;
+  };
+  const int c = tx, r0 = 4 * ty;
+  float z[3][6];  // tile columns c - 1 .. c + 1, rows r0 - 1 .. r0 + 4
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int r = tx + h * kBlockX;
-      if (r >= kFf) continue;
-      const float zc = zs[c + 1][r + 1];
-      const float lo = fminf(
-          fminf(fminf(nan_to_neg_inf(zs[c][r]), nan_to_neg_inf(zs[c][r + 1])),
-                fminf(nan_to_neg_inf(zs[c][r + 2]), nan_to_neg_inf(zs[c + 1][r]))),
-          fminf(fminf(nan_to_neg_inf(zs[c + 1][r + 2]), nan_to_neg_inf(zs[c + 2][r])),
-                fminf(nan_to_neg_inf(zs[c + 2][r + 1]), nan_to_neg_inf(zs[c + 2][r + 2]))));
-      const bool f = r >= ilo && r < ihi && c >= jlo && c < jhi && zc == zc && !(lo < zc);
-      fs[c][r] = (uint8_t)f;
+  for (int dc = 0; dc < 3; dc++)
+#pragma unroll
+    for (int u = 0; u < 6; u++) z[dc][u] = zs[c + 1 + dc][r0 + 1 + u];
+  {  // flat bits of the strip, one aligned word
+    uint32_t w = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (interior(r0 + u, c) && is_flat(z[0][u], z[0][u + 1], z[0][u + 2], z[1][u], z[1][u + 1],
+                                         z[1][u + 2], z[2][u], z[2][u + 1], z[2][u + 2]))
+        w |= 1u << (8 * u);
+    *reinterpret_cast<uint32_t *>(&fs[c + 1][r0 + kFr]) = w;
+  }
+  {  // flat bits of the ring: rows -1 and 32 (columns -1 .. 32), columns -1
+     // and 32 (rows 0 .. 31)
+    const int k = ty * kBlockX + tx;
+    if (k < 2 * (kTile + 2) + 2 * kTile) {
+      int rr, cc;
+      if (k < kTile + 2) { rr = -1; cc = k - 1; }
+      else if (k < 2 * (kTile + 2)) { rr = kTile; cc = k - (kTile + 2) - 1; }
+      else if (k < 2 * (kTile + 2) + kTile) { cc = -1; rr = k - 2 * (kTile + 2); }
+      else { cc = kTile; rr = k - 2 * (kTile + 2) - kTile; }
+      const int zc = cc + 2, zr = rr + 2;  // staged coordinates of the pixel
+      const bool f = interior(rr, cc) &&
+                     is_flat(zs[zc - 1][zr - 1], zs[zc - 1][zr], zs[zc - 1][zr + 1],
+                             zs[zc][zr - 1], zs[zc][zr], zs[zc][zr + 1], zs[zc + 1][zr - 1],
+                             zs[zc + 1][zr], zs[zc + 1][zr + 1]);
+      fs[cc + 1][rr + kFr] = (uint8_t)f;
     }
+  }
   __syncthreads();
   // sill / presill: a neighbour of the other kind at the same elevation
   unsigned cnt = 0;
   {
-    const int c = tx, r0 = 4 * ty;
-    uint32_t f[3][2];
-    float z[3][6];
+    uint32_t fb[3];  // flat bits of rows r0 - 1 .. r0 + 4 (bit u) of the three columns
 #pragma unroll
     for (int dc = 0; dc < 3; dc++) {
-      f[dc][0] = *reinterpret_cast<const uint32_t *>(&fs[c + dc][r0]);
-      f[dc][1] = *reinterpret_cast<const uint32_t *>(&fs[c + dc][r0 + 4]);
-#pragma unroll
-      for (int u = 0; u < 6; u++) z[dc][u] = zs[c + 1 + dc][r0 + 1 + u];
+      const uint8_t *col = fs[c + dc];
+      const uint32_t w0 = *reinterpret_cast<const uint32_t *>(col + r0);
+      const uint32_t w1 = *reinterpret_cast<const uint32_t *>(col + r0 + 4);
+      const uint32_t w2 = *reinterpret_cast<const uint32_t *>(col + r0 + 8);
+      fb[dc] = ((w0 >> 24) & 1u) | ((w1 & 1u) << 1) | (((w1 >> 8) & 1u) << 2) |
+               (((w1 >> 16) & 1u) << 3) | (((w1 >> 24) & 1u) << 4) | ((w2 & 1u) << 5);
     }
+    if (fb[0] | fb[1] | fb[2]) {
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int uc = u + 1;  // centre row in the 6-row window
-      const unsigned fc = (f[1][uc >> 2] >> (8 * (uc & 3))) & 1u;
-      const float z1 = z[1][uc];
-      bool hit = false;
+      for (int u = 0; u < 4; u++) {
+        const int uc = u + 1;
+        const unsigned fc = (fb[1] >> uc) & 1u;
+        const float z1 = z[1][uc];
+        bool hit = false;
 #pragma unroll
-      for (int dc = 0; dc < 3; dc++)
+        for (int dc = 0; dc < 3; dc++)
 #pragma unroll
-        for (int du = -1; du <= 1; du++) {
-          if (dc == 1 && du == 0) continue;
-          const int w = uc + du;
-          const unsigned fn = (f[dc][w >> 2] >> (8 * (w & 3))) & 1u;
-          hit |= (fn != fc) & (z[dc][w] == z1);
-        }
-      os[c][r0 + u] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
-      if (i0 + r0 + u < m && j0 + c < n) cnt += fc;
+          for (int du = -1; du <= 1; du++) {
+            if (dc == 1 && du == 0) continue;
+            hit |= (((fb[dc] >> (uc + du)) & 1u) != fc) & (z[dc][uc + du] == z1);
+          }
+        os[c][r0 + u] = (int32_t)(fc | (hit ? (fc ? 4u : 2u) : 0u));
+        cnt += fc;
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; u++) os[c][r0 + u] = 0;
     }
   }
   __syncthreads();
@@ -140,9 +179,9 @@ identifyflats_kernel(int32_t *__restrict__ out, const float *__restrict__ dem, i
     if (i < m)
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const int c = ty + k * kBlockY;
-        const int64_t j = j0 + c;
-        if (j < n) out[j * m + i] = os[c][tx];
+        const int cc = ty + k * kBlockY;
+        const int64_t j = j0 + cc;
+        if (j < n) out[j * m + i] = os[cc][tx];
       }
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);

@@ -54,7 +54,7 @@ int relax_schedule() {
   static const int env = [] {
     const char *s = std::getenv("TT_CUDA_RELAX_SCHEDULE");
     const int v = s ? std::atoi(s) : 0;
-    return (v >= 0 && v < 4) ? v : 0;
+    return (v >= 0 && v < 6) ? v : 0;
   }();
   return env;
 }
@@ -291,7 +291,7 @@ int64_t tt_cuda_launch_count(int reset) {
 int64_t tt_cuda_last_rounds(void) { return g_last_rounds; }
 
 void tt_cuda_set_relax_schedule(int schedule) {
-  g_relax_schedule = (schedule >= 0 && schedule < 4) ? schedule : -1;
+  g_relax_schedule = (schedule >= 0 && schedule < 6) ? schedule : -1;
 }
 
 }  // extern "C"

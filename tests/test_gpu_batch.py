@@ -35,7 +35,7 @@ def test_batch_matches_single_calls(gpu, tmp_path, monkeypatch):
     dems = [_t(d, torch) for d, _ in tiles]
     bcs = [_t(b, torch) for _, b in tiles]
     best, results = tune(shapes, dems, bcs, reps=1, scales=(0.9, 1.3))
-    assert len(results) == 2 + 3  # two widths, then the other three schedules
+    assert len(results) == 2 + 5  # two widths, then the other five schedules
     bt = Batch(shapes)  # picks the tuned width and schedule from the cache
     assert bt.info()["canvas_cols"] == best["canvas_cols"]
     assert bt.schedule == best["schedule"]
@@ -110,7 +110,7 @@ def test_batch_every_schedule_same_bits(gpu, tmp_path, monkeypatch):
     dems = [_t(d, torch) for d, _ in tiles]
     bcs = [_t(b, torch) for _, b in tiles]
     ref = None
-    for sched in range(4):
+    for sched in range(6):
         bt = Batch(shapes, schedule=sched)
         out = bt.run(dems, bcs)
         torch.cuda.synchronize()
