@@ -115,13 +115,12 @@ __device__ __forceinline__ int run_start(uint32_t starts, int b) {
 
 struct CclTile {
   // Union-find over run ids (column * 32 + first row); once every run knows
-  // its root, the root slots hold per-component reductions: the maximum
-  // depth key, then the smallest pixel attaining it.
+  // its root, the same slots hold per-root reductions: the maximum depth
+  // key, then the smallest pixel attaining it.
   int lab[kTile * kTile];
-  int rkey[kTile * kTile];       // per run: maximum depth key (INT_MIN: none)
-  int16_t rarg[kTile * kTile];   // per run: first pixel attaining it
-  int16_t rroot[kTile * kTile];  // per run: its component's root run
-  uint32_t starts[kTile];        // run starts of each column
+  int key[kTile * kTile];    // per pixel: depth key (INT_MIN: none)
+  int16_t root[kTile * kTile];  // per pixel: local root, -1 for non-flats
+  uint32_t starts[kTile];    // run starts of each column
 };
 
 // One warp per tile.  Each lane owns one column's flat mask (32 bits): a
@@ -169,19 +168,10 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
           const float d = __fsub_rn(fl[u], og[u]);
           if (!isnan(d)) k = ordered_key(d);
         }
+        t.key[jj * kTile + lane] = k;
+        t.root[jj * kTile + lane] = -1;
         const uint32_t b = __ballot_sync(0xffffffffu, f);
         if (lane == jj) my_mask = b;
-        if (!b) continue;
-        // per vertical run of this column: the maximum key and the first
-        // row attaining it, at the run's start slot
-        const int rs = f ? run_start(b & ~(b << 1), lane) : -1 - lane;
-        const unsigned grp = __match_any_sync(0xffffffffu, rs);
-        const int rk = __reduce_max_sync(grp, k);
-        const unsigned at = __ballot_sync(0xffffffffu, f && k == rk) & grp;
-        if (f && lane == rs) {
-          t.rkey[jj * kTile + rs] = rk;
-          t.rarg[jj * kTile + rs] = (int16_t)(rk == INT_MIN ? -1 : jj * kTile + __ffs(at) - 1);
-        }
       }
     }
     {  // the tile's edge flat masks for the border pass: top and bottom row
@@ -203,13 +193,18 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       continue;
     }
     if (full && __all_sync(0xffffffffu, my_mask == 0xffffffffu)) {
-      // one component; its root is run 0 (column 0, row 0) at pixel (i0, j0);
-      // each column is one run starting at row 0 (lane = column here)
-      __syncwarp();
-      const int ck = t.rkey[lane * kTile];
-      const int kmax = __reduce_max_sync(0xffffffffu, ck);
-      const int first = __reduce_min_sync(  // smallest tile index attaining it
-          0xffffffffu, (kmax != INT_MIN && ck == kmax) ? (int)t.rarg[lane * kTile] : INT_MAX);
+      // one component; its root is run 0 (column 0, row 0) at pixel (i0, j0)
+      int kmax = INT_MIN;
+      for (int jj = 0; jj < kTile; jj++) kmax = max(kmax, t.key[jj * kTile + lane]);
+      kmax = __reduce_max_sync(0xffffffffu, kmax);
+      int first = INT_MAX;  // smallest tile index attaining the maximum
+      if (kmax != INT_MIN)
+        for (int jj = 0; jj < kTile; jj++)
+          if (t.key[jj * kTile + lane] == kmax) {
+            first = jj * kTile + lane;
+            break;
+          }
+      first = __reduce_min_sync(0xffffffffu, first);
       const int64_t rootp = j0 * m + i0;
       for (int jj = 0; jj < kTile; jj++) {
         const int64_t gp = (j0 + jj) * m + i;
@@ -251,10 +246,13 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       }
     }
     __syncwarp();
-    // lane = column: every run learns its root; roots reset their slot
+    // lane = column: every pixel of a run takes the run's root; roots reset
+    // their reduction slot
     for (uint32_t s = S; s; s &= s - 1) {
       const int s0 = __ffs(s) - 1;
-      t.rroot[lane * kTile + s0] = (int16_t)sfind(t.lab, lane * kTile + s0);
+      const int r = sfind(t.lab, lane * kTile + s0);
+      const uint32_t rm = run_mask(M, s0);
+      for (uint32_t b = rm; b; b &= b - 1) t.root[lane * kTile + __ffs(b) - 1] = (int16_t)r;
     }
     __syncwarp();
     {  // local roots: reset their reduction slot and list them (one
@@ -262,7 +260,7 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       uint32_t rs = 0;
       for (uint32_t s = S; s; s &= s - 1) {
         const int loc = lane * kTile + __ffs(s) - 1;
-        if (t.rroot[loc] == loc) {
+        if (t.root[loc] == loc) {
           t.lab[loc] = INT_MIN;
           rs |= s & (~s + 1u);
         }
@@ -282,41 +280,42 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         roots[base++] = (int)((j0 + lane) * m + (i0 + __ffs(b) - 1));
     }
     __syncwarp();
-    for (uint32_t s = S; s; s &= s - 1) {  // component maxima over runs
-      const int loc = lane * kTile + __ffs(s) - 1;
-      if (t.rkey[loc] != INT_MIN) atomicMax(&t.lab[t.rroot[loc]], t.rkey[loc]);
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc], k = t.key[loc];
+      if (r >= 0 && k != INT_MIN) atomicMax(&t.lab[r], k);
     }
     __syncwarp();
-    for (uint32_t s = S; s; s &= s - 1) {  // runs attaining their maximum
-      const int loc = lane * kTile + __ffs(s) - 1, r = t.rroot[loc];
-      const int cm = t.lab[r];
-      if (r == loc) {  // the root keeps the maximum aside (in lmax)
-        const int64_t ri = i0 + loc % kTile, rj = j0 + loc / kTile;
-        lmax[rj * m + ri] = cm;
-      }
-      t.rkey[loc] = (cm != INT_MIN && t.rkey[loc] == cm) ? (int)t.rarg[loc] : INT_MAX;
+    for (int jj = 0; jj < kTile; jj++) {  // per pixel: its component's maximum
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      if (r >= 0 && t.key[loc] != INT_MIN && t.key[loc] == t.lab[r]) t.key[loc] = INT_MAX;
     }
     __syncwarp();
-    for (uint32_t s = S; s; s &= s - 1) {
-      const int loc = lane * kTile + __ffs(s) - 1;
-      if (t.rroot[loc] == loc) t.lab[loc] = INT_MAX;
+    // roots: keep the maximum aside (in lmax) and turn the slot into an argmin
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      const int64_t j = j0 + jj;
+      if (r == loc && i < m && j < n) lmax[j * m + i] = t.lab[loc];
     }
     __syncwarp();
-    for (uint32_t s = S; s; s &= s - 1) {  // the smallest pixel attaining it
-      const int loc = lane * kTile + __ffs(s) - 1;
-      if (t.rkey[loc] != INT_MAX) atomicMin(&t.lab[t.rroot[loc]], t.rkey[loc]);
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane;
+      if (t.root[loc] == loc) t.lab[loc] = INT_MAX;
     }
     __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {  // lane = row
+    for (int jj = 0; jj < kTile; jj++) {
+      const int loc = jj * kTile + lane, r = t.root[loc];
+      if (r >= 0 && t.key[loc] == INT_MAX) atomicMin(&t.lab[r], loc);
+    }
+    __syncwarp();
+    for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       const bool in = i < m && j < n;
-      const uint32_t Mj = __shfl_sync(0xffffffffu, M, jj);
-      if (!in) continue;
       const int64_t gp = j * m + i;
       const int loc = jj * kTile + lane;
+      const int r = t.root[loc];
+      if (!in) continue;
       int v = -1;
-      if ((Mj >> lane) & 1u) {
-        const int r = t.rroot[jj * kTile + run_start(Mj & ~(Mj << 1), lane)];
+      if (r >= 0) {
         v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
         if (r == loc) {
           const int a = t.lab[loc];

@@ -123,29 +123,6 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-// Brings tile `tile`'s state and aux (with halo) towards L2 while the warp
-// relaxes another tile, so that staging it later does not wait on DRAM:
-// lane c prefetches the lines of halo column c (and of columns 32, 33 for
-// lanes 0, 1).
-__device__ __forceinline__ void prefetch_tile(const RelaxArgs &a, int tile, int lane) {
-  const int ti = tile % a.tm, tj = tile / a.tm;
-  const int64_t i0 = (int64_t)ti * kTile - 1;
-  const int64_t ic = i0 < 0 ? 0 : i0;
-  for (int c = lane; c < kHalo; c += 32) {
-    const int64_t j = (int64_t)tj * kTile - 1 + c;
-    if (j < 0 || j >= a.n) continue;
-    const int64_t p = j * a.m + ic;
-    const int64_t q = j * a.m + (i0 + kHalo - 1 < a.m ? i0 + kHalo - 1 : a.m - 1);
-    const int64_t mid = p + 32 < q ? p + 32 : q;  // a column spans up to three lines
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.state + p));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.state + mid));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.state + q));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.aux + p));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.aux + mid));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.aux + q));
-  }
-}
-
 // Transpose of a 32 x 32 bit matrix held one row per lane.
 __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
   uint32_t y = 0;
@@ -438,7 +415,6 @@ relax_persistent_kernel(RelaxArgs a) {
         const int l = __ffs(mask) - 1;
         mask &= mask - 1;
         const int tile = base + l * W;
-        if (mask) prefetch_tile(a, base + (__ffs(mask) - 1) * W, lane);
         int got = 0;
         if (lane == 0) {
           // ordered: clear the priority before taking the flag, so a value
