@@ -96,6 +96,38 @@ TT_CUDA_API int64_t tt_cuda_last_rounds(void);
  *  TT_CUDA_RELAX_SCHEDULE, else 0).  A batch takes the schedule in effect
  *  when its graph is captured (its first run). */
 TT_CUDA_API void tt_cuda_set_relax_schedule(int schedule);
+/** Deferred status for this thread's device-pointer calls; no counterpart
+ *  in the reference.  Without it, every tt_cuda_*_dev call synchronises its
+ *  stream before it returns, to report the iteration cap, a cycle or an
+ *  invalid direction or weight.  Between tt_cuda_defer_begin(stream) and
+ *  tt_cuda_defer_end(), the calls of the D8 path on this thread
+ *  (fillsinks, reconstruct, identifyflats, gwdt_computecosts, gwdt,
+ *  flow_routing_d8_carve, flow_accumulation with or without weights,
+ *  gradient_secondorder, hillshade_fused, hillshade_backward, d8_pipeline)
+ *  only enqueue their work on `stream`: each stage's status words are copied
+ *  into a device record, and the call returns TT_CUDA_SUCCESS unless a check
+ *  on the host fails (arguments, allocation, a launch).  The results are the
+ *  same bits as without deferral.  tt_cuda_defer_end() copies the records
+ *  back, synchronises the stream once and returns the first failure
+ *  recorded (TT_CUDA_ERR_NOT_CONVERGED, TT_CUDA_ERR_CYCLE,
+ *  TT_CUDA_ERR_INVALID_ARGUMENT) or TT_CUDA_SUCCESS.
+ *   - A device-pointer call on this thread with another stream, while
+ *     deferral is on, returns TT_CUDA_ERR_INVALID_ARGUMENT (deferred calls
+ *     share private scratch ordered by that one stream).  Calls on another
+ *     device, and host-pointer calls, run as usual.
+ *   - The edge-list, drainage-basin, graphflood, file and adjoint
+ *     (flow_accumulation_backward) forms still wait for their own results
+ *     (they size outputs or test convergence on the host), and so for the
+ *     deferred work before them on the stream.
+ *   - Weighted accumulation under deferral computes its scales on the
+ *     device and keeps scratch for four passes (32 bytes per cell).
+ *   - tt_cuda_last_rounds() is not updated by deferred calls.
+ *   - 4096 stage records per deferral (a pipeline call takes three); a stage
+ *     past that reads its status back and synchronises as usual.
+ *  tt_cuda_defer_begin returns TT_CUDA_ERR_INVALID_ARGUMENT when deferral
+ *  is already on; tt_cuda_defer_end when it is not. */
+TT_CUDA_API tt_cuda_status tt_cuda_defer_begin(void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_defer_end(void);
 /* ------------------------------------------------------------------ */
 /* Drop-in host-pointer entry points                                    */
 /* ------------------------------------------------------------------ */

@@ -28,6 +28,8 @@ SIGNATURES = {
     "tt_cuda_launch_count": (I64, [C.c_int]),
     "tt_cuda_last_rounds": (I64, []),
     "tt_cuda_set_relax_schedule": (None, [C.c_int]),
+    "tt_cuda_defer_begin": (ST, [P]),
+    "tt_cuda_defer_end": (ST, []),
     # drop-in host-pointer forms
     "tt_cuda_fillsinks": (None, [P, P, P, PD]),
     "tt_cuda_fillsinks_hybrid": (None, [P, P, P, P, PD]),

@@ -14,6 +14,7 @@ on torch's current CUDA stream.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -357,6 +358,22 @@ class dev:  # namespace
     @staticmethod
     def _dims(t):
         return (t.shape[1], t.shape[0])
+
+    @staticmethod
+    @contextlib.contextmanager
+    def deferred():
+        """Defers the status checks of the D8 path's device calls in the block
+        (tt_cuda_defer_begin / tt_cuda_defer_end): they only enqueue their
+        work on torch's current stream, which must stay the same in the
+        block.  Leaving the block synchronises the stream once and raises
+        ``TTCudaError`` for the first failure any call recorded."""
+        N.check(N.lib().tt_cuda_defer_begin(dev._stream()), "defer_begin")
+        try:
+            yield
+        except BaseException:
+            N.lib().tt_cuda_defer_end()
+            raise
+        N.check(N.lib().tt_cuda_defer_end(), "defer_end")
 
     @staticmethod
     def _p(t):

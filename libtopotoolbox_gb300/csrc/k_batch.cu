@@ -39,7 +39,6 @@ struct tt_cuda_batch {
   std::vector<const void *> cap_ptr;     // pointers the graph was captured with
   float *dem = nullptr, *filled = nullptr, *costs = nullptr, *dist = nullptr, *acc = nullptr;
   int32_t *flats = nullptr;
-  ptrdiff_t *cc = nullptr;
   uint8_t *bc = nullptr, *dir = nullptr;
   int *d_sink = nullptr;
   int *h_sink = nullptr;
@@ -144,7 +143,7 @@ tt_cuda_status enqueue(tt_cuda_batch *b, cudaStream_t st) {
   tt_cuda_status s;
   if ((s = fill_dev(b->filled, b->dem, b->bc, g, st)) != TT_CUDA_SUCCESS) return s;
   if ((s = identifyflats_dev(b->flats, b->filled, g, nullptr, st)) != TT_CUDA_SUCCESS) return s;
-  if ((s = costs_dev(b->costs, b->cc, b->flats, b->dem, b->filled, g, st)) != TT_CUDA_SUCCESS)
+  if ((s = costs_dev(b->costs, nullptr, b->flats, b->dem, b->filled, g, st)) != TT_CUDA_SUCCESS)
     return s;
   if ((s = gwdt_dev(b->dist, nullptr, b->costs, b->flats, g, st)) != TT_CUDA_SUCCESS) return s;
   if ((s = directions_dev(b->dir, b->filled, b->dist, b->flats, g, 0, st)) != TT_CUDA_SUCCESS)
@@ -158,15 +157,7 @@ tt_cuda_status enqueue(tt_cuda_batch *b, cudaStream_t st) {
 
 // Status recorded by the deferred stages.
 tt_cuda_status read_sink(tt_cuda_batch *b, int records) {
-  for (int r = 0; r < records; r++) {
-    const int *rec = b->h_sink + r * kRecordInts;
-    if (rec[0] == REC_RELAX && rec[1] != 0) return TT_CUDA_ERR_NOT_CONVERGED;
-    if (rec[0] == REC_FOREST) {
-      if (rec[1] != rec[2] || (rec[3] & 1)) return TT_CUDA_ERR_CYCLE;
-      if (rec[3] & 6) return TT_CUDA_ERR_INVALID_ARGUMENT;
-    }
-  }
-  return TT_CUDA_SUCCESS;
+  return sink_status(b->h_sink, records);
 }
 
 void free_batch(tt_cuda_batch *b) {
@@ -181,7 +172,6 @@ void free_batch(tt_cuda_batch *b) {
   cudaFree(b->dist);
   cudaFree(b->acc);
   cudaFree(b->flats);
-  cudaFree(b->cc);
   cudaFree(b->bc);
   cudaFree(b->dir);
   cudaFree(b->d_sink);
@@ -246,7 +236,6 @@ tt_cuda_status tt_cuda_batch_create(int count, const ptrdiff_t *dims, int64_t ca
             cudaMalloc(&b->dist, N * 4) == cudaSuccess &&
             cudaMalloc(&b->acc, N * 4) == cudaSuccess &&
             cudaMalloc(&b->flats, N * 4) == cudaSuccess &&
-            cudaMalloc(&b->cc, N * 8) == cudaSuccess &&
             cudaMalloc(&b->bc, N) == cudaSuccess && cudaMalloc(&b->dir, N) == cudaSuccess &&
             cudaMalloc(&b->d_sink, (size_t)b->sink_cap * kRecordInts * 4) == cudaSuccess &&
             cudaMallocHost(&b->h_sink, (size_t)b->sink_cap * kRecordInts * 4) == cudaSuccess &&
@@ -305,58 +294,57 @@ tt_cuda_status tt_cuda_batch_run(tt_cuda_batch *b, const float *const *dem,
     return TT_CUDA_ERR_CUDA;
   }
   StatusSink sink{b->d_sink, b->sink_cap, 0};
-  set_status_sink(&sink);
-  set_workspace_override(&b->ws);
-  if (!b->exec || ptrs != b->cap_ptr) {
-    // A plain run sizes the private workspace and produces this call's
-    // result; the same sequence is then captured for later calls.
-    if (cudaMemcpyAsync(b->d_ptr, ptrs.data(), ptrs.size() * sizeof(void *),
-                        cudaMemcpyHostToDevice, b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
-    if (s == TT_CUDA_SUCCESS) s = enqueue(b, b->st);
-    const int records = sink.next;
-    if (s == TT_CUDA_SUCCESS &&
-        cudaMemcpyAsync(b->h_sink, b->d_sink, (size_t)records * kRecordInts * 4,
-                        cudaMemcpyDeviceToHost, b->st) != cudaSuccess)
-      s = TT_CUDA_ERR_CUDA;
-    if (cudaStreamSynchronize(b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
-    if (s == TT_CUDA_SUCCESS) s = read_sink(b, records);
-    if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED || s == TT_CUDA_ERR_CYCLE) {
-      if (b->exec) cudaGraphExecDestroy(b->exec);
-      b->exec = nullptr;
-      cudaGraph_t graph = nullptr;
-      sink.next = 0;
-      tt_cuda_status cs = TT_CUDA_SUCCESS;
-      if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-        cs = TT_CUDA_ERR_CUDA;
-      if (cs == TT_CUDA_SUCCESS) {
-        cs = enqueue(b, b->st);
-        cudaMemcpyAsync(b->h_sink, b->d_sink, (size_t)sink.next * kRecordInts * 4,
-                        cudaMemcpyDeviceToHost, b->st);
-        if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) cs = TT_CUDA_ERR_CUDA;
-      }
-      if (cs == TT_CUDA_SUCCESS &&
-          cudaGraphInstantiate(&b->exec, graph, 0) != cudaSuccess) cs = TT_CUDA_ERR_CUDA;
-      if (graph) {
-        size_t nn = 0;
-        cudaGraphGetNodes(graph, nullptr, &nn);
-        b->graph_nodes = (int64_t)nn;
-        cudaGraphDestroy(graph);
-      }
-      if (cs == TT_CUDA_SUCCESS) {
-        b->cap_ptr = ptrs;
-      } else {
-        cudaGetLastError();
+  {
+    SinkScope scope(&sink, &b->ws);
+    if (!b->exec || ptrs != b->cap_ptr) {
+      // A plain run sizes the private workspace and produces this call's
+      // result; the same sequence is then captured for later calls.
+      if (cudaMemcpyAsync(b->d_ptr, ptrs.data(), ptrs.size() * sizeof(void *),
+                          cudaMemcpyHostToDevice, b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
+      if (s == TT_CUDA_SUCCESS) s = enqueue(b, b->st);
+      const int records = sink.next;
+      if (s == TT_CUDA_SUCCESS &&
+          cudaMemcpyAsync(b->h_sink, b->d_sink, (size_t)records * kRecordInts * 4,
+                          cudaMemcpyDeviceToHost, b->st) != cudaSuccess)
+        s = TT_CUDA_ERR_CUDA;
+      if (cudaStreamSynchronize(b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
+      if (s == TT_CUDA_SUCCESS) s = read_sink(b, records);
+      if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED || s == TT_CUDA_ERR_CYCLE) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
-        b->cap_ptr.clear();
+        cudaGraph_t graph = nullptr;
+        sink.next = 0;
+        tt_cuda_status cs = TT_CUDA_SUCCESS;
+        if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+          cs = TT_CUDA_ERR_CUDA;
+        if (cs == TT_CUDA_SUCCESS) {
+          cs = enqueue(b, b->st);
+          cudaMemcpyAsync(b->h_sink, b->d_sink, (size_t)sink.next * kRecordInts * 4,
+                          cudaMemcpyDeviceToHost, b->st);
+          if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) cs = TT_CUDA_ERR_CUDA;
+        }
+        if (cs == TT_CUDA_SUCCESS &&
+            cudaGraphInstantiate(&b->exec, graph, 0) != cudaSuccess) cs = TT_CUDA_ERR_CUDA;
+        if (graph) {
+          size_t nn = 0;
+          cudaGraphGetNodes(graph, nullptr, &nn);
+          b->graph_nodes = (int64_t)nn;
+          cudaGraphDestroy(graph);
+        }
+        if (cs == TT_CUDA_SUCCESS) {
+          b->cap_ptr = ptrs;
+        } else {
+          cudaGetLastError();
+          b->exec = nullptr;
+          b->cap_ptr.clear();
+        }
       }
+    } else {
+      if (cudaGraphLaunch(b->exec, b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
+      if (cudaStreamSynchronize(b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
+      if (s == TT_CUDA_SUCCESS) s = read_sink(b, b->sink_cap);
     }
-  } else {
-    if (cudaGraphLaunch(b->exec, b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
-    if (cudaStreamSynchronize(b->st) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
-    if (s == TT_CUDA_SUCCESS) s = read_sink(b, b->sink_cap);
-  }
-  set_workspace_override(nullptr);
-  set_status_sink(nullptr);
+  }  // scope
   if (s == TT_CUDA_ERR_CUDA) cudaGetLastError();
   set_status(s);
   return s;

@@ -187,9 +187,7 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
     // general one below.
     const bool full = i0 + kTile <= m && j0 + kTile <= n;
     if (!__any_sync(0xffffffffu, my_mask != 0)) {
-      if (i < m)
-        for (int jj = 0; jj < kTile && j0 + jj < n; jj++) L[(j0 + jj) * m + i] = -1;
-      __syncwarp();
+      __syncwarp();  // no labels: L is only ever read at flat pixels
       continue;
     }
     if (full && __all_sync(0xffffffffu, my_mask == 0xffffffffu)) {
@@ -313,20 +311,16 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       const int64_t gp = j * m + i;
       const int loc = jj * kTile + lane;
       const int r = t.root[loc];
-      if (!in) continue;
-      int v = -1;
-      if (r >= 0) {
-        v = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
-        if (r == loc) {
-          const int a = t.lab[loc];
-          larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
-          maxkey[gp] = INT_MIN;
-          argmax[gp] = INT_MAX;
-        } else {
-          larg[gp] = -1;  // not a local root
-        }
+      if (!in || r < 0) continue;  // L is only ever read at flat pixels
+      if (r == loc) {
+        const int a = t.lab[loc];
+        larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
+        maxkey[gp] = INT_MIN;
+        argmax[gp] = INT_MAX;
+      } else {
+        larg[gp] = -1;  // not a local root
       }
-      L[gp] = v;
+      L[gp] = (int)((j0 + r / kTile) * m + (i0 + r % kTile));
     }
     __syncwarp();
   }
@@ -415,7 +409,9 @@ __global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ l
 
 // Four pixels per thread: each level of the dependent gather (a pixel's
 // local root, its global root, the root's maximum and argmax) is issued for
-// all four before any result is used.
+// all four before any result is used.  Labels are read at flat pixels only
+// (the labelling writes none elsewhere); `conncomps` may be null (the
+// pipeline needs the costs alone).
 constexpr int kCostPer = 4;
 
 __global__ void costs_kernel(float *__restrict__ costs,
@@ -437,10 +433,11 @@ __global__ void costs_kernel(float *__restrict__ costs,
       fv[u] = in ? flats[p] : 0;
       fl[u] = in ? filled[p] : 0.f;
       og[u] = in ? orig[p] : 0.f;
-      l1[u] = in ? L[p] : -1;
     }
 #pragma unroll
-    for (int u = 0; u < kCostPer; u++) R[u] = ((fv[u] & 1) && l1[u] >= 0) ? L[l1[u]] : -1;
+    for (int u = 0; u < kCostPer; u++) l1[u] = (fv[u] & 1) ? L[p0 + u * stride] : -1;
+#pragma unroll
+    for (int u = 0; u < kCostPer; u++) R[u] = l1[u] >= 0 ? L[l1[u]] : -1;
 #pragma unroll
     for (int u = 0; u < kCostPer; u++) {
       mk[u] = R[u] >= 0 ? maxkey[R[u]] : 0;
@@ -460,7 +457,7 @@ __global__ void costs_kernel(float *__restrict__ costs,
         lab = (am[u] == INT_MAX) ? R[u] : am[u];
       }
       costs[p] = c;
-      conncomps[p] = lab;
+      if (conncomps) conncomps[p] = lab;
     }
   }
 }

@@ -107,7 +107,19 @@ struct UpArgs {
   int *h_out;
   int *hmax;
   int *err;
+  // Deferred weighted sums: {passes, k1, d} computed on the device.  When
+  // set, this launch is pass `pass` (scale k1 + pass * d); a pass at or past
+  // `passes` does nothing, and a single-pass plan writes acc_out directly.
+  const int *plan;
+  int pass;
 };
+
+__device__ __forceinline__ bool pass_unused(const UpArgs &a) {
+  return a.plan && a.pass >= a.plan[0];
+}
+__device__ __forceinline__ int pass_shift(const UpArgs &a) {
+  return a.plan ? a.plan[1] + a.pass * a.plan[2] : a.wshift;
+}
 
 __device__ __forceinline__ long long to_fixed(float w, int k, int *err) {
   unsigned bits = __float_as_uint(w);
@@ -247,6 +259,8 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
   const int tid = threadIdx.x;
   const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
+  if (pass_unused(a)) return;
+  const int wshift = pass_shift(a);
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
@@ -277,7 +291,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       t.rl[e] = (int16_t)rl;
       bad |= rl == RL_BADDIR;
       if (rl >= 0) atomicAdd(&t.pend[rl], 1);
-      if (ACC) t.acc[e] = in ? (a.w ? to_fixed(a.w[g0 + u * gstep], a.wshift, a.err) : 1LL) : 0LL;
+      if (ACC) t.acc[e] = in ? (a.w ? to_fixed(a.w[g0 + u * gstep], wshift, a.err) : 1LL) : 0LL;
       if (H) t.h[e] = 0;
       nvalid += in;
     }
@@ -402,6 +416,10 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
   const int tid = threadIdx.x;
   const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
+  if (pass_unused(a)) return;
+  const int wshift = pass_shift(a);
+  // a deferred single-pass plan needs no combination: write floats
+  long long *const raw_out = (a.plan && a.plan[0] == 1) ? nullptr : a.raw_out;
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
@@ -456,11 +474,11 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
       if (ACC) {
         if (a.count_out) {
           a.count_out[gp] = (int)t.acc[e];
-        } else if (a.raw_out) {
-          a.raw_out[gp] = t.acc[e];
+        } else if (raw_out) {
+          raw_out[gp] = t.acc[e];
         } else {
           const float v = __ll2float_rn(t.acc[e]);
-          a.acc_out[gp] = a.wshift ? ldexpf(v, -a.wshift) : v;
+          a.acc_out[gp] = wshift ? ldexpf(v, -wshift) : v;
         }
       }
       if (H) {
@@ -598,14 +616,33 @@ __global__ void coarse_scatter_kernel(const int *__restrict__ ecount,
 // ------------------------------------------------------------------
 constexpr int kSmallBins = 256;
 
+// Bins of the height histogram, read on the device from the maximum height
+// of the contraction: heights 0 .. hmax, never more than N.  Heights outside
+// the bins (only possible when the contraction reported a cycle) are skipped.
+__device__ __forceinline__ int height_bins(const int *hmax, int64_t N) {
+  const int64_t H = (int64_t)*hmax + 1;
+  return (int)(H < N ? (H > 0 ? H : 0) : N);
+}
+
+__global__ void clear_bins_kernel(int *__restrict__ hist, int *__restrict__ cursor,
+                                  const int *__restrict__ hmax, int64_t N) {
+  const int H = height_bins(hmax, N);
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < H; b += gridDim.x * blockDim.x) {
+    hist[b] = 0;
+    cursor[b] = 0;
+  }
+}
+
 __global__ void h_hist_kernel(const int *__restrict__ h, int64_t N,
-                              int *__restrict__ hist) {
+                              int *__restrict__ hist, const int *__restrict__ hmax) {
   __shared__ int sb[kSmallBins];
+  const int H = height_bins(hmax, N);
   for (int b = threadIdx.x; b < kSmallBins; b += blockDim.x) sb[b] = 0;
   __syncthreads();
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
     int v = h[p];
+    if ((unsigned)v >= (unsigned)H) continue;
     if (v < kSmallBins) {
       atomicAdd(&sb[v], 1);
     } else {
@@ -619,11 +656,13 @@ __global__ void h_hist_kernel(const int *__restrict__ h, int64_t N,
     if (sb[b]) atomicAdd(&hist[b], sb[b]);
 }
 
-// Exclusive scan of n ints by one block of 1024 threads.
+// Exclusive scan of the height bins by one block of 1024 threads.
 __global__ void __launch_bounds__(1024) scan_kernel(const int *__restrict__ in,
-                                                    int *__restrict__ out, int n) {
+                                                    int *__restrict__ out,
+                                                    const int *__restrict__ hmax, int64_t N) {
   __shared__ int part[1024];
   const int tid = threadIdx.x;
+  const int n = height_bins(hmax, N);
   const int chunk = (n + 1023) / 1024;
   const int b0 = tid * chunk, b1 = min(n, b0 + chunk);
   int s = 0;
@@ -649,9 +688,11 @@ constexpr int kScatterPer = 8;  // elements per thread per chunk
 __global__ void node_scatter_kernel(const int *__restrict__ h, int64_t N,
                                     const int *__restrict__ off,
                                     int *__restrict__ cursor,
-                                    ptrdiff_t *__restrict__ node) {
+                                    ptrdiff_t *__restrict__ node,
+                                    const int *__restrict__ hmax) {
   __shared__ int cnt[kSmallBins];
   __shared__ int base[kSmallBins];
+  const int H = height_bins(hmax, N);
   // Chunks of blockDim * kScatterPer pixels: count small bins in shared
   // memory, reserve each bin's range once per chunk, then place.
   const int64_t chunk = (int64_t)blockDim.x * kScatterPer;
@@ -664,6 +705,7 @@ __global__ void node_scatter_kernel(const int *__restrict__ h, int64_t N,
     for (int u = 0; u < kScatterPer; u++) {
       const int64_t p = start + (int64_t)u * blockDim.x + threadIdx.x;
       v[u] = p < N ? h[p] : -1;
+      if (v[u] >= H) v[u] = -1;
     }
 #pragma unroll
     for (int u = 0; u < kScatterPer; u++)
@@ -936,7 +978,14 @@ __device__ __forceinline__ void dd_add_scaled(double &hi, double &lo, long long 
 // correction delta_i = R_i - (R_(i-1) << d) (mod 2^64, signed) at scale
 // 2^-(k1 + i d).
 __global__ void combine_passes_kernel(float *__restrict__ acc, const long long *__restrict__ R,
-                                      int passes, int64_t N, int k1, int d) {
+                                      int passes, int64_t N, int k1, int d,
+                                      const int *__restrict__ plan) {
+  if (plan) {  // deferred: the plan is on the device; one pass wrote acc itself
+    passes = plan[0];
+    k1 = plan[1];
+    d = plan[2];
+    if (passes <= 1) return;
+  }
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
     long long prev = R[p];
@@ -968,7 +1017,17 @@ struct UpWork {
   int *xmap, *xsteps, *elist, *leaves, *h;
   long long *raw;  // passes * N fixed-point totals (multi-scale sums only)
   int *counters;  // [0] ecount, [1] lcount, [2] processed, [3] hmax, [4] err
+  int *plan;      // [0..2] deferred weighted sums' {passes, k1, d}, [4..5] their range,
+                  // [8] the maximum height, kept from the pass that computed it
 };
+
+// Later passes of a multi-scale sum reset the counters, so the maximum
+// height that the node order reads is copied aside by the pass that
+// computes the heights.
+tt_cuda_status keep_hmax(UpWork &w, cudaStream_t st) {
+  TT_CHECK(cudaMemcpyAsync(w.plan + 8, w.counters + 3, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  return TT_CUDA_SUCCESS;
+}
 
 tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
                         UpWork &w, int raw_passes = 0) {
@@ -976,13 +1035,14 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
   Workspace &ws = workspace();
   // Exits are ring pixels: at most 124 per tile.
   const size_t E = std::min(N, (size_t)g.tiles() * kRing);
-  size_t need = 256 + align_up(N * sizeof(CoarseCell)) + align_up(E * sizeof(CoarseCell)) +
+  size_t need = 512 + align_up(N * sizeof(CoarseCell)) + align_up(E * sizeof(CoarseCell)) +
                 align_up(E * 8) + 2 * align_up(E * 4) + 2 * align_up(N * 4) +
                 (want_acc ? align_up(N * 8) : 0) + (want_h ? align_up(N * 4) : 0) +
                 align_up(N * 2) + align_up((size_t)g.tiles() * kRing) +
                 (size_t)raw_passes * align_up(N * 8) + 4096;
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   w.counters = (int *)ws.take(256);
+  w.plan = (int *)ws.take(256);
   w.cell = (CoarseCell *)ws.take(N * sizeof(CoarseCell));
   w.ccell = (CoarseCell *)ws.take(E * sizeof(CoarseCell));
   w.link = (int2 *)ws.take(E * 8);
@@ -1002,7 +1062,8 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
 tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
                       const GridDims &g, unsigned order, bool want_acc,
                       bool want_h, float *acc_out, UpWork &w, cudaStream_t st,
-                      int *count_out = nullptr, long long *raw_out = nullptr) {
+                      int *count_out = nullptr, long long *raw_out = nullptr,
+                      const int *plan = nullptr, int pass = 0) {
   const int T = g.tiles();
   TT_CHECK(cudaMemsetAsync(w.counters, 0, 256, st));
   UpArgs a{};
@@ -1028,6 +1089,8 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.ecount = w.counters + 0;
   a.acc_out = acc_out;
   a.raw_out = raw_out;
+  a.plan = plan;
+  a.pass = pass;
   a.count_out = count_out;
   a.h_out = w.h;
   a.hmax = w.counters + 3;
@@ -1065,13 +1128,12 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
 
 // Reads the counters back and maps error bits to a status.
 tt_cuda_status up_status(UpWork &w, cudaStream_t st, int *host6) {
-  if (status_sink()) {  // deferred: ecount, processed, error bits
-    int *rec = sink_record(REC_FOREST, st);
-    if (rec) {
-      TT_CHECK(cudaMemcpyAsync(rec + 1, w.counters + 0, sizeof(int), cudaMemcpyDeviceToDevice, st));
-      TT_CHECK(cudaMemcpyAsync(rec + 2, w.counters + 2, sizeof(int), cudaMemcpyDeviceToDevice, st));
-      TT_CHECK(cudaMemcpyAsync(rec + 3, w.counters + 4, sizeof(int), cudaMemcpyDeviceToDevice, st));
-    }
+  // deferred: ecount, processed and error bits go to the status sink (when
+  // the sink is full, the status is read back here as usual)
+  if (int *rec = status_sink() ? sink_record(REC_FOREST, st) : nullptr) {
+    TT_CHECK(cudaMemcpyAsync(rec + 1, w.counters + 0, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    TT_CHECK(cudaMemcpyAsync(rec + 2, w.counters + 2, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    TT_CHECK(cudaMemcpyAsync(rec + 3, w.counters + 4, sizeof(int), cudaMemcpyDeviceToDevice, st));
     for (int k = 0; k < 6; k++) host6[k] = 0;
     return TT_CUDA_SUCCESS;
   }
@@ -1121,6 +1183,50 @@ struct WeightPlan {
   int passes = 1;  // contractions to run
 };
 
+// ceil(log2(x)) of a positive finite double, exactly: x = f * 2^e with f in
+// [0.5, 1), so the answer is e, or e - 1 when x is a power of two.
+__host__ __device__ inline int ceil_log2(double x) {
+  int e = 0;
+  const double f = frexp(x, &e);
+  return f == 0.5 ? e - 1 : e;
+}
+
+// The plan from the weights' largest and smallest nonzero magnitudes (as
+// float bit patterns).  The host and the device run this same function, so
+// the deferred form scales exactly like the synchronous one.
+__host__ __device__ inline WeightPlan plan_from_range(unsigned mx_bits, unsigned mn_bits,
+                                                      double N) {
+  WeightPlan p;
+  if (mx_bits >= 0x7f800000u) return p;  // non-finite: flagged per pixel
+  if (mx_bits == 0) return p;            // all weights zero
+  float mxv, mnv;
+#ifdef __CUDA_ARCH__
+  mxv = __uint_as_float(mx_bits);
+  mnv = __uint_as_float(mn_bits);
+#else
+  std::memcpy(&mxv, &mx_bits, 4);
+  std::memcpy(&mnv, &mn_bits, 4);
+#endif
+  p.k1 = 62 - ceil_log2((double)mxv * N);
+  p.d = 61 - ceil_log2(N > 2.0 ? N : 2.0);
+  const int need = ceil_log2(0.5 / ((double)mnv * kRelTarget));
+  if (need > p.k1 && p.d > 0) {
+    const int more = (need - p.k1 + p.d - 1) / p.d;
+    p.passes = 1 + more < kMaxPasses ? 1 + more : kMaxPasses;
+  }
+  return p;
+}
+
+// One thread: the plan of the range found by weight_range_kernel, as
+// {passes, k1, d}.
+__global__ void weight_plan_kernel(const unsigned *__restrict__ rng, double N,
+                                   int *__restrict__ plan) {
+  const WeightPlan p = plan_from_range(rng[0], rng[1], N);
+  plan[0] = p.passes;
+  plan[1] = p.k1;
+  plan[2] = p.d;
+}
+
 tt_cuda_status weight_plan(const float *weights, const GridDims &g, cudaStream_t st,
                            WeightPlan *plan) {
   *plan = WeightPlan{};
@@ -1135,18 +1241,7 @@ tt_cuda_status weight_plan(const float *weights, const GridDims &g, cudaStream_t
   if (!h) return TT_CUDA_ERR_ALLOC;
   TT_CHECK(cudaMemcpyAsync(h, rng, 8, cudaMemcpyDeviceToHost, st));
   TT_CHECK(cudaStreamSynchronize(st));
-  float mxv, mnv;
-  std::memcpy(&mxv, &h[0], 4);
-  std::memcpy(&mnv, &h[1], 4);
-  if (h[0] >= 0x7f800000u) return TT_CUDA_SUCCESS;  // non-finite: flagged per pixel
-  if (!(mxv > 0.0f)) return TT_CUDA_SUCCESS;        // all weights zero
-  const double N = (double)g.cells();
-  plan->k1 = 62 - (int)std::ceil(std::log2((double)mxv * N));
-  plan->d = 61 - (int)std::ceil(std::log2(std::max(N, 2.0)));
-  const double need = std::ceil(std::log2(0.5 / ((double)mnv * kRelTarget)));
-  if (need > plan->k1 && plan->d > 0)
-    plan->passes = std::min(kMaxPasses,
-                            1 + (int)std::ceil((need - plan->k1) / (double)plan->d));
+  *plan = plan_from_range(h[0], h[1], (double)g.cells());
   return TT_CUDA_SUCCESS;
 }
 
@@ -1159,6 +1254,7 @@ tt_cuda_status accumulate_planned(float *acc, const uint8_t *dir, const float *w
                                   UpWork &w, cudaStream_t st, int h6[6]) {
   if (plan.passes == 1) {
     TT_TRY_STATUS(up_run(dir, weights, plan.k1, g, 0, true, want_h, acc, w, st));
+    if (want_h) TT_TRY_STATUS(keep_hmax(w, st));
     return up_status(w, st, h6);
   }
   const int64_t N = g.cells();
@@ -1167,31 +1263,62 @@ tt_cuda_status accumulate_planned(float *acc, const uint8_t *dir, const float *w
     TT_TRY_STATUS(up_run(dir, weights, plan.k1 + p * plan.d, g, 0, true, want_h && p == 0,
                          nullptr, w, st, nullptr, w.raw + (size_t)p * N));
     if (p == 0) {  // later passes walk the same forest
+      if (want_h) TT_TRY_STATUS(keep_hmax(w, st));
       first = up_status(w, st, h6);
       if (first == TT_CUDA_ERR_CYCLE) return first;
     }
   }
   TT_LAUNCH(combine_passes_kernel, list_grid(N), 256, 0, st, acc, w.raw, plan.passes, N,
-            plan.k1, plan.d);
+            plan.k1, plan.d, (const int *)nullptr);
+  TT_CHECK(cudaGetLastError());
+  return first;
+}
+
+// Deferred weighted accumulation (a status sink is set): the weights'
+// range and the plan stay on the device and every pass reads the plan, so
+// nothing waits for the weights.  kMaxPasses passes are enqueued; those
+// past the plan's count return at once, and a single-pass plan writes
+// `acc` from the first pass as the synchronous form does.  w must come from
+// up_alloc with kMaxPasses raw slots.
+tt_cuda_status accumulate_deferred(float *acc, const uint8_t *dir, const float *weights,
+                                   const GridDims &g, bool want_h, UpWork &w,
+                                   cudaStream_t st, int h6[6]) {
+  const int64_t N = g.cells();
+  unsigned *rng = (unsigned *)(w.plan + 4);
+  TT_CHECK(cudaMemsetAsync(rng, 0, 4, st));
+  TT_CHECK(cudaMemsetAsync(rng + 1, 0xff, 4, st));
+  TT_LAUNCH(weight_range_kernel, list_grid(N), 256, 0, st, weights, N, rng);
+  TT_LAUNCH(weight_plan_kernel, 1, 1, 0, st, rng, (double)N, w.plan);
+  tt_cuda_status first = TT_CUDA_SUCCESS;
+  for (int p = 0; p < kMaxPasses; p++) {
+    TT_TRY_STATUS(up_run(dir, weights, 0, g, 0, true, want_h && p == 0, acc, w, st, nullptr,
+                         w.raw + (size_t)p * N, w.plan, p));
+    if (p == 0) {
+      if (want_h) TT_TRY_STATUS(keep_hmax(w, st));
+      first = up_status(w, st, h6);
+      if (first == TT_CUDA_ERR_CYCLE) return first;
+    }
+  }
+  TT_LAUNCH(combine_passes_kernel, list_grid(N), 256, 0, st, acc, w.raw, kMaxPasses, N, 0, 0,
+            (const int *)w.plan);
   TT_CHECK(cudaGetLastError());
   return first;
 }
 
 // Node order from the subtree heights of a finished up_run: pixels sorted
 // by height (a donor's height is below its receiver's), stable within a
-// height by a counting sort.
-tt_cuda_status node_scatter(ptrdiff_t *node, UpWork &w, const int h6[6], const GridDims &g,
-                            cudaStream_t st) {
-  const int H = h6[3] + 1;
-  // hist, off and cursor reuse the coarse arrays (no longer needed).
+// height by a counting sort.  The number of heights is read on the device
+// (the contraction's maximum height), so nothing waits for it.
+tt_cuda_status node_scatter(ptrdiff_t *node, UpWork &w, const GridDims &g, cudaStream_t st) {
+  // hist, off and cursor reuse the coarse arrays (N ints each, no longer needed).
   int *hist = w.xmap, *off = w.xsteps, *cursor = reinterpret_cast<int *>(w.cell);
-  if ((int64_t)H > g.cells()) return TT_CUDA_ERR_CYCLE;
-  TT_CHECK(cudaMemsetAsync(hist, 0, (size_t)H * 4, st));
-  TT_CHECK(cudaMemsetAsync(cursor, 0, (size_t)H * 4, st));
-  const int eg = list_grid(g.cells());
-  TT_LAUNCH(h_hist_kernel, eg, 256, 0, st, w.h, g.cells(), hist);
-  TT_LAUNCH(scan_kernel, 1, 1024, 0, st, hist, off, H);
-  TT_LAUNCH(node_scatter_kernel, eg, 256, 0, st, w.h, g.cells(), off, cursor, node);
+  const int *hmax = w.plan + 8;
+  const int64_t N = g.cells();
+  const int eg = list_grid(N);
+  TT_LAUNCH(clear_bins_kernel, eg, 256, 0, st, hist, cursor, hmax, N);
+  TT_LAUNCH(h_hist_kernel, eg, 256, 0, st, w.h, N, hist, hmax);
+  TT_LAUNCH(scan_kernel, 1, 1024, 0, st, hist, off, hmax, N);
+  TT_LAUNCH(node_scatter_kernel, eg, 256, 0, st, w.h, N, off, cursor, node, hmax);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }
@@ -1201,11 +1328,15 @@ tt_cuda_status node_scatter(ptrdiff_t *node, UpWork &w, const int h6[6], const G
 tt_cuda_status accumulate_dev(float *acc, const uint8_t *dir,
                               const float *weights, const GridDims &g,
                               cudaStream_t st) {
+  UpWork w;
+  int h6[6];
+  if (weights && status_sink()) {
+    TT_TRY_STATUS(up_alloc(g, true, false, w, kMaxPasses));
+    return accumulate_deferred(acc, dir, weights, g, false, w, st, h6);
+  }
   WeightPlan plan;
   TT_TRY_STATUS(weight_plan(weights, g, st, &plan));
-  UpWork w;
   TT_TRY_STATUS(up_alloc(g, true, false, w, plan.passes > 1 ? plan.passes : 0));
-  int h6[6];
   return accumulate_planned(acc, dir, weights, plan, g, false, w, st, h6);
 }
 
@@ -1215,10 +1346,11 @@ tt_cuda_status node_order_dev(ptrdiff_t *node, const uint8_t *dir,
   UpWork w;
   TT_TRY_STATUS(up_alloc(g, false, true, w));
   TT_TRY_STATUS(up_run(dir, nullptr, 0, g, order, false, true, nullptr, w, st));
+  TT_TRY_STATUS(keep_hmax(w, st));
   int h6[6];
   tt_cuda_status s = up_status(w, st, h6);
   if (s == TT_CUDA_ERR_CYCLE) return s;
-  TT_TRY_STATUS(node_scatter(node, w, h6, g, st));
+  TT_TRY_STATUS(node_scatter(node, w, g, st));
   return s;
 }
 
@@ -1229,15 +1361,21 @@ tt_cuda_status node_order_acc_dev(ptrdiff_t *node, float *acc, const uint8_t *di
                                   const float *weights, const GridDims &g,
                                   cudaStream_t st, tt_cuda_status (*acc_done)(void *),
                                   void *ctx) {
-  WeightPlan plan;
-  TT_TRY_STATUS(weight_plan(weights, g, st, &plan));
   UpWork w;
-  TT_TRY_STATUS(up_alloc(g, true, true, w, plan.passes > 1 ? plan.passes : 0));
   int h6[6];
-  tt_cuda_status s = accumulate_planned(acc, dir, weights, plan, g, true, w, st, h6);
+  tt_cuda_status s;
+  if (weights && status_sink()) {
+    TT_TRY_STATUS(up_alloc(g, true, true, w, kMaxPasses));
+    s = accumulate_deferred(acc, dir, weights, g, true, w, st, h6);
+  } else {
+    WeightPlan plan;
+    TT_TRY_STATUS(weight_plan(weights, g, st, &plan));
+    TT_TRY_STATUS(up_alloc(g, true, true, w, plan.passes > 1 ? plan.passes : 0));
+    s = accumulate_planned(acc, dir, weights, plan, g, true, w, st, h6);
+  }
   if (s == TT_CUDA_ERR_CYCLE) return s;
   if (acc_done) TT_TRY_STATUS(acc_done(ctx));  // acc is complete on `st` here
-  TT_TRY_STATUS(node_scatter(node, w, h6, g, st));
+  TT_TRY_STATUS(node_scatter(node, w, g, st));
   return s;
 }
 

@@ -916,10 +916,10 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   if (KIND == GWDT)
     TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
-  if (status_sink()) {  // deferred: record the abort word, no round trip
-    int *rec = sink_record(REC_RELAX, st);
-    if (rec) TT_CHECK(cudaMemcpyAsync(rec + 1, &ctl->abort, sizeof(int),
-                                      cudaMemcpyDeviceToDevice, st));
+  // deferred: the abort word goes to the status sink, no round trip (when the
+  // sink is full, the status is read back here as usual)
+  if (int *rec = status_sink() ? sink_record(REC_RELAX, st) : nullptr) {
+    TT_CHECK(cudaMemcpyAsync(rec + 1, &ctl->abort, sizeof(int), cudaMemcpyDeviceToDevice, st));
     return TT_CUDA_SUCCESS;
   }
   TT_CHECK(cudaMemcpyAsync(hctl, ctl, sizeof(QueueCtl), cudaMemcpyDeviceToHost, st));

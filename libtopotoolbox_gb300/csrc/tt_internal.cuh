@@ -118,9 +118,10 @@ class Workspace {
   size_t used_ = 0;
 };
 
-// Deferred status (used while a batch is captured into a CUDA graph): when a
-// sink is set, stages record their status words into it with device copies
-// instead of reading them back and synchronising the stream.  Each record is
+// Deferred status (a batch captured into a CUDA graph, and device-pointer
+// calls between tt_cuda_defer_begin and tt_cuda_defer_end): when a sink is
+// set, stages record their status words into it with device copies instead
+// of reading them back and synchronising the stream.  Each record is
 // kRecordInts ints: {kind, a, b, c}.
 constexpr int kRecordInts = 4;
 enum : int { REC_RELAX = 1, REC_FOREST = 2 };
@@ -130,17 +131,33 @@ struct StatusSink {
   int next;      // next free record
 };
 StatusSink *status_sink();               // nullptr unless deferring
-void set_status_sink(StatusSink *sink);  // per thread
-// Reserves a record and returns its device address, or nullptr when full.
+// Reserves a record and returns its device address, or nullptr when full
+// (the stage then reads its status back itself).
 int *sink_record(int kind, cudaStream_t st);
+// The first failure among `count` records read back to the host.
+tt_cuda_status sink_status(const int *records, int count);
+
+// For the life of the scope, this thread's stages record into `sink` and
+// take their scratch from `ws` (and the pipeline's staging from `io`, when
+// given) instead of the device's shared workspaces; the previous settings
+// come back at its end.  Work left in flight on a private workspace keeps
+// it busy, which the device's shared one must never be.
+class SinkScope {
+ public:
+  SinkScope(StatusSink *sink, Workspace *ws, Workspace *io = nullptr);
+  ~SinkScope();
+  SinkScope(const SinkScope &) = delete;
+  SinkScope &operator=(const SinkScope &) = delete;
+
+ private:
+  StatusSink *sink_;
+  Workspace *ws_, *io_;
+};
 
 Workspace &workspace();          // of the current device (or the override)
-// While set, workspace() returns `ws` on this thread (a batch keeps its own
-// workspace so that addresses captured in its CUDA graph stay valid).
-void set_workspace_override(Workspace *ws);
 void *pinned_scratch();          // 4 KiB of pinned host memory per device
 int64_t max_rounds();
-// Sweep schedule of the relaxations (0..3) for this thread's calls.
+// Sweep schedule of the relaxations (0..5) for this thread's calls.
 int relax_schedule();
 void set_last_rounds(int64_t r);
 

@@ -18,6 +18,7 @@ thread_local int64_t g_launches = 0;
 thread_local int64_t g_last_rounds = 0;
 thread_local StatusSink *g_sink = nullptr;
 thread_local Workspace *g_ws_override = nullptr;
+thread_local Workspace *g_io_override = nullptr;
 thread_local int g_relax_schedule = -1;  // -1: the environment's or 0
 int64_t g_max_rounds_override = 0;
 
@@ -37,6 +38,31 @@ struct DeviceState {
 };
 
 DeviceState g_dev[kMaxDevices];
+
+// Deferred status of one thread's device-pointer calls
+// (tt_cuda_defer_begin / tt_cuda_defer_end).  Deferred calls take their
+// scratch from private workspaces, because their work is still in flight
+// when the call returns and the device's shared workspaces are reused by
+// the next call of any thread.
+struct Deferral {
+  int device = -1;
+  bool active = false;
+  cudaStream_t stream = nullptr;
+  Workspace ws, io;
+  int *d_rec = nullptr, *h_rec = nullptr;  // kDeferRecords status records
+  StatusSink sink{nullptr, 0, 0};
+};
+constexpr int kDeferRecords = 4096;
+thread_local Deferral *g_defer = nullptr;
+
+void release_deferral(Deferral &d) {
+  d.ws.release();
+  d.io.release();
+  if (d.d_rec) cudaFree(d.d_rec);
+  if (d.h_rec) cudaFreeHost(d.h_rec);
+  d.d_rec = d.h_rec = nullptr;
+  d.device = -1;
+}
 
 int current_device() {
   int d = 0;
@@ -60,7 +86,30 @@ int relax_schedule() {
 }
 
 StatusSink *status_sink() { return g_sink; }
-void set_status_sink(StatusSink *sink) { g_sink = sink; }
+
+SinkScope::SinkScope(StatusSink *sink, Workspace *ws, Workspace *io)
+    : sink_(g_sink), ws_(g_ws_override), io_(g_io_override) {
+  g_sink = sink;
+  g_ws_override = ws;
+  g_io_override = io;
+}
+SinkScope::~SinkScope() {
+  g_sink = sink_;
+  g_ws_override = ws_;
+  g_io_override = io_;
+}
+
+tt_cuda_status sink_status(const int *records, int count) {
+  for (int r = 0; r < count; r++) {
+    const int *rec = records + (size_t)r * kRecordInts;
+    if (rec[0] == REC_RELAX && rec[1] != 0) return TT_CUDA_ERR_NOT_CONVERGED;
+    if (rec[0] == REC_FOREST) {
+      if (rec[1] != rec[2] || (rec[3] & 1)) return TT_CUDA_ERR_CYCLE;  // unreached exits
+      if (rec[3] & 6) return TT_CUDA_ERR_INVALID_ARGUMENT;  // bad direction or weight
+    }
+  }
+  return TT_CUDA_SUCCESS;
+}
 
 int *sink_record(int kind, cudaStream_t st) {
   StatusSink *s = g_sink;
@@ -123,8 +172,9 @@ void Workspace::release() {
 Workspace &workspace() {
   return g_ws_override ? *g_ws_override : g_dev[current_device()].scratch;
 }
-void set_workspace_override(Workspace *ws) { g_ws_override = ws; }
-static Workspace &io_workspace() { return g_dev[current_device()].io; }
+static Workspace &io_workspace() {
+  return g_io_override ? *g_io_override : g_dev[current_device()].io;
+}
 
 void *pinned_scratch() {
   DeviceState &d = g_dev[current_device()];
@@ -280,6 +330,7 @@ void tt_cuda_release_workspace(void) {
   DeviceLock lock;
   workspace().release();
   io_workspace().release();
+  if (g_defer && !g_defer->active) release_deferral(*g_defer);
 }
 
 int64_t tt_cuda_launch_count(int reset) {
@@ -301,6 +352,11 @@ void tt_cuda_set_relax_schedule(int schedule) {
 // ------------------------------------------------------------------
 namespace {
 
+Deferral *active_deferral() {
+  return (g_defer && g_defer->active && g_defer->device == current_device()) ? g_defer
+                                                                             : nullptr;
+}
+
 template <class F>
 tt_cuda_status dev_call(const ptrdiff_t dims[2], void *stream, F &&body) {
   if (!dims_ok(dims)) {
@@ -314,6 +370,21 @@ tt_cuda_status dev_call(const ptrdiff_t dims[2], void *stream, F &&body) {
   DeviceLock lock;
   cudaStream_t st = (cudaStream_t)stream;
   GridDims g = make_dims(dims);
+  if (Deferral *d = active_deferral()) {
+    if (st != d->stream) {  // the private workspaces are ordered by one stream
+      set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+      return TT_CUDA_ERR_INVALID_ARGUMENT;
+    }
+    tt_cuda_status s;
+    {
+      SinkScope scope(&d->sink, &d->ws, &d->io);
+      s = body(g, st);
+    }
+    // no synchronisation: the stages' status words wait in the sink
+    if (s == TT_CUDA_ERR_CUDA) cudaGetLastError();
+    set_status(s);
+    return s;
+  }
   tt_cuda_status s = body(g, st);
   return finish(s, st);
 }
@@ -321,6 +392,64 @@ tt_cuda_status dev_call(const ptrdiff_t dims[2], void *stream, F &&body) {
 }  // namespace
 
 extern "C" {
+
+tt_cuda_status tt_cuda_defer_begin(void *stream) {
+  if (!have_device()) {
+    set_status(TT_CUDA_ERR_NO_DEVICE);
+    return TT_CUDA_ERR_NO_DEVICE;
+  }
+  if (g_defer && g_defer->active) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return TT_CUDA_ERR_INVALID_ARGUMENT;
+  }
+  const int dev = current_device();
+  if (!g_defer) g_defer = new Deferral;
+  Deferral &d = *g_defer;
+  if (d.device != dev) release_deferral(d);  // buffers of another device
+  if (!d.d_rec) {
+    const size_t bytes = (size_t)kDeferRecords * kRecordInts * sizeof(int);
+    if (std::getenv("TT_CUDA_FAIL_ALLOC") || cudaMalloc(&d.d_rec, bytes) != cudaSuccess ||
+        cudaMallocHost(&d.h_rec, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      release_deferral(d);
+      set_status(TT_CUDA_ERR_ALLOC);
+      return TT_CUDA_ERR_ALLOC;
+    }
+  }
+  d.device = dev;
+  d.stream = (cudaStream_t)stream;
+  d.sink = StatusSink{d.d_rec, kDeferRecords, 0};
+  d.active = true;
+  set_status(TT_CUDA_SUCCESS);
+  return TT_CUDA_SUCCESS;
+}
+
+tt_cuda_status tt_cuda_defer_end(void) {
+  if (!g_defer || !g_defer->active) {
+    set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
+    return TT_CUDA_ERR_INVALID_ARGUMENT;
+  }
+  Deferral &d = *g_defer;
+  d.active = false;
+  int prev = -1;
+  const bool other = cudaGetDevice(&prev) == cudaSuccess && prev != d.device;
+  if (other && cudaSetDevice(d.device) != cudaSuccess) {
+    cudaGetLastError();
+    set_status(TT_CUDA_ERR_CUDA);
+    return TT_CUDA_ERR_CUDA;
+  }
+  tt_cuda_status s = TT_CUDA_SUCCESS;
+  const int n = d.sink.next;
+  if (n > 0 && cudaMemcpyAsync(d.h_rec, d.d_rec, (size_t)n * kRecordInts * sizeof(int),
+                               cudaMemcpyDeviceToHost, d.stream) != cudaSuccess)
+    s = TT_CUDA_ERR_CUDA;
+  if (cudaStreamSynchronize(d.stream) != cudaSuccess) s = TT_CUDA_ERR_CUDA;
+  if (s == TT_CUDA_SUCCESS) s = sink_status(d.h_rec, n);
+  if (s == TT_CUDA_ERR_CUDA) cudaGetLastError();
+  if (other) cudaSetDevice(prev);
+  set_status(s);
+  return s;
+}
 
 tt_cuda_status tt_cuda_fillsinks_dev(float *output, const float *dem,
                                      const uint8_t *bc, const ptrdiff_t dims[2],
@@ -623,7 +752,7 @@ static tt_cuda_status pipeline_body(float *filled, int32_t *flats, float *dist,
   if (out) TT_TRY(out->send(out->filled, filled, n * 4, st));
   TT_TRY(identifyflats_dev(flats, filled, g, nullptr, st));
   if (out) TT_TRY(out->send(out->flats, flats, n * 4, st));
-  TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));
+  TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));  // conncomps may be null
   TT_TRY_SOFT(gwdt_dev(dist, nullptr, costs, flats, g, st), soft);
   if (out) TT_TRY(out->send(out->dist, dist, n * 4, st));
   TT_TRY(directions_dev(direction, filled, dist, flats, g, 0, st));
@@ -669,21 +798,19 @@ extern "C" tt_cuda_status tt_cuda_d8_pipeline_dev(
     int64_t N = g.cells();
     Staging sg;
     sg.add(N * 4);  // costs
-    sg.add(N * 8);  // conncomps
     if (!filled) sg.add(N * 4);
     if (!flats) sg.add(N * 4);
     if (!dist) sg.add(N * 4);
     if (!direction) sg.add(N);
     if (!sg.reserve()) return TT_CUDA_ERR_ALLOC;
     float *costs = (float *)sg.take(N * 4);
-    ptrdiff_t *cc = (ptrdiff_t *)sg.take(N * 8);
     if (!filled) filled = (float *)sg.take(N * 4);
     if (!flats) flats = (int32_t *)sg.take(N * 4);
     if (!dist) dist = (float *)sg.take(N * 4);
     if (!direction) direction = (uint8_t *)sg.take(N);
     return pipeline_body(filled, flats, dist, node, direction, acc, hillshade,
                          dem, bc, weights, azimuth, altitude, cellsize, costs,
-                         cc, g, st);
+                         nullptr, g, st);
   });
 }
 
@@ -1167,8 +1294,7 @@ void tt_cuda_d8_pipeline(float *filled, int32_t *flats, float *dist,
              {nullptr, node ? N * 8 : 0, false, false},
              {nullptr, N, false, false},
              {nullptr, acc ? N * 4 : 0, false, false},
-             {nullptr, N * 4, false, false},   // costs
-             {nullptr, N * 8, false, false}},  // conncomps
+             {nullptr, N * 4, false, false}},  // costs
             [&](const GridDims &g, cudaStream_t st, std::vector<HostArg> &a) {
               EarlyOut out;
               out.filled = filled;
@@ -1183,7 +1309,7 @@ void tt_cuda_d8_pipeline(float *filled, int32_t *flats, float *dist,
                   node ? (ptrdiff_t *)a[6].dev : nullptr, (uint8_t *)a[7].dev,
                   acc ? (float *)a[8].dev : nullptr, nullptr, (const float *)a[0].dev,
                   (const uint8_t *)a[1].dev, weights ? (const float *)a[2].dev : nullptr,
-                  0.f, 0.f, 1.f, (float *)a[9].dev, (ptrdiff_t *)a[10].dev, g, st, &out);
+                  0.f, 0.f, 1.f, (float *)a[9].dev, nullptr, g, st, &out);
               // copies already issued end before the call returns, even when
               // a later stage failed
               if (out.cs && out.used && cudaStreamSynchronize(out.cs) != cudaSuccess) {
