@@ -113,14 +113,29 @@ __device__ __forceinline__ int run_start(uint32_t starts, int b) {
   return 31 - __clz(below);
 }
 
+// A component's maximum depth key and the smallest tile index attaining it,
+// packed so that one 64-bit maximum reduces both: the key (sign flipped to
+// order as unsigned) above, 1023 - index below.  0 means no key.
+__device__ __forceinline__ unsigned long long pack_best(int key, int loc) {
+  return ((unsigned long long)((unsigned)key ^ 0x80000000u) << 32) | (unsigned)(1023 - loc);
+}
+
 struct CclTile {
-  // Union-find over run ids (column * 32 + first row); once every run knows
-  // its root, the same slots hold per-root reductions: the maximum depth
-  // key, then the smallest pixel attaining it.
-  int lab[kTile * kTile];
-  int key[kTile * kTile];    // per pixel: depth key (INT_MIN: none)
+  // Union-find over run ids (column * 32 + first row).  Two run starts of
+  // one column are at least two rows apart, so start >> 1 gives every run
+  // its own 64-bit slot: once every run knows its root, lab64 holds the
+  // per-root reduction (pack_best), and each run parks its own best in
+  // key64 at its start (its pixels' keys are read by then).
+  union {
+    int lab[kTile * kTile];
+    unsigned long long lab64[kTile * kTile / 2];
+  };
+  union {
+    int key[kTile * kTile];  // per pixel: depth key (INT_MIN: none)
+    unsigned long long key64[kTile * kTile / 2];
+  };
   int16_t root[kTile * kTile];  // per pixel: local root, -1 for non-flats
-  uint32_t starts[kTile];    // run starts of each column
+  uint32_t starts[kTile];       // run starts of each column
 };
 
 // One warp per tile.  Each lane owns one column's flat mask (32 bits): a
@@ -244,22 +259,31 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       }
     }
     __syncwarp();
-    // lane = column: every pixel of a run takes the run's root; roots reset
-    // their reduction slot
+    // lane = column: every pixel of a run takes the run's root, and the run
+    // parks its best (largest key, first pixel attaining it) at its start
     for (uint32_t s = S; s; s &= s - 1) {
       const int s0 = __ffs(s) - 1;
       const int r = sfind(t.lab, lane * kTile + s0);
-      const uint32_t rm = run_mask(M, s0);
-      for (uint32_t b = rm; b; b &= b - 1) t.root[lane * kTile + __ffs(b) - 1] = (int16_t)r;
+      int km = INT_MIN, kl = 0;
+      for (uint32_t b = run_mask(M, s0); b; b &= b - 1) {
+        const int loc = lane * kTile + __ffs(b) - 1;
+        t.root[loc] = (int16_t)r;
+        const int k = t.key[loc];
+        if (k > km) {  // strictly: the first (smallest) pixel keeps a tie
+          km = k;
+          kl = loc;
+        }
+      }
+      t.key64[(lane * kTile + s0) >> 1] = km == INT_MIN ? 0ULL : pack_best(km, kl);
     }
     __syncwarp();
-    {  // local roots: reset their reduction slot and list them (one
+    {  // local roots: clear their reduction slot and list them (one
        // reservation per tile, lane = column)
       uint32_t rs = 0;
       for (uint32_t s = S; s; s &= s - 1) {
         const int loc = lane * kTile + __ffs(s) - 1;
         if (t.root[loc] == loc) {
-          t.lab[loc] = INT_MIN;
+          t.lab64[loc >> 1] = 0ULL;
           rs |= s & (~s + 1u);
         }
       }
@@ -278,33 +302,14 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         roots[base++] = (int)((j0 + lane) * m + (i0 + __ffs(b) - 1));
     }
     __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {
-      const int loc = jj * kTile + lane, r = t.root[loc], k = t.key[loc];
-      if (r >= 0 && k != INT_MIN) atomicMax(&t.lab[r], k);
+    // one 64-bit maximum per run folds its best into its root
+    for (uint32_t s = S; s; s &= s - 1) {
+      const int loc = lane * kTile + __ffs(s) - 1;
+      const unsigned long long v = t.key64[loc >> 1];
+      if (v) atomicMax(&t.lab64[t.root[loc] >> 1], v);
     }
     __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {  // per pixel: its component's maximum
-      const int loc = jj * kTile + lane, r = t.root[loc];
-      if (r >= 0 && t.key[loc] != INT_MIN && t.key[loc] == t.lab[r]) t.key[loc] = INT_MAX;
-    }
-    __syncwarp();
-    // roots: keep the maximum aside (in lmax) and turn the slot into an argmin
-    for (int jj = 0; jj < kTile; jj++) {
-      const int loc = jj * kTile + lane, r = t.root[loc];
-      const int64_t j = j0 + jj;
-      if (r == loc && i < m && j < n) lmax[j * m + i] = t.lab[loc];
-    }
-    __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {
-      const int loc = jj * kTile + lane;
-      if (t.root[loc] == loc) t.lab[loc] = INT_MAX;
-    }
-    __syncwarp();
-    for (int jj = 0; jj < kTile; jj++) {
-      const int loc = jj * kTile + lane, r = t.root[loc];
-      if (r >= 0 && t.key[loc] == INT_MAX) atomicMin(&t.lab[r], loc);
-    }
-    __syncwarp();
+    // lane = row: labels and the roots' maximum / argmax, coalesced per column
     for (int jj = 0; jj < kTile; jj++) {
       const int64_t j = j0 + jj;
       const bool in = i < m && j < n;
@@ -313,8 +318,10 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
       const int r = t.root[loc];
       if (!in || r < 0) continue;  // L is only ever read at flat pixels
       if (r == loc) {
-        const int a = t.lab[loc];
-        larg[gp] = a == INT_MAX ? INT_MAX : (int)((j0 + a / kTile) * m + (i0 + a % kTile));
+        const unsigned long long v = t.lab64[loc >> 1];
+        const int a = 1023 - (int)(v & 1023u);
+        lmax[gp] = v ? (int)((unsigned)(v >> 32) ^ 0x80000000u) : INT_MIN;
+        larg[gp] = v ? (int)((j0 + a / kTile) * m + (i0 + a % kTile)) : INT_MAX;
         maxkey[gp] = INT_MIN;
         argmax[gp] = INT_MAX;
       } else {

@@ -189,7 +189,7 @@ __device__ __forceinline__ void sweep_fill(WarpTile &t, int lane, int dir, uint3
   uint32_t dm = 0, evald = 0;
   float ob = 0.f, op = 0.f, lp = 0.f, rp = 0.f;  // own behind / here, adjacent here
   bool have = false;  // the registers hold the previous step's values
-#pragma unroll 4
+#pragma unroll 1
   for (int s = first; s < kTile; s++) {
     const int k = dir > 0 ? s : kTile - 1 - s;  // position along the line
     const uint32_t bit = 1u << k;
@@ -246,7 +246,7 @@ __device__ __forceinline__ void sweep_gwdt_run(WarpTile &t, int lane, int dir, u
   float ob = 0.f, op = 0.f, lp = 0.f, rp = 0.f;
   float cb0 = 0.f, cb1 = 0.f, cb2 = 0.f, cp0 = 0.f, cp1 = 0.f, cp2 = 0.f;
   bool have = false;
-#pragma unroll 2
+#pragma unroll 1
   for (int s = first; s < kTile; s++) {
     const int k = dir > 0 ? s : kTile - 1 - s;
     const uint32_t bit = 1u << k;
