@@ -45,6 +45,9 @@ HS_AZ, HS_ALT = 3.9269908, 1.0471976
 # Host memory one whole-DEM oracle pipeline holds at its peak (gwdt: DEM, bc,
 # filled, flats, costs, dist, heap, back), bytes per pixel, with headroom.
 CPU_BYTES_PER_PIXEL = 40
+# One whole 16384 x 16384 step of the oracle pipeline on one Grace core:
+# 179 s measured (the reference arm's single-step median), per pixel.
+CPU_SECONDS_PER_PIXEL = 179.0 / 2**28
 
 # name -> (generator in libtopotoolbox_gb300.dems, hillshade in the step)
 WORKLOADS = {
@@ -505,11 +508,17 @@ def mem_available():
 def run_reference(args):
     """--impl reference: the CPU implementation on whole workload DEMs.
 
-    Every step is one whole DEM of the workload (the same DEM, config and
-    metric as the GPU arm) through the oracle's C restatement of the
+    Every timed step is one whole DEM of the workload (the same DEM, config
+    and metric as the GPU arm) through the oracle's C restatement of the
     reference, which is serial per DEM; steps run concurrently on the host
-    cores, as many at once as the cores and the host memory allow.  W
-    warm-up steps, then K timed steps; value = K * pixels / wall time."""
+    cores, as many at once as the cores and the host memory allow.  A crop
+    is not the same workload (the CPU cost per pixel grows with the DEM), so
+    the warm-up steps, which only warm the code path (there is no compiler
+    or cache state to prepare across whole-DEM runs), run on the workload's
+    top-left 1024 x 1024 corner.  value = K * pixels / wall time of the K
+    timed steps.  When K whole DEMs at that concurrency would take longer
+    than --ref-budget-s, the arm prints its `unavailable` line instead, with
+    the single-step time it is projected from."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -523,18 +532,39 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     per = cells * CPU_BYTES_PER_PIXEL
     avail = mem_available()
-    conc = max(1, min(cores, args.steps, int(0.7 * avail / per) if avail else 1))
+    mem_conc = int(0.7 * avail / per) if avail else 1
+    conc = max(1, min(cores, args.steps, mem_conc))
     hsarg = (HS_AZ, HS_ALT, cs) if hs else None
+    rounds = -(-args.steps // conc)
+    projected = rounds * CPU_SECONDS_PER_PIXEL * cells
+    if projected > args.ref_budget_s:
+        m, n = dem.shape
+        print(json.dumps({
+            "impl": "reference",
+            "unavailable": f"{args.steps} whole {m}x{n} DEM steps, {conc} at a time (host "
+                           f"memory), need ~{projected / 60:.0f} min at the measured "
+                           f"{CPU_SECONDS_PER_PIXEL * 2**28:.0f} s per 16384x16384 step on one "
+                           f"Grace core, beyond the {args.ref_budget_s / 60:.0f} min budget of "
+                           f"this arm; a crop is not the same workload"}), flush=True)
+        return 0
+    c0 = min(1024, dem.shape[0]), min(1024, dem.shape[1])
+    wdem = np.asfortranarray(dem[:c0[0], :c0[1]])
+    wbc = np.asfortranarray(bc[:c0[0], :c0[1]]).copy()
+    wbc[0, :] = wbc[-1, :] = 1
+    wbc[:, 0] = wbc[:, -1] = 1
 
-    def one(_):
+    def one(whole):
         t0 = time.perf_counter()
-        orc.run_pipeline(dem, bc, hillshade=hsarg)
+        if whole:
+            orc.run_pipeline(dem, bc, hillshade=hsarg)
+        else:
+            orc.run_pipeline(wdem, wbc, hillshade=hsarg)
         return time.perf_counter() - t0
 
     with ThreadPoolExecutor(max_workers=conc) as ex:
-        warm = list(ex.map(one, range(args.warmup)))
+        warm = list(ex.map(one, [False] * args.warmup))
         t0 = time.perf_counter()
-        per_step = list(ex.map(one, range(args.steps)))
+        per_step = list(ex.map(one, [True] * args.steps))
         wall = time.perf_counter() - t0
     ms = 1e3 * wall / args.steps
     value = cells * args.steps / wall / 1e9
@@ -549,12 +579,14 @@ def run_reference(args):
                                    f"pipeline{' + hillshade' if hs else ''} (oracle C "
                                    f"restatement of the reference, pinned bit for bit to it; "
                                    f"the reference's sources are not on this host); {conc} "
-                                   f"steps at a time on {cores} host cores, limited by host "
-                                   f"memory ({avail / 2**30:.0f} GiB available)",
+                                   f"steps at a time, one per core (the fewest of K, the "
+                                   f"{cores} host cores and the {max(mem_conc, 1)} that "
+                                   f"{avail / 2**30:.0f} GiB of host memory hold)",
                          "single_step_s": {"median": float(np.median(per_step)),
                                            "min": float(np.min(per_step)),
                                            "max": float(np.max(per_step))},
-                         "warmup_s": float(np.sum(warm))},
+                         "warmup": f"{args.warmup} untimed steps on the top-left "
+                                   f"{c0[0]}x{c0[1]} corner ({float(np.sum(warm)):.1f} s)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -754,6 +786,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="plain_16384", choices=sorted(WORKLOADS))
+    ap.add_argument("--ref-budget-s", type=float, default=1800.0,
+                    help="reference arm: longest projected run of the timed whole-DEM steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
