@@ -141,7 +141,7 @@ tt_cuda_status enqueue(tt_cuda_batch *b, cudaStream_t st) {
             b->Mc, b->dem, b->bc);
   TT_CHECK(cudaGetLastError());
   tt_cuda_status s;
-  if ((s = fill_dev(b->filled, b->dem, b->bc, g, st)) != TT_CUDA_SUCCESS) return s;
+  if ((s = fill_dev(b->filled, b->dem, b->bc, g, st, false)) != TT_CUDA_SUCCESS) return s;
   if ((s = identifyflats_dev(b->flats, b->filled, g, nullptr, st)) != TT_CUDA_SUCCESS) return s;
   if ((s = costs_dev(b->costs, nullptr, b->flats, b->dem, b->filled, g, st)) != TT_CUDA_SUCCESS)
     return s;

@@ -181,8 +181,11 @@ int sm_count();
 // status; iterative stages synchronise `st`.
 // ------------------------------------------------------------------
 
+// `bounded`: on large grids, start from the fill of a max-pooled DEM (the
+// same result, fewer tile visits); off for canvases of many DEMs, whose NaN
+// gutters make that bound useless.
 tt_cuda_status fill_dev(float *f, const float *dem, const uint8_t *bc,
-                        const GridDims &g, cudaStream_t st);
+                        const GridDims &g, cudaStream_t st, bool bounded = true);
 // Grayscale reconstruction by dilation: marker := R(marker, mask).
 tt_cuda_status reconstruct_dev(float *marker, const float *mask,
                                const GridDims &g, cudaStream_t st);
