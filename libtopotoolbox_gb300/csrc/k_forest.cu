@@ -295,8 +295,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       if (H) t.h[e] = 0;
       nvalid += in;
     }
-    nvalid = __reduce_add_sync(0xffffffffu, nvalid);  // one atomic per warp
-    if ((tid & 31) == 0 && nvalid) atomicAdd(&t.nvalid, nvalid);
+    if (nvalid) atomicAdd(&t.nvalid, nvalid);
     if (bad) t.bad = 1;
     __syncthreads();
 
@@ -321,12 +320,11 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       }
       a.emask[(size_t)tile * kRing + tid] = (uint8_t)ne;
     }
-    // Leaves, listed before any walk starts (a walk empties counts); the
-    // leaves of a warp take consecutive slots with one atomic.
+    // Leaves, listed before any walk starts (a walk empties counts).
 #pragma unroll
     for (int u = 0; u < kPerThread; u++) {
       const int e = tid + u * kUpThreads;
-      if (t.rl[e] != RL_NONE && t.pend[e] == 0) t.leaf[append_slot(&t.nleaf)] = (int16_t)e;
+      if (t.rl[e] != RL_NONE && t.pend[e] == 0) t.leaf[atomicAdd(&t.nleaf, 1)] = (int16_t)e;
     }
     __syncthreads();
 
@@ -340,8 +338,8 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       long long v = 0;
       int hv = 0;
       for (int guard = 0; guard < 2 * kTileCells + 2; guard++) {
-        if (cur < 0) {  // the threads that need a leaf together take one atomic
-          const int k = append_slot(&t.next);
+        if (cur < 0) {
+          const int k = atomicAdd(&t.next, 1);
           if (k >= nleaf) break;
           cur = t.leaf[k];
           if (ACC) v = t.acc[cur];
@@ -366,9 +364,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
         if (H) hv = t.h[cur];
       }
     }
-    __syncwarp();
-    owned = __reduce_add_sync(0xffffffffu, owned);
-    if ((tid & 31) == 0 && owned) atomicAdd(&t.owned, owned);
+    if (owned) atomicAdd(&t.owned, owned);
     __syncthreads();
     if (tid == 0 && t.owned != t.nvalid) atomicOr(a.err, ERR_CYCLE);
 

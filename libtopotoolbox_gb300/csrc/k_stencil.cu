@@ -36,8 +36,6 @@ constexpr int kBlockY = 8;   // along j
 // kCountSlots counters (spread so that blocks do not queue on one address),
 // which a last step sums.
 // ------------------------------------------------------------------
-__device__ __forceinline__ float nan_to_neg_inf(float v) { return v != v ? -INFINITY : v; }
-
 constexpr int kFz = kTile + 4;  // staged DEM side (two-pixel halo)
 constexpr int kFr = 4;          // flat-bit row r of the tile is stored at r + kFr
 constexpr int kFp = 44;         // flat-bit column pitch (bytes): rows -1 .. 32 at 3 .. 36,
@@ -45,14 +43,15 @@ constexpr int kFp = 44;         // flat-bit column pitch (bytes): rows -1 .. 32 
 constexpr int kCountSlots = 64;
 
 // Flat test of the pixel whose 3 x 3 neighbourhood is (a0 a1 a2 | b0 b1 b2 |
-// c0 c1 c2), centre b1: not NaN and no neighbour lower (NaN counts as -INF).
+// c0 c1 c2), centre b1: not NaN and no neighbour lower, a NaN neighbour
+// counting as -INF.  A neighbour x passes when (NaN ? -INF : x) >= b1: for
+// b1 = -INF every neighbour passes, otherwise x passes exactly when
+// x >= b1 (false for NaN), one compare per neighbour.
 __device__ __forceinline__ bool is_flat(float a0, float a1, float a2, float b0, float b1,
                                         float b2, float c0, float c1, float c2) {
-  const float lo = fminf(fminf(fminf(nan_to_neg_inf(a0), nan_to_neg_inf(a1)),
-                               fminf(nan_to_neg_inf(a2), nan_to_neg_inf(b0))),
-                         fminf(fminf(nan_to_neg_inf(b2), nan_to_neg_inf(c0)),
-                               fminf(nan_to_neg_inf(c1), nan_to_neg_inf(c2))));
-  return b1 == b1 && !(lo < b1);
+  const bool ge = (a0 >= b1) & (a1 >= b1) & (a2 >= b1) & (b0 >= b1) & (b2 >= b1) &
+                  (c0 >= b1) & (c1 >= b1) & (c2 >= b1);
+  return b1 == b1 && (ge || b1 == -INFINITY);
 }
 
 __global__ void __launch_bounds__(kBlockX * kBlockY)
@@ -220,6 +219,42 @@ __global__ void sum_slots_kernel(const unsigned long long *__restrict__ slots,
 // difference itself beats the best slope so far (fl(diff / sqrt(2)) <= diff,
 // so otherwise it cannot win).
 // The direction bytes go out through shared memory in coalesced rows.
+// Directions of a 4-pixel column strip from its 3 x 6 window (dem z,
+// auxiliary topography d), one byte per pixel.  FLATS: whether the strip
+// may hold flats (bit 8u of fl4: pixel u is flat and compares d).
+template <unsigned ORDER, bool FLATS>
+__device__ __forceinline__ uint32_t strip_directions(const float (&z)[3][6],
+                                                     const float (&d)[3][6], uint32_t fl4,
+                                                     float sq2) {
+  uint32_t out4 = 0;
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const bool fl = FLATS && ((fl4 >> (8 * u)) & 1u);
+    const float zc = z[1][u + 1];
+    const float zz0 = fl ? d[1][u + 1] : zc;
+    float best = 0.0f;
+    unsigned dv = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
+      const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
+      const float zn = z[1 + dj][u + 1 + di];
+      const float zz = fl ? d[1 + dj][u + 1 + di] : zn;
+      const float diff = __fsub_rn(zz0, zz);
+      // skip higher neighbours; a difference that does not beat the best
+      // (or is NaN) cannot win, since a diagonal's quotient is <= diff
+      if (zn > zc || !(diff > best)) continue;
+      const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
+      if (g > best) {
+        best = g;
+        dv = 1u << k;
+      }
+    }
+    out4 |= dv << (8 * u);
+  }
+  return out4;
+}
+
 template <unsigned ORDER>
 __global__ void __launch_bounds__(kBlockX * kBlockY)
 directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
@@ -303,32 +338,9 @@ directions_kernel(uint8_t *__restrict__ dir, const float *__restrict__ dem,
         d[dc][u] = ds[c + dc][r0 + u];
       }
     const uint32_t fl4 = *reinterpret_cast<const uint32_t *>(&fs[c][r0]);
-    uint32_t out4 = 0;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const bool fl = (fl4 >> (8 * u)) & 1u;
-      const float zc = z[1][u + 1];
-      const float zz0 = fl ? d[1][u + 1] : zc;
-      float best = 0.0f;
-      unsigned dv = 0;
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        constexpr unsigned A = ORDER ? kD8B : kD8A, B = ORDER ? kD8A : kD8B;
-        const int di = (int)((A >> (2 * k)) & 3u) - 1, dj = (int)((B >> (2 * k)) & 3u) - 1;
-        const float zn = z[1 + dj][u + 1 + di];
-        const float zz = fl ? d[1 + dj][u + 1 + di] : zn;
-        const float diff = __fsub_rn(zz0, zz);
-        // skip higher neighbours; a difference that does not beat the best
-        // (or is NaN) cannot win, since a diagonal's quotient is <= diff
-        if (zn > zc || !(diff > best)) continue;
-        const float g = (k & 1) ? __fdiv_rn(diff, sq2) : diff;
-        if (g > best) {
-          best = g;
-          dv = 1u << k;
-        }
-      }
-      out4 |= dv << (8 * u);
-    }
+    // One code path for every strip: a second one without the flat selects
+    // measured slower (warps whose strips differ run both).
+    const uint32_t out4 = strip_directions<ORDER, true>(z, d, fl4, sq2);
     *reinterpret_cast<uint32_t *>(&os[c][r0]) = out4;
   }
   __syncthreads();
