@@ -421,13 +421,15 @@ __global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ l
 // pipeline needs the costs alone).
 constexpr int kCostPer = 4;
 
+template <bool SEED>
 __global__ void costs_kernel(float *__restrict__ costs,
                              ptrdiff_t *__restrict__ conncomps, int *__restrict__ L,
                              const int *__restrict__ maxkey,
                              const int *__restrict__ argmax,
                              const int32_t *__restrict__ flats,
                              const float *__restrict__ orig,
-                             const float *__restrict__ filled, int64_t N) {
+                             const float *__restrict__ filled, int64_t N,
+                             GwdtSeed seed, int64_t m, int64_t n, int tm) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N;
        p0 += kCostPer * stride) {
@@ -463,7 +465,14 @@ __global__ void costs_kernel(float *__restrict__ costs,
         c = __double2float_rn(__dadd_rn((double)diff, 0.1));
         lab = (am[u] == INT_MAX) ? R[u] : am[u];
       }
-      costs[p] = c;
+      if (SEED) {  // the gwdt start (src/gwdt.c:296-308) instead of plain costs
+        const int32_t f = fv[u];
+        costs[p] = (f & 1) ? c : NAN;
+        seed.dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
+        if ((f & 5) == 5) mark_tiles_near(seed.dirty, tm, p % m, p / m, m, n);
+      } else {
+        costs[p] = c;
+      }
       if (conncomps) conncomps[p] = lab;
     }
   }
@@ -480,7 +489,7 @@ int ew_grid(int64_t N) {
 tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
                          const int32_t *flats, const float *orig,
                          const float *filled, const GridDims &g,
-                         cudaStream_t st) {
+                         cudaStream_t st, const GwdtSeed *seed) {
   const int64_t N = g.cells();
   Workspace &ws = workspace();
   const int T = g.tiles();
@@ -505,8 +514,13 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
   TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
             maxkey, argmax);
-  TT_LAUNCH(costs_kernel, (int)std::min<int64_t>((N + 1023) / 1024, (int64_t)sm_count() * 32),
-            256, 0, st, costs, conncomps, L, maxkey, argmax, flats, orig, filled, N);
+  const int cgrid = (int)std::min<int64_t>((N + 1023) / 1024, (int64_t)sm_count() * 32);
+  if (seed)
+    TT_LAUNCH(costs_kernel<true>, cgrid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
+              flats, orig, filled, N, *seed, g.m, g.n, g.tm);
+  else
+    TT_LAUNCH(costs_kernel<false>, cgrid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
+              flats, orig, filled, N, GwdtSeed{nullptr, nullptr}, g.m, g.n, g.tm);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;
 }

@@ -104,7 +104,6 @@ constexpr int kUrgent = (int)0x80000000;  // below every key: runs at any thresh
 
 // Dirty flag bits: 1 = a halo pixel changed (re-evaluate the edge ring),
 // 2 = evaluate every pixel (first visit, or a visit that hit its sweep cap).
-enum : int { DIRTY_EDGE = 1, DIRTY_FULL = 2 };
 
 // Release / acquire at device scope (lighter than a sequentially consistent
 // fence): a writer fences before it sets a flag, a reader after it takes one.
@@ -662,13 +661,12 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
 // (Ordered schedules: those tiles also get the most urgent priority.)
 __device__ __forceinline__ void mark_tiles_around(int *dirty, int *prio, int tm, int64_t i,
                                                   int64_t j, int64_t m, int64_t n) {
+  mark_tiles_near(dirty, tm, i, j, m, n);
+  if (!prio) return;
   const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
   const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
   for (int tj = tj0; tj <= tj1; tj++)
-    for (int ti = ti0; ti <= ti1; ti++) {
-      dirty[tj * tm + ti] = DIRTY_FULL;
-      if (prio) prio[tj * tm + ti] = kUrgent;
-    }
+    for (int ti = ti0; ti <= ti1; ti++) prio[tj * tm + ti] = kUrgent;
 }
 
 // Elements per thread and loop trip of the elementwise kernels: their loads
@@ -958,20 +956,27 @@ template <int KIND>
 tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
                          const GridDims &g, cudaStream_t st, const uint8_t *bc = nullptr,
                          const float *bound = nullptr, int64_t bound_mc = 0,
-                         int64_t bound_nc = 0, bool report = true) {
+                         int64_t bound_nc = 0, bool report = true,
+                         int *seeded_dirty = nullptr) {
   const int T = g.tiles();
   const int sched = relax_schedule();
   const bool ordered = sched >= 4;
+  // gwdt seeded by the costs pass: state, costs and flags are in place
+  const bool seeded = KIND == GWDT && seeded_dirty;
+  if (seeded && ordered) return TT_CUDA_ERR_INVALID_ARGUMENT;  // no priorities seeded
   const int wmax = sm_count() * 32 * kWarps;  // more warp slots than any grid has warps
   Workspace &ws = workspace();
   size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
-  if (KIND == GWDT) need += align_up((size_t)g.cells() * 4);
+  if (KIND == GWDT && !seeded) need += align_up((size_t)g.cells() * 4);
   if (ordered) need += align_up((size_t)T * 4) + align_up((size_t)wmax * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
-  int *dirty = (int *)ws.take((size_t)T * 4);
-  // gwdt relaxes over a copy of the costs with NaN at non-flat pixels
-  float *wcost = KIND == GWDT ? (float *)ws.take((size_t)g.cells() * 4) : nullptr;
+  int *dirty = seeded ? seeded_dirty : (int *)ws.take((size_t)T * 4);
+  // gwdt relaxes over a copy of the costs with NaN at non-flat pixels (a
+  // seeded run over the costs array itself, already in that form)
+  float *wcost = KIND != GWDT ? nullptr
+                 : seeded    ? const_cast<float *>(aux)
+                             : (float *)ws.take((size_t)g.cells() * 4);
   int *prio = ordered ? (int *)ws.take((size_t)T * 4) : nullptr;
   int *wmin = ordered ? (int *)ws.take((size_t)wmax * 4) : nullptr;
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
@@ -999,7 +1004,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
               g.n, dirty, prio, g.tm);
   } else if (KIND == FILL) {
     TT_LAUNCH(dirty_all_kernel, tgrid, 256, 0, st, dirty, prio, T);
-  } else {
+  } else if (!seeded) {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(gwdt_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, wcost, aux,
               flats, g.m, g.n, ra);
@@ -1094,6 +1099,11 @@ tt_cuda_status reconstruct_dev(float *marker, const float *mask,
     TT_LAUNCH(negate_kernel, elementwise_grid(N), 256, 0, st, marker, f, N);
   cudaFreeAsync(buf, st);
   return s;
+}
+
+tt_cuda_status gwdt_seeded_dev(float *dist, const float *costs, const int32_t *flats,
+                               int *dirty, const GridDims &g, cudaStream_t st) {
+  return run_queue<GWDT>(dist, costs, flats, g, st, nullptr, nullptr, 0, 0, true, dirty);
 }
 
 tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,

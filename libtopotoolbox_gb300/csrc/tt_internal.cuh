@@ -193,13 +193,39 @@ tt_cuda_status identifyflats_dev(int32_t *flags, const float *dem,
                                  const GridDims &g,
                                  unsigned long long *count_dev,
                                  cudaStream_t st);
+// Tile flags of the relaxations: a tile waits with its edge ring or its
+// whole interior to be evaluated.
+enum : int { DIRTY_EDGE = 1, DIRTY_FULL = 2 };
+// Marks dirty (whole interior) the tiles whose pixels or halo hold pixel
+// (i, j) of an m x n grid with tm tiles along i.
+__device__ __forceinline__ void mark_tiles_near(int *dirty, int tm, int64_t i, int64_t j,
+                                                int64_t m, int64_t n) {
+  const int ti0 = (int)((i > 0 ? i - 1 : 0) / kTile), ti1 = (int)((i + 1 < m ? i + 1 : i) / kTile);
+  const int tj0 = (int)((j > 0 ? j - 1 : 0) / kTile), tj1 = (int)((j + 1 < n ? j + 1 : j) / kTile);
+  for (int tj = tj0; tj <= tj1; tj++)
+    for (int ti = ti0; ti <= ti1; ti++) dirty[tj * tm + ti] = DIRTY_FULL;
+}
+
+// The gwdt start written by the costs pass (pipeline entry points, which do
+// not return the costs): the costs array becomes the relaxation's cost
+// array (NaN at non-flat pixels), `dist` gets 1 at presills and +INF
+// elsewhere, and the tiles around presills are marked in `dirty` (zeroed
+// by the caller, one int per tile).
+struct GwdtSeed {
+  float *dist;
+  int *dirty;
+};
 tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
                          const int32_t *flats, const float *orig,
                          const float *filled, const GridDims &g,
-                         cudaStream_t st);
+                         cudaStream_t st, const GwdtSeed *seed = nullptr);
 tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
                         const int32_t *flats, const GridDims &g,
                         cudaStream_t st);
+// gwdt from the start a costs pass with a GwdtSeed wrote (`costs` in the
+// relaxation's form, `dirty` its tile flags).
+tt_cuda_status gwdt_seeded_dev(float *dist, const float *costs, const int32_t *flats,
+                               int *dirty, const GridDims &g, cudaStream_t st);
 tt_cuda_status directions_dev(uint8_t *dir, const float *dem,
                               const float *dist, const int32_t *flats,
                               const GridDims &g, unsigned order,

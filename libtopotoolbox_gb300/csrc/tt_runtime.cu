@@ -752,8 +752,26 @@ static tt_cuda_status pipeline_body(float *filled, int32_t *flats, float *dist,
   if (out) TT_TRY(out->send(out->filled, filled, n * 4, st));
   TT_TRY(identifyflats_dev(flats, filled, g, nullptr, st));
   if (out) TT_TRY(out->send(out->flats, flats, n * 4, st));
-  TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));  // conncomps may be null
-  TT_TRY_SOFT(gwdt_dev(dist, nullptr, costs, flats, g, st), soft);
+  // The costs pass writes the gwdt start directly (the pipeline does not
+  // return the costs), except under the ordered schedules, whose tile
+  // priorities the start would have to set as well.
+  if (relax_schedule() < 4) {
+    const size_t tb = (size_t)g.tiles() * 4;
+    int *gdirty = nullptr;
+    TT_CHECK(cudaMallocAsync((void **)&gdirty, tb, st));
+    struct Free {
+      void *p;
+      cudaStream_t st;
+      ~Free() { cudaFreeAsync(p, st); }
+    } free_dirty{gdirty, st};
+    TT_CHECK(cudaMemsetAsync(gdirty, 0, tb, st));
+    const GwdtSeed seed{dist, gdirty};
+    TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st, &seed));
+    TT_TRY_SOFT(gwdt_seeded_dev(dist, costs, flats, gdirty, g, st), soft);
+  } else {
+    TT_TRY(costs_dev(costs, conncomps, flats, dem, filled, g, st));  // conncomps may be null
+    TT_TRY_SOFT(gwdt_dev(dist, nullptr, costs, flats, g, st), soft);
+  }
   if (out) TT_TRY(out->send(out->dist, dist, n * 4, st));
   TT_TRY(directions_dev(direction, filled, dist, flats, g, 0, st));
   if (out) TT_TRY(out->send(out->direction, direction, n, st));
