@@ -717,6 +717,8 @@ __global__ void fill_init_kernel(float *__restrict__ f, const float *__restrict_
 constexpr int kCoarse = 4;
 
 // Coarse DEM and seeds; grid: x over coarse rows, y over coarse columns.
+// bcc: 1 for a coarse seed, 2 for a cell whose seed pixels cannot make it
+// one (it holds a NaN pixel), 0 for a cell without seed pixels.
 __global__ void maxpool_kernel(float *__restrict__ dc, uint8_t *__restrict__ bcc,
                                const float *__restrict__ dem, const uint8_t *__restrict__ bc,
                                int64_t m, int64_t n, int64_t mc, int64_t nc) {
@@ -738,17 +740,16 @@ __global__ void maxpool_kernel(float *__restrict__ dc, uint8_t *__restrict__ bcc
         }
       }
       dc[jc * mc + ic] = nan ? INFINITY : mx;
-      bcc[jc * mc + ic] = (seed && !nan) ? 1 : 0;
+      bcc[jc * mc + ic] = !seed ? 0 : nan ? 2 : 1;
     }
 }
 
 // f = dem at seeds and NaN pixels, max(dem, coarse fill of the pixel's cell)
-// elsewhere; tiles around seeds start dirty (as from the seeded start).
+// elsewhere.
 __global__ void fill_bound_init_kernel(float *__restrict__ f, const float *__restrict__ dem,
                                        const uint8_t *__restrict__ bc,
                                        const float *__restrict__ fc, int64_t m, int64_t n,
-                                       int64_t mc, int *__restrict__ dirty,
-                                       int *__restrict__ prio, int tm) {
+                                       int64_t mc) {
   for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
     const float *const fcol = fc + (j / kCoarse) * mc;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
@@ -757,23 +758,28 @@ __global__ void fill_bound_init_kernel(float *__restrict__ f, const float *__res
       const float z = dem[p];
       const bool seed = bc[p] == 1 || isnan(z);
       f[p] = seed ? z : fmaxf(z, fcol[i / kCoarse]);
-      if (seed) mark_tiles_around(dirty, prio, tm, i, j, m, n);
     }
   }
 }
 
-// Tiles with a finite bound anywhere start dirty: their pixels are not yet
-// at the tile's fixpoint.  One thread per tile over its coarse cells.
+// The tiles that can change start dirty: a pixel at +INF is lowered only by
+// a finite pixel beside it, and a finite non-seed pixel may lie above the
+// fill.  So a tile starts dirty when a coarse cell over it or over its
+// one-pixel halo (the ring of cells around it) has a finite bound or a
+// seed pixel.  One thread per tile.
 __global__ void dirty_bound_kernel(int *__restrict__ dirty, int *__restrict__ prio,
-                                   const float *__restrict__ fc, int64_t mc, int64_t nc,
+                                   const float *__restrict__ fc,
+                                   const uint8_t *__restrict__ bcc, int64_t mc, int64_t nc,
                                    int tm, int T) {
   constexpr int kCells = kTile / kCoarse;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
     const int64_t ic0 = (int64_t)(t % tm) * kCells, jc0 = (int64_t)(t / tm) * kCells;
+    const int64_t ia = ic0 > 0 ? ic0 - 1 : 0, ib = ic0 + kCells + 1 < mc ? ic0 + kCells + 1 : mc;
+    const int64_t ja = jc0 > 0 ? jc0 - 1 : 0, jb = jc0 + kCells + 1 < nc ? jc0 + kCells + 1 : nc;
     bool any = false;
-    for (int64_t jc = jc0; jc < jc0 + kCells && jc < nc && !any; jc++)
-      for (int64_t ic = ic0; ic < ic0 + kCells && ic < mc; ic++)
-        if (fc[jc * mc + ic] < INFINITY) {
+    for (int64_t jc = ja; jc < jb && !any; jc++)
+      for (int64_t ic = ia; ic < ib; ic++)
+        if (fc[jc * mc + ic] < INFINITY || bcc[jc * mc + ic]) {
           any = true;
           break;
         }
@@ -957,7 +963,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
                          const GridDims &g, cudaStream_t st, const uint8_t *bc = nullptr,
                          const float *bound = nullptr, int64_t bound_mc = 0,
                          int64_t bound_nc = 0, bool report = true,
-                         int *seeded_dirty = nullptr) {
+                         int *seeded_dirty = nullptr, const uint8_t *bound_seeds = nullptr) {
   const int T = g.tiles();
   const int sched = relax_schedule();
   const bool ordered = sched >= 4;
@@ -995,9 +1001,9 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   if (KIND == FILL && bc && bound) {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(fill_bound_init_kernel, col_grid(g.m, g.n), 256, 0, st, state, aux, bc, bound,
-              g.m, g.n, bound_mc, dirty, prio, g.tm);
-    TT_LAUNCH(dirty_bound_kernel, tgrid, 256, 0, st, dirty, prio, bound, bound_mc, bound_nc,
-              g.tm, T);
+              g.m, g.n, bound_mc);
+    TT_LAUNCH(dirty_bound_kernel, tgrid, 256, 0, st, dirty, prio, bound, bound_seeds,
+              bound_mc, bound_nc, g.tm, T);
   } else if (KIND == FILL && bc) {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
     TT_LAUNCH(fill_init_kernel, elementwise_grid(g.cells()), 256, 0, st, state, aux, bc, g.m,
@@ -1075,7 +1081,7 @@ tt_cuda_status fill_impl(float *f, const float *dem, const uint8_t *bc, const Gr
   tt_cuda_status s = fill_impl(fc, dc, bcc, make_dims(cd), st, true, false);
   // A coarse fill that reached the iteration cap is still an upper bound.
   if (s == TT_CUDA_SUCCESS || s == TT_CUDA_ERR_NOT_CONVERGED)
-    s = run_queue<FILL>(f, dem, nullptr, g, st, bc, fc, mc, nc, report);
+    s = run_queue<FILL>(f, dem, nullptr, g, st, bc, fc, mc, nc, report, nullptr, bcc);
   cudaFreeAsync(buf, st);
   return s;
 }
