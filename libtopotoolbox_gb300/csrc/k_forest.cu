@@ -53,6 +53,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include <cuda/atomic>
 
@@ -94,7 +95,7 @@ struct UpArgs {
   bool want_h;
   CoarseCell *ccell;  // per exit id: sums, longest path, pending coarse donors
   CoarseCell *cell;   // per exit pixel: final totals, read by the final pass
-  long long *lacc;   // per pixel: in-tile (local) fixed-point total
+  void *lacc;        // per pixel: in-tile (local) total, long long (int for unit counts)
   int16_t *lrl;      // per pixel: local receiver or RL_* code
   uint8_t *emask;    // per tile and ring pixel: directions of donors in other tiles
   int *xmap;        // per entry pixel: id of the exit reached in-tile, or -1
@@ -183,12 +184,23 @@ constexpr int kUpBlocks = 9;
 constexpr int kFinBlocks = 11;
 constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
 
+// Tile sums: 64-bit fixed point for weights, 32-bit pixel counts for unit
+// weights (a count never exceeds the 2^31 - 1 pixels a grid may hold), which
+// halves the local totals' traffic and the shared-memory atomics' width.
+template <bool U32>
+using AccT = typename std::conditional<U32, int, long long>::type;
+__device__ __forceinline__ void acc_add(int *p, int v) { atomicAdd(p, v); }
+__device__ __forceinline__ void acc_add(long long *p, long long v) {
+  atomicAdd((unsigned long long *)p, (unsigned long long)v);
+}
+
+template <typename AT>
 struct UpTile {
   uint8_t dir[kHalo][36];   // [c][r], one-pixel halo
   int16_t rl[kTileCells];   // local receiver or an RL_* code
   int16_t leaf[kTileCells];  // in-tile leaves, in the order the walks take them
   int pend[kTileCells];     // in-tile donors not yet arrived
-  long long acc[kTileCells];
+  AT acc[kTileCells];
   int h[kTileCells];
   int nvalid;
   int owned;
@@ -253,9 +265,10 @@ __device__ __forceinline__ void stage_dirs(uint8_t (*dir)[36], const uint8_t *__
 // columns jj = tid / 32 + 4 u, so its global indices advance by 4 m.
 constexpr int kPerThread = kTileCells / kUpThreads;  // 8
 
-template <bool ACC, bool H, unsigned ORDER>
+template <bool ACC, bool H, unsigned ORDER, bool U32>
 __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs a) {
-  __shared__ UpTile t;
+  using AT = AccT<U32>;
+  __shared__ UpTile<AT> t;
   const int tid = threadIdx.x;
   const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
@@ -291,7 +304,10 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       t.rl[e] = (int16_t)rl;
       bad |= rl == RL_BADDIR;
       if (rl >= 0) atomicAdd(&t.pend[rl], 1);
-      if (ACC) t.acc[e] = in ? (a.w ? to_fixed(a.w[g0 + u * gstep], wshift, a.err) : 1LL) : 0LL;
+      if (ACC)
+        t.acc[e] = !in ? AT(0)
+                   : (U32 || !a.w) ? AT(1)
+                                   : AT(to_fixed(a.w[g0 + u * gstep], wshift, a.err));
       if (H) t.h[e] = 0;
       nvalid += in;
     }
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
     {
       const int nleaf = t.nleaf;
       int cur = -1;
-      long long v = 0;
+      AT v = 0;
       int hv = 0;
       for (int guard = 0; guard < 2 * kTileCells + 2; guard++) {
         if (cur < 0) {
@@ -351,7 +367,7 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
           cur = -1;
           continue;
         }
-        if (ACC) atomicAdd((unsigned long long *)&t.acc[q], (unsigned long long)v);
+        if (ACC) acc_add(&t.acc[q], v);
         if (H) atomicMax(&t.h[q], hv + 1);
         cuda::atomic_ref<int, cuda::thread_scope_block> pend(t.pend[q]);
         if (pend.fetch_sub(1, cuda::std::memory_order_acq_rel) != 1) {
@@ -373,13 +389,13 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
       const int jj = jb + 4 * u, e = tid + u * kUpThreads;
       if (!(inner || (row_in && j0 + jj < a.n))) continue;
       const int64_t gp = g0 + u * gstep;
-      if (ACC) a.lacc[gp] = t.acc[e];  // local totals for the final pass
+      if (ACC) static_cast<AT *>(a.lacc)[gp] = t.acc[e];  // local totals for the final pass
       if (H) a.h_out[gp] = t.h[e];
       const int rl = t.rl[e];
       a.lrl[gp] = (int16_t)rl;
       if (rl != RL_EXIT) continue;
       const int id = append_slot(a.ecount);  // dense exit ids
-      a.ccell[id] = CoarseCell{ACC ? t.acc[e] : 0LL, H ? t.h[e] : 0, 0};
+      a.ccell[id] = CoarseCell{ACC ? (long long)t.acc[e] : 0LL, H ? t.h[e] : 0, 0};
       a.elist[id] = (int)gp;
       t.pend[e] = id;  // the counts are spent: keep the exit's id there
     }
@@ -404,15 +420,17 @@ __global__ void __launch_bounds__(kUpThreads, kUpBlocks) forest_up_kernel(UpArgs
 // ring pixel) gathers its inflow from the coarse cells of those donors and
 // walks its path to the terminal, adding the inflow and raising h to
 // (longest path into the entry) + (steps walked).
+template <typename AT>
 struct FinTile {
-  long long acc[kTileCells];
+  AT acc[kTileCells];
   int h[kTileCells];
   int16_t rl[kTileCells];
 };
 
-template <bool ACC, bool H, unsigned ORDER>
+template <bool ACC, bool H, unsigned ORDER, bool U32>
 __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpArgs a) {
-  __shared__ FinTile t;
+  using AT = AccT<U32>;
+  __shared__ FinTile<AT> t;
   const int tid = threadIdx.x;
   const int ii = tid & (kTile - 1), jb = tid >> 5;
   const int T = a.tm * a.tn;
@@ -432,7 +450,7 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
       const int e = tid + u * kUpThreads;
       const bool in = full || (row_in && j0 + jb + 4 * u < a.n);
       const int64_t gp = g0 + u * gstep;
-      if (ACC) t.acc[e] = in ? a.lacc[gp] : 0LL;
+      if (ACC) t.acc[e] = in ? static_cast<const AT *>(a.lacc)[gp] : AT(0);
       if (H) t.h[e] = in ? a.h_out[gp] : 0;
       t.rl[e] = in ? a.lrl[gp] : (int16_t)RL_NONE;
     }
@@ -455,8 +473,7 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
       }
       int cur = re;
       for (int d = 0; d < kTileCells; d++) {
-        if (ACC && inflow)
-          atomicAdd((unsigned long long *)&t.acc[cur], (unsigned long long)inflow);
+        if (ACC && inflow) acc_add(&t.acc[cur], (AT)inflow);
         if (H) atomicMax(&t.h[cur], hin + d);
         const int q = t.rl[cur];
         if (q < 0) break;
@@ -477,7 +494,7 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
         } else if (raw_out) {
           raw_out[gp] = t.acc[e];
         } else {
-          const float v = __ll2float_rn(t.acc[e]);
+          const float v = U32 ? __int2float_rn((int)t.acc[e]) : __ll2float_rn(t.acc[e]);
           a.acc_out[gp] = wshift ? ldexpf(v, -wshift) : v;
         }
       }
@@ -1010,7 +1027,7 @@ int list_grid(int64_t n) {
 
 struct UpWork {
   CoarseCell *ccell, *cell;
-  long long *lacc;
+  void *lacc;  // long long per pixel (int for unit counts)
   int16_t *lrl;
   uint8_t *emask;
   int2 *link;
@@ -1046,7 +1063,7 @@ tt_cuda_status up_alloc(const GridDims &g, bool want_acc, bool want_h,
   w.cell = (CoarseCell *)ws.take(N * sizeof(CoarseCell));
   w.ccell = (CoarseCell *)ws.take(E * sizeof(CoarseCell));
   w.link = (int2 *)ws.take(E * 8);
-  w.lacc = want_acc ? (long long *)ws.take(N * 8) : nullptr;
+  w.lacc = want_acc ? ws.take(N * 8) : nullptr;
   w.lrl = (int16_t *)ws.take(N * 2);
   w.emask = (uint8_t *)ws.take((size_t)g.tiles() * kRing);
   w.h = want_h ? (int *)ws.take(N * 4) : nullptr;
@@ -1100,15 +1117,27 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   const int fgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks);
   void (*up)(UpArgs) = nullptr;
   void (*fin)(UpArgs) = nullptr;
-  if (want_acc && want_h) {
-    up = order ? forest_up_kernel<true, true, 1> : forest_up_kernel<true, true, 0>;
-    fin = order ? forest_fin_kernel<true, true, 1> : forest_fin_kernel<true, true, 0>;
+  const bool u32 = !weights;  // unit weights: 32-bit counts in the tile passes
+  if (want_acc && want_h && u32) {
+    up = order ? forest_up_kernel<true, true, 1, true> : forest_up_kernel<true, true, 0, true>;
+    fin = order ? forest_fin_kernel<true, true, 1, true> : forest_fin_kernel<true, true, 0, true>;
+  } else if (want_acc && want_h) {
+    up = order ? forest_up_kernel<true, true, 1, false> : forest_up_kernel<true, true, 0, false>;
+    fin = order ? forest_fin_kernel<true, true, 1, false>
+                : forest_fin_kernel<true, true, 0, false>;
+  } else if (want_acc && u32) {
+    up = order ? forest_up_kernel<true, false, 1, true> : forest_up_kernel<true, false, 0, true>;
+    fin = order ? forest_fin_kernel<true, false, 1, true>
+                : forest_fin_kernel<true, false, 0, true>;
   } else if (want_acc) {
-    up = order ? forest_up_kernel<true, false, 1> : forest_up_kernel<true, false, 0>;
-    fin = order ? forest_fin_kernel<true, false, 1> : forest_fin_kernel<true, false, 0>;
+    up = order ? forest_up_kernel<true, false, 1, false>
+               : forest_up_kernel<true, false, 0, false>;
+    fin = order ? forest_fin_kernel<true, false, 1, false>
+                : forest_fin_kernel<true, false, 0, false>;
   } else {
-    up = order ? forest_up_kernel<false, true, 1> : forest_up_kernel<false, true, 0>;
-    fin = order ? forest_fin_kernel<false, true, 1> : forest_fin_kernel<false, true, 0>;
+    up = order ? forest_up_kernel<false, true, 1, false> : forest_up_kernel<false, true, 0, false>;
+    fin = order ? forest_fin_kernel<false, true, 1, false>
+                : forest_fin_kernel<false, true, 0, false>;
   }
   TT_LAUNCH(up, tgrid, kUpThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
