@@ -467,7 +467,7 @@ __global__ void costs_kernel(float *__restrict__ costs,
       }
       if (SEED) {  // the gwdt start (src/gwdt.c:296-308) instead of plain costs
         const int32_t f = fv[u];
-        costs[p] = (f & 1) ? c : NAN;
+        costs[p] = (f & 1) ? c * 0.5f : NAN;  // halved: c >= 0.1, exact
         seed.dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
         if ((f & 5) == 5) mark_tiles_near(seed.dirty, tm, p % m, p / m, m, n);
       } else {

@@ -56,7 +56,11 @@ constexpr int kWarps = 4;        // tiles per block
 constexpr int kMaxSweeps = 256;  // per tile visit; a capped tile re-enqueues
 constexpr float kSqrt2 = 1.41421356237309504880f;
 
-enum Kind { FILL = 0, GWDT = 1 };
+// GWDT_HALF: gwdt over costs stored halved (the pipeline's own costs, at
+// least 0.1, so halving is exact and every intermediate stays normal): a
+// step's weights lose one multiplication and keep their bits, since
+// RN(x / 2) = RN(x) / 2 for normal x.
+enum Kind { FILL = 0, GWDT = 1, GWDT_HALF = 2 };
 
 struct WarpTile {
   float s[kHalo][kPitch];  // state: f (fill) or dist (gwdt); [c][r]
@@ -231,7 +235,7 @@ __device__ __forceinline__ void sweep_fill(WarpTile &t, int lane, int dir, uint3
 // Non-flat and off-grid pixels are staged as state +INF and cost NaN: every
 // path through them evaluates to +INF or NaN, which never wins the minimum,
 // and a non-flat centre (cost NaN) keeps its value.
-template <bool ALONG_C>
+template <bool ALONG_C, bool HALF>
 __device__ __forceinline__ void sweep_gwdt_run(WarpTile &t, int lane, int dir, uint32_t &nd,
                                                uint32_t &dm_all) {
   const uint32_t steps = __reduce_or_sync(0xffffffffu, nd);
@@ -269,12 +273,15 @@ __device__ __forceinline__ void sweep_gwdt_run(WarpTile &t, int lane, int dir, u
     const float oa = sp[D], la = sp[-LS + D], ra = sp[LS + D];
     const float ca0 = ap[-LS + D], ca1 = ap[D], ca2 = ap[LS + D];
     const float cur = op, cs = cp1;
-    // d(u) + chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact
+    // d(u) + chamfer * (c(u) + c(v)) / 2; multiplying by 1 is exact (HALF:
+    // the costs are already halved)
     auto side = [&](float d, float c) {
-      return __fadd_rn(d, __fmul_rn(__fadd_rn(cs, c), 0.5f));
+      return HALF ? __fadd_rn(d, __fadd_rn(cs, c))
+                  : __fadd_rn(d, __fmul_rn(__fadd_rn(cs, c), 0.5f));
     };
     auto diag = [&](float d, float c) {
-      return __fadd_rn(d, __fmul_rn(__fmul_rn(kSqrt2, __fadd_rn(cs, c)), 0.5f));
+      return HALF ? __fadd_rn(d, __fmul_rn(kSqrt2, __fadd_rn(cs, c)))
+                  : __fadd_rn(d, __fmul_rn(__fmul_rn(kSqrt2, __fadd_rn(cs, c)), 0.5f));
     };
     float best = fminf(cur, fminf(side(oa, ca1), side(lp, cp0)));
     best = fminf(best, fminf(side(rp, cp2), diag(la, ca0)));
@@ -308,7 +315,7 @@ __device__ __forceinline__ void sweep(WarpTile &t, int lane, int dir, uint32_t &
   if (KIND == FILL)
     sweep_fill<ALONG_C>(t, lane, dir, nd, dm_all);
   else
-    sweep_gwdt_run<ALONG_C>(t, lane, dir, nd, dm_all);
+    sweep_gwdt_run<ALONG_C, KIND == GWDT_HALF>(t, lane, dir, nd, dm_all);
 }
 
 // Sweep schedules (a template parameter, picked at run time): bit 0 runs the
@@ -968,19 +975,19 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   const int sched = relax_schedule();
   const bool ordered = sched >= 4;
   // gwdt seeded by the costs pass: state, costs and flags are in place
-  const bool seeded = KIND == GWDT && seeded_dirty;
+  const bool seeded = KIND != FILL && seeded_dirty;
   if (seeded && ordered) return TT_CUDA_ERR_INVALID_ARGUMENT;  // no priorities seeded
   const int wmax = sm_count() * 32 * kWarps;  // more warp slots than any grid has warps
   Workspace &ws = workspace();
   size_t need = align_up(sizeof(QueueCtl)) + align_up((size_t)T * 4);
-  if (KIND == GWDT && !seeded) need += align_up((size_t)g.cells() * 4);
+  if (KIND != FILL && !seeded) need += align_up((size_t)g.cells() * 4);
   if (ordered) need += align_up((size_t)T * 4) + align_up((size_t)wmax * 4);
   if (!ws.reserve(need)) return TT_CUDA_ERR_ALLOC;
   QueueCtl *ctl = (QueueCtl *)ws.take(sizeof(QueueCtl));
   int *dirty = seeded ? seeded_dirty : (int *)ws.take((size_t)T * 4);
   // gwdt relaxes over a copy of the costs with NaN at non-flat pixels (a
   // seeded run over the costs array itself, already in that form)
-  float *wcost = KIND != GWDT ? nullptr
+  float *wcost = KIND == FILL ? nullptr
                  : seeded    ? const_cast<float *>(aux)
                              : (float *)ws.take((size_t)g.cells() * 4);
   int *prio = ordered ? (int *)ws.take((size_t)T * 4) : nullptr;
@@ -988,7 +995,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   QueueCtl *hctl = (QueueCtl *)pinned_scratch();
   if (!hctl) return TT_CUDA_ERR_ALLOC;
 
-  RelaxArgs ra{state, KIND == GWDT ? wcost : aux, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1,
+  RelaxArgs ra{state, KIND != FILL ? wcost : aux, g.m, g.n, g.tm, g.tn, ctl, dirty, 0, 1,
                prio, wmin};
   if (ordered) {  // no priorities, no waiting work (kClean = 0x7f7f7f7f)
     TT_CHECK(cudaMemsetAsync(prio, 0x7f, (size_t)T * 4, st));
@@ -1016,7 +1023,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
               flats, g.m, g.n, ra);
   }
   TT_CHECK(cudaGetLastError());
-  static int blocks_per_sm[2][kSchedules] = {};
+  static int blocks_per_sm[3][kSchedules] = {};
   if (!blocks_per_sm[KIND][sched]) {
     int b = 0;
     switch (sched) {
@@ -1041,7 +1048,7 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
     case 5: TT_CHECK((launch_relax<KIND, 5>(grid, ra, st))); break;
     default: TT_CHECK((launch_relax<KIND, 0>(grid, ra, st))); break;
   }
-  if (KIND == GWDT)
+  if (KIND != FILL)
     TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
   // deferred: the abort word goes to the status sink, no round trip (when the
@@ -1109,7 +1116,7 @@ tt_cuda_status reconstruct_dev(float *marker, const float *mask,
 
 tt_cuda_status gwdt_seeded_dev(float *dist, const float *costs, const int32_t *flats,
                                int *dirty, const GridDims &g, cudaStream_t st) {
-  return run_queue<GWDT>(dist, costs, flats, g, st, nullptr, nullptr, 0, 0, true, dirty);
+  return run_queue<GWDT_HALF>(dist, costs, flats, g, st, nullptr, nullptr, 0, 0, true, dirty);
 }
 
 tt_cuda_status gwdt_dev(float *dist, ptrdiff_t *prev, const float *costs,
