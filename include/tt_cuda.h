@@ -24,9 +24,9 @@
  *
  * The `_dev` variants take DEVICE pointers and a `cudaStream_t` (passed as
  * `void *`, NULL = legacy default stream), enqueue their work on that stream
- * and return a status.  Iterative stages (fill, gwdt) read a small
- * convergence counter back to the host between device sweeps, so these calls
- * synchronise the stream before they return.
+ * and return a status.  They synchronise the stream before they return, to
+ * report an iteration cap or a cycle, unless the caller defers their status
+ * (tt_cuda_defer_begin / tt_cuda_defer_end below).
  *
  * Calls are serialised per device by an internal mutex.
  */
@@ -132,7 +132,11 @@ TT_CUDA_API tt_cuda_status tt_cuda_defer_end(void);
 /* Drop-in host-pointer entry points                                    */
 /* ------------------------------------------------------------------ */
 
-/** include/topotoolbox.h:293 fillsinks (src/fillsinks.c:23-48). */
+/** include/topotoolbox.h:293 fillsinks (src/fillsinks.c:23-48).  Grids of
+ *  12288 pixels a side and more start from the fill of the DEM max-pooled
+ *  over 4 x 4 cells, an upper bound of the result (the same bits, fewer
+ *  iterations); the environment variable TT_CUDA_FILL_BOUND_MIN sets that
+ *  side at load time (0: never). */
 TT_CUDA_API void tt_cuda_fillsinks(float *output, float *dem, uint8_t *bc,
                                    ptrdiff_t dims[2]);
 /** include/topotoolbox.h:351 fillsinks_hybrid (src/fillsinks.c:51-77).
