@@ -61,3 +61,16 @@ def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
 
     with pytest.raises(ImportError):
         api.fillsinks(np.zeros((4, 4), np.float32), np.ones((4, 4), np.uint8))
+
+
+def test_deferral_without_a_device():
+    """Deferred status on a host without a GPU: nothing to defer, and ending a
+    deferral that never began is an argument error (no device call made)."""
+    from libtopotoolbox_gb300 import _native
+
+    lib = _native.lib()
+    if lib.tt_cuda_has_gpu():
+        pytest.skip("a GPU is present: tests/test_gpu_deferred.py covers deferral")
+    assert lib.tt_cuda_defer_end() == 1
+    assert lib.tt_cuda_defer_begin(None) == 6
+    assert lib.tt_cuda_defer_end() == 1
