@@ -314,10 +314,18 @@ def batch_leg(dev, reps=3, rank=0, world=1, dist=None):
 
     per_dem()
     per = max_over_ranks(timed(per_dem, 1))
+
+    def per_dem_deferred():  # the same calls without a host round trip each
+        with D.deferred():
+            per_dem()
+
+    per_dem_deferred()
+    per_def = max_over_ranks(timed(per_dem_deferred, 1))
     info = bt.info()
     bt.close()
     res = {"workload": f"{len(all_shapes)} DEMs, sides log-uniform 128..2048, {cells} pixels",
            "batched_ms": batched, "per_dem_ms": per, "speedup": per / batched,
+           "per_dem_deferred_ms": per_def, "speedup_vs_deferred": per_def / batched,
            "batched_gcells_s": cells / (batched * 1e-3) / 1e9,
            "canvas": [info["canvas_rows"], info["canvas_cols"]],
            "graph_nodes": info["graph_nodes"], "tuned_canvas_cols": best["canvas_cols"],
