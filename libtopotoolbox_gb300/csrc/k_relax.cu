@@ -751,6 +751,42 @@ __global__ void maxpool_kernel(float *__restrict__ dc, uint8_t *__restrict__ bcc
     }
 }
 
+// The same for grids whose rows come in whole cells (m a multiple of 4,
+// so every column of a 16-byte aligned array starts 16-byte aligned): a
+// thread takes one cell's four rows of a column with one 16-byte load.
+__global__ void maxpool4_kernel(float *__restrict__ dc, uint8_t *__restrict__ bcc,
+                                const float4 *__restrict__ dem,
+                                const uint32_t *__restrict__ bc, int64_t m, int64_t n,
+                                int64_t mc, int64_t nc) {
+  const int64_t m4 = m / kCoarse;  // == mc
+  for (int64_t jc = blockIdx.y; jc < nc; jc += gridDim.y)
+    for (int64_t ic = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ic < mc;
+         ic += (int64_t)gridDim.x * blockDim.x) {
+      float mx = -INFINITY;
+      bool nan = false, seed = false;
+      float4 v[kCoarse];
+      uint32_t b[kCoarse];
+#pragma unroll
+      for (int dj = 0; dj < kCoarse; dj++) {
+        const int64_t j = jc * kCoarse + dj;
+        const int64_t jj = j < n ? j : n - 1;  // a partial last cell repeats its last column
+        v[dj] = dem[jj * m4 + ic];
+        b[dj] = bc[jj * m4 + ic];
+      }
+#pragma unroll
+      for (int dj = 0; dj < kCoarse; dj++) {
+        nan |= isnan(v[dj].x) | isnan(v[dj].y) | isnan(v[dj].z) | isnan(v[dj].w);
+        mx = fmaxf(mx, fmaxf(fmaxf(v[dj].x, v[dj].y), fmaxf(v[dj].z, v[dj].w)));
+        // bc bytes are 0 or 1 on the path; a seed is a byte equal to 1
+        const uint32_t w = b[dj];
+        seed |= ((w & 0xffu) == 1u) | (((w >> 8) & 0xffu) == 1u) | (((w >> 16) & 0xffu) == 1u) |
+                ((w >> 24) == 1u);
+      }
+      dc[jc * mc + ic] = nan ? INFINITY : mx;
+      bcc[jc * mc + ic] = !seed ? 0 : nan ? 2 : 1;
+    }
+}
+
 // f = dem at seeds and NaN pixels, max(dem, coarse fill of the pixel's cell)
 // elsewhere.
 __global__ void fill_bound_init_kernel(float *__restrict__ f, const float *__restrict__ dem,
@@ -765,6 +801,31 @@ __global__ void fill_bound_init_kernel(float *__restrict__ f, const float *__res
       const float z = dem[p];
       const bool seed = bc[p] == 1 || isnan(z);
       f[p] = seed ? z : fmaxf(z, fcol[i / kCoarse]);
+    }
+  }
+}
+
+// fill_bound_init_kernel for m a multiple of 4: a thread takes the four
+// rows of one cell in one column (one coarse value, 16-byte loads and
+// stores).
+__global__ void fill_bound_init4_kernel(float4 *__restrict__ f, const float4 *__restrict__ dem,
+                                        const uint32_t *__restrict__ bc,
+                                        const float *__restrict__ fc, int64_t m, int64_t n,
+                                        int64_t mc) {
+  const int64_t m4 = m / kCoarse;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const float *const fcol = fc + (j / kCoarse) * mc;
+    for (int64_t i4 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i4 < m4;
+         i4 += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t q = j * m4 + i4;
+      const float4 z = dem[q];
+      const uint32_t b = bc[q];
+      const float c = fcol[i4];
+      auto one = [&](float zv, uint32_t bv) {
+        return (bv == 1u || isnan(zv)) ? zv : fmaxf(zv, c);
+      };
+      f[q] = make_float4(one(z.x, b & 0xffu), one(z.y, (b >> 8) & 0xffu),
+                         one(z.z, (b >> 16) & 0xffu), one(z.w, b >> 24));
     }
   }
 }
@@ -927,6 +988,9 @@ dim3 col_grid(int64_t rows, int64_t cols) {
   return dim3((unsigned)bx, (unsigned)by);
 }
 
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+inline bool aligned4(const void *p) { return ((uintptr_t)p & 3u) == 0; }
+
 // Smallest grid side that starts the fill from a coarse bound (0: never);
 // TT_CUDA_FILL_BOUND_MIN overrides it.  Measured on the 16384² workload
 // generator: 16384² 10.11 -> 9.45 ms (visits per tile 5 -> 3), 8192² no
@@ -1007,8 +1071,13 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
   const int tgrid = (T + 255) / 256;
   if (KIND == FILL && bc && bound) {
     TT_CHECK(cudaMemsetAsync(dirty, 0, (size_t)T * 4, st));
-    TT_LAUNCH(fill_bound_init_kernel, col_grid(g.m, g.n), 256, 0, st, state, aux, bc, bound,
-              g.m, g.n, bound_mc);
+    if (g.m % kCoarse == 0 && aligned16(state) && aligned16(aux) && aligned4(bc))
+      TT_LAUNCH(fill_bound_init4_kernel, col_grid(g.m / kCoarse, g.n), 256, 0, st,
+                (float4 *)state, (const float4 *)aux, (const uint32_t *)bc, bound, g.m, g.n,
+                bound_mc);
+    else
+      TT_LAUNCH(fill_bound_init_kernel, col_grid(g.m, g.n), 256, 0, st, state, aux, bc, bound,
+                g.m, g.n, bound_mc);
     TT_LAUNCH(dirty_bound_kernel, tgrid, 256, 0, st, dirty, prio, bound, bound_seeds,
               bound_mc, bound_nc, g.tm, T);
   } else if (KIND == FILL && bc) {
@@ -1083,7 +1152,11 @@ tt_cuda_status fill_impl(float *f, const float *dem, const uint8_t *bc, const Gr
   TT_CHECK(cudaMallocAsync((void **)&buf, align_up(Nc * 4) * 2 + align_up(Nc), st));
   float *dc = (float *)buf, *fc = (float *)(buf + align_up(Nc * 4));
   uint8_t *bcc = (uint8_t *)(buf + 2 * align_up(Nc * 4));
-  TT_LAUNCH(maxpool_kernel, col_grid(mc, nc), 256, 0, st, dc, bcc, dem, bc, g.m, g.n, mc, nc);
+  if (g.m % kCoarse == 0 && aligned16(dem) && aligned4(bc))
+    TT_LAUNCH(maxpool4_kernel, col_grid(mc, nc), 256, 0, st, dc, bcc, (const float4 *)dem,
+              (const uint32_t *)bc, g.m, g.n, mc, nc);
+  else
+    TT_LAUNCH(maxpool_kernel, col_grid(mc, nc), 256, 0, st, dc, bcc, dem, bc, g.m, g.n, mc, nc);
   const ptrdiff_t cd[2] = {(ptrdiff_t)mc, (ptrdiff_t)nc};
   tt_cuda_status s = fill_impl(fc, dc, bcc, make_dims(cd), st, true, false);
   // A coarse fill that reached the iteration cap is still an upper bound.
