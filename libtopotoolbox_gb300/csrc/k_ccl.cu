@@ -146,7 +146,7 @@ struct CclTile {
 // maximum depth and the smallest pixel attaining it.
 __global__ void __launch_bounds__(kCclWarps * 32)
 ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ larg,
-                int *__restrict__ maxkey, int *__restrict__ argmax,
+                unsigned long long *__restrict__ best,
                 int *__restrict__ roots, int *__restrict__ nroots,
                 uint4 *__restrict__ edges,
                 const int32_t *__restrict__ flats, const float *__restrict__ orig,
@@ -229,8 +229,7 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         larg[rootp] = first == INT_MAX
                           ? INT_MAX
                           : (int)((j0 + first / kTile) * m + (i0 + first % kTile));
-        maxkey[rootp] = INT_MIN;
-        argmax[rootp] = INT_MAX;
+        best[rootp] = 0ULL;
         roots[atomicAdd(nroots, 1)] = (int)rootp;
       }
       __syncwarp();
@@ -322,8 +321,7 @@ ccl_tile_kernel(int *__restrict__ L, int *__restrict__ lmax, int *__restrict__ l
         const int a = 1023 - (int)(v & 1023u);
         lmax[gp] = v ? (int)((unsigned)(v >> 32) ^ 0x80000000u) : INT_MIN;
         larg[gp] = v ? (int)((j0 + a / kTile) * m + (i0 + a % kTile)) : INT_MAX;
-        maxkey[gp] = INT_MIN;
-        argmax[gp] = INT_MAX;
+        best[gp] = 0ULL;
       } else {
         larg[gp] = -1;  // not a local root
       }
@@ -384,33 +382,38 @@ __global__ void ccl_border_kernel(int *__restrict__ L, const uint4 *__restrict__
   }
 }
 
-// Local roots (a compact list) fold their maxima into their global root.
-__global__ void ccl_max_kernel(int *__restrict__ L, const int *__restrict__ lmax,
-                               const int *__restrict__ roots, const int *__restrict__ nroots,
-                               int *__restrict__ rootR, int *__restrict__ maxkey) {
+// A component's maximum depth key and the smallest pixel attaining it,
+// packed so that one 64-bit maximum over its local roots reduces both: the
+// key (sign flipped to order as unsigned) above, 2^31 - 1 - pixel below.
+// 0 means no key.
+__device__ __forceinline__ unsigned long long pack_root(int key, int pixel) {
+  return ((unsigned long long)((unsigned)key ^ 0x80000000u) << 32) |
+         (unsigned)(0x7fffffff - pixel);
+}
+__device__ __forceinline__ int root_key(unsigned long long v) {
+  return v ? (int)((unsigned)(v >> 32) ^ 0x80000000u) : INT_MIN;
+}
+__device__ __forceinline__ int root_arg(unsigned long long v) {
+  return v ? 0x7fffffff - (int)(unsigned)(v & 0xffffffffu) : INT_MAX;
+}
+
+// Local roots (a compact list) fold their maximum and its first pixel into
+// their global root with one 64-bit maximum, and then point straight at it,
+// so any flat pixel p reaches its root in two steps: L[L[p]] (every label
+// above a pixel is a local root).  The roots are final here (every union
+// is done), and a label only ever moves down to the root, so pointing a
+// local root at it while other threads still walk through it is safe.
+__global__ void ccl_root_kernel(int *__restrict__ L, const int *__restrict__ lmax,
+                                const int *__restrict__ larg, const int *__restrict__ roots,
+                                const int *__restrict__ nroots,
+                                unsigned long long *__restrict__ best) {
   const int K = *nroots;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
     const int p = roots[k];
     const int R = uf_find(L, p);
-    rootR[k] = R;
-    if (lmax[p] != INT_MIN) atomicMax(&maxkey[R], lmax[p]);
-  }
-}
-
-// The argmax of each component over its local roots; afterwards every local
-// root points straight at its global root, so any flat pixel p reaches its
-// root in two steps: L[L[p]] (every label above a pixel is a local root).
-__global__ void ccl_argmax_kernel(int *__restrict__ L, const int *__restrict__ lmax,
-                                  const int *__restrict__ larg,
-                                  const int *__restrict__ roots, const int *__restrict__ nroots,
-                                  const int *__restrict__ rootR,
-                                  const int *__restrict__ maxkey, int *__restrict__ argmax) {
-  const int K = *nroots;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
-    const int p = roots[k];
-    const int R = rootR[k];
-    if (lmax[p] != INT_MIN && lmax[p] == maxkey[R]) atomicMin(&argmax[R], larg[p]);
-    L[p] = R;
+    const int key = lmax[p];
+    if (key != INT_MIN) atomicMax(&best[R], pack_root(key, larg[p]));
+    atomicMin(&L[p], R);
   }
 }
 
@@ -424,8 +427,7 @@ constexpr int kCostPer = 4;
 template <bool SEED>
 __global__ void costs_kernel(float *__restrict__ costs,
                              ptrdiff_t *__restrict__ conncomps, int *__restrict__ L,
-                             const int *__restrict__ maxkey,
-                             const int *__restrict__ argmax,
+                             const unsigned long long *__restrict__ best,
                              const int32_t *__restrict__ flats,
                              const float *__restrict__ orig,
                              const float *__restrict__ filled, int64_t N,
@@ -449,8 +451,9 @@ __global__ void costs_kernel(float *__restrict__ costs,
     for (int u = 0; u < kCostPer; u++) R[u] = l1[u] >= 0 ? L[l1[u]] : -1;
 #pragma unroll
     for (int u = 0; u < kCostPer; u++) {
-      mk[u] = R[u] >= 0 ? maxkey[R[u]] : 0;
-      am[u] = R[u] >= 0 ? argmax[R[u]] : 0;
+      const unsigned long long v = R[u] >= 0 ? best[R[u]] : 0ULL;
+      mk[u] = root_key(v);
+      am[u] = root_arg(v);
     }
 #pragma unroll
     for (int u = 0; u < kCostPer; u++) {
@@ -468,7 +471,7 @@ __global__ void costs_kernel(float *__restrict__ costs,
       if (SEED) {  // the gwdt start (src/gwdt.c:296-308) instead of plain costs
         const int32_t f = fv[u];
         costs[p] = (f & 1) ? c * 0.5f : NAN;  // halved: c >= 0.1, exact
-        seed.dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
+        seed.dist[p] = (f & 5) == 5 ? 1.0f : (f & 1) ? INFINITY : 0.0f;
         if ((f & 5) == 5) mark_tiles_near(seed.dirty, tm, p % m, p / m, m, n);
       } else {
         costs[p] = c;
@@ -493,33 +496,30 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   const int64_t N = g.cells();
   Workspace &ws = workspace();
   const int T = g.tiles();
-  if (!ws.reserve(7 * align_up((size_t)N * 4) + align_up((size_t)T * 16) + 256))
+  if (!ws.reserve(4 * align_up((size_t)N * 4) + align_up((size_t)N * 8) +
+                  align_up((size_t)T * 16) + 256))
     return TT_CUDA_ERR_ALLOC;
   int *nroots = (int *)ws.take(256);
   uint4 *edges = (uint4 *)ws.take((size_t)T * 16);
   int *roots = (int *)ws.take((size_t)N * 4);
-  int *rootR = (int *)ws.take((size_t)N * 4);
   int *L = (int *)ws.take((size_t)N * 4);
   int *lmax = (int *)ws.take((size_t)N * 4);
   int *larg = (int *)ws.take((size_t)N * 4);
-  int *maxkey = (int *)ws.take((size_t)N * 4);
-  int *argmax = (int *)ws.take((size_t)N * 4);
+  unsigned long long *best = (unsigned long long *)ws.take((size_t)N * 8);
   const int grid = ew_grid(N);
   const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
                                            (int64_t)sm_count() * 16);
   TT_CHECK(cudaMemsetAsync(nroots, 0, sizeof(int), st));
-  TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, maxkey, argmax,
-            roots, nroots, edges, flats, orig, filled, g.m, g.n, g.tm, g.tn);
+  TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, best, roots,
+            nroots, edges, flats, orig, filled, g.m, g.n, g.tm, g.tn);
   TT_LAUNCH(ccl_border_kernel, ew_grid(T), 256, 0, st, L, edges, g.m, g.tm, g.tn);
-  TT_LAUNCH(ccl_max_kernel, grid, 256, 0, st, L, lmax, roots, nroots, rootR, maxkey);
-  TT_LAUNCH(ccl_argmax_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, rootR,
-            maxkey, argmax);
+  TT_LAUNCH(ccl_root_kernel, grid, 256, 0, st, L, lmax, larg, roots, nroots, best);
   const int cgrid = (int)std::min<int64_t>((N + 1023) / 1024, (int64_t)sm_count() * 32);
   if (seed)
-    TT_LAUNCH(costs_kernel<true>, cgrid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
+    TT_LAUNCH(costs_kernel<true>, cgrid, 256, 0, st, costs, conncomps, L, best,
               flats, orig, filled, N, *seed, g.m, g.n, g.tm);
   else
-    TT_LAUNCH(costs_kernel<false>, cgrid, 256, 0, st, costs, conncomps, L, maxkey, argmax,
+    TT_LAUNCH(costs_kernel<false>, cgrid, 256, 0, st, costs, conncomps, L, best,
               flats, orig, filled, N, GwdtSeed{nullptr, nullptr}, g.m, g.n, g.tm);
   TT_CHECK(cudaGetLastError());
   return TT_CUDA_SUCCESS;

@@ -232,8 +232,8 @@ __device__ __forceinline__ void sweep_fill(WarpTile &t, int lane, int dir, uint3
 // the end of the line, no votes, with the values a step would re-read
 // unchanged carried in registers (state of the lane's own pixel behind and
 // here, adjacent lines here; costs of all three lines behind and here).
-// Non-flat and off-grid pixels are staged as state +INF and cost NaN: every
-// path through them evaluates to +INF or NaN, which never wins the minimum,
+// Non-flat and off-grid pixels are staged with cost NaN (state 0 or +INF):
+// every path through them evaluates to NaN, which never wins the minimum,
 // and a non-flat centre (cost NaN) keeps its value.
 template <bool ALONG_C, bool HALF>
 __device__ __forceinline__ void sweep_gwdt_run(WarpTile &t, int lane, int dir, uint32_t &nd,
@@ -501,8 +501,8 @@ __device__ void relax_tile(const RelaxArgs &a, WarpTile &t, int lane, int tile, 
   // asynchronous copies.  Off-grid pixels are staged as state +INF with aux
   // +INF (fill: never lowered, never lowers) or NaN (gwdt: a NaN cost makes
   // every path through the pixel NaN, which never wins a minimum).  gwdt's
-  // non-flat pixels arrive that way from global memory already (state +INF,
-  // cost NaN during the run), so no flat flags are staged.
+  // non-flat pixels arrive with cost NaN from global memory already (state
+  // 0 during the run), so no flat flags are staged.
   constexpr float kOffAux = KIND == FILL ? INFINITY : NAN;
   float sv[kHalo], sx[3];
   const int64_t im = i0 - 1 + lane;
@@ -886,10 +886,11 @@ __global__ void dirty_all_kernel(int *dirty, int *prio, int n) {
   }
 }
 
-// gwdt working arrays: distance 1 at presills and +INF at other flats, as
-// src/gwdt.c:296-308 starts; non-flat pixels take +INF with cost NaN for the
-// run (no path passes through them and they are never lowered) and get
-// their 0 back from gwdt_fix_kernel.  Tiles next to a presill start dirty.
+// gwdt working arrays: distance 1 at presills, +INF at other flats and 0
+// at non-flat pixels, as src/gwdt.c:296-308 starts.  Non-flat pixels take
+// cost NaN for the run: every path through one and every update of one
+// evaluates to NaN, which never wins a minimum, so they keep their 0 and
+// pass nothing on.  Tiles next to a presill start dirty.
 __global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ wcost,
                                  const float *__restrict__ costs,
                                  const int32_t *__restrict__ flats, int64_t m,
@@ -910,24 +911,10 @@ __global__ void gwdt_init_kernel(float *__restrict__ dist, float *__restrict__ w
       const int64_t p = p0 + u * stride;
       if (p >= N) continue;
       const int32_t f = fv[u];
-      dist[p] = (f & 5) == 5 ? 1.0f : INFINITY;
+      dist[p] = (f & 5) == 5 ? 1.0f : (f & 1) ? INFINITY : 0.0f;
       wcost[p] = (f & 1) ? cv[u] : NAN;
       if ((f & 5) == 5) mark_tiles_around(qa.dirty, qa.prio, qa.tm, p % m, p / m, m, n);
     }
-  }
-}
-
-// Non-flat pixels: distance 0 (src/gwdt.c:300-302).
-__global__ void gwdt_fix_kernel(float *__restrict__ dist, const int32_t *__restrict__ flats,
-                                int64_t N) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < N; p0 += kEw * stride) {
-    int32_t fv[kEw];
-#pragma unroll
-    for (int u = 0; u < kEw; u++) fv[u] = p0 + u * stride < N ? flats[p0 + u * stride] : 1;
-#pragma unroll
-    for (int u = 0; u < kEw; u++)
-      if (!(fv[u] & 1)) dist[p0 + u * stride] = 0.0f;
   }
 }
 
@@ -1117,8 +1104,6 @@ tt_cuda_status run_queue(float *state, const float *aux, const int32_t *flats,
     case 5: TT_CHECK((launch_relax<KIND, 5>(grid, ra, st))); break;
     default: TT_CHECK((launch_relax<KIND, 0>(grid, ra, st))); break;
   }
-  if (KIND != FILL)
-    TT_LAUNCH(gwdt_fix_kernel, elementwise_grid(g.cells()), 256, 0, st, state, flats, g.cells());
   TT_CHECK(cudaGetLastError());
   // deferred: the abort word goes to the status sink, no round trip (when the
   // sink is full, the status is read back here as usual)

@@ -208,8 +208,9 @@ __device__ __forceinline__ void mark_tiles_near(int *dirty, int tm, int64_t i, i
 
 // The gwdt start written by the costs pass (pipeline entry points, which do
 // not return the costs): the costs array becomes the relaxation's cost
-// array (halved, NaN at non-flat pixels), `dist` gets 1 at presills and +INF
-// elsewhere, and the tiles around presills are marked in `dirty` (zeroed
+// array (halved, NaN at non-flat pixels), `dist` gets 1 at presills, +INF at
+// other flats and 0 elsewhere, and the tiles around presills are marked in
+// `dirty` (zeroed
 // by the caller, one int per tile).
 struct GwdtSeed {
   float *dist;
