@@ -440,13 +440,18 @@ __global__ void costs_kernel(float *__restrict__ costs,
 #pragma unroll
     for (int u = 0; u < kCostPer; u++) {
       const int64_t p = p0 + u * stride;
-      const bool in = p < N;
-      fv[u] = in ? flats[p] : 0;
-      fl[u] = in ? filled[p] : 0.f;
-      og[u] = in ? orig[p] : 0.f;
+      fv[u] = p < N ? flats[p] : 0;
     }
+    // the depths are read with the labels, at flat pixels only: the same
+    // dependent level, two thirds fewer bytes where flats are a third
 #pragma unroll
-    for (int u = 0; u < kCostPer; u++) l1[u] = (fv[u] & 1) ? L[p0 + u * stride] : -1;
+    for (int u = 0; u < kCostPer; u++) {
+      const int64_t p = p0 + u * stride;
+      const bool f = fv[u] & 1;
+      l1[u] = f ? L[p] : -1;
+      fl[u] = f ? filled[p] : 0.f;
+      og[u] = f ? orig[p] : 0.f;
+    }
 #pragma unroll
     for (int u = 0; u < kCostPer; u++) R[u] = l1[u] >= 0 ? L[l1[u]] : -1;
 #pragma unroll
