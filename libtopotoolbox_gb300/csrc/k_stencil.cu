@@ -411,28 +411,6 @@ __device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
   float t = __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
   return f2_norm(p.hi, __fadd_rn(p.lo, t));
 }
-__device__ __forceinline__ F2 f2_mulf(F2 a, float b) {
-  F2 p = two_prod(a.hi, b);
-  return f2_norm(p.hi, __fmaf_rn(a.lo, b, p.lo));
-}
-// a / b for float b.
-__device__ __forceinline__ F2 f2_divf(F2 a, float b) {
-  float q = __fdiv_rn(a.hi, b);
-  float r = __fadd_rn(__fmaf_rn(-q, b, a.hi), a.lo);
-  return f2_norm(q, __fdiv_rn(r, b));
-}
-__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
-  float q = __fdiv_rn(a.hi, b.hi);
-  F2 qb = f2_mulf(b, q);
-  F2 r = f2_add(a, F2{-qb.hi, -qb.lo});
-  return f2_norm(q, __fdiv_rn(r.hi, b.hi));
-}
-__device__ __forceinline__ F2 f2_sqrt(F2 a) {
-  float s = __fsqrt_rn(a.hi);
-  F2 ss = two_prod(s, s);
-  float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, ss.hi), ss.lo), a.lo);
-  return f2_norm(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
-}
 
 // Exact stencil sums: the one-sided [-3 4 -1] / [1 -4 3] and central
 // [-1 0 1] combinations of float32 samples, as float-float.
