@@ -240,6 +240,22 @@ TT_CUDA_API void tt_cuda_flow_accumulation_edgelist(float *acc, ptrdiff_t *sourc
 TT_CUDA_API void tt_cuda_traverse_down_f32_add_mul(float *output, float *input,
                                                    ptrdiff_t *source, ptrdiff_t *target,
                                                    ptrdiff_t edge_count);
+/** include/topotoolbox.h:1235 traverse_down_u32_or_and
+ *  (src/streamquad.c:49-60): output[target] |= output[source] & input[e]
+ *  for every edge e in list order, any order, exact. */
+TT_CUDA_API void tt_cuda_traverse_down_u32_or_and(uint32_t *output, uint32_t *input,
+                                                  ptrdiff_t *source, ptrdiff_t *target,
+                                                  ptrdiff_t edge_count);
+/** include/topotoolbox.h:1186 traverse_up_u32_or_and
+ *  (src/streamquad.c:37-47): output[source] |= output[target] & weights[e]
+ *  for every edge e in reverse list order, any order, exact.  With
+ *  `output` holding a distinct bit pattern at each outlet and zero elsewhere
+ *  and all-ones weights, this labels drainage basins on a D8 edge list
+ *  (test/random_dem.cpp:550-580).  Both or/and sweeps: `output` spans nodes
+ *  0 .. the largest index the edges name, as in the reference. */
+TT_CUDA_API void tt_cuda_traverse_up_u32_or_and(uint32_t *output, uint32_t *weights,
+                                                ptrdiff_t *source, ptrdiff_t *target,
+                                                ptrdiff_t edge_count);
 /** include/topotoolbox.h:2304 drainagebasins (src/drainagebasins.c:6-27).
  *  For a topologically ordered edge list (as flow_routing_d8_edgelist
  *  produces) the labels equal the reference's on the same list. */
@@ -371,6 +387,13 @@ TT_CUDA_API tt_cuda_status tt_cuda_flow_accumulation_edgelist_dev(
 TT_CUDA_API tt_cuda_status tt_cuda_traverse_down_f32_add_mul_dev(
     float *output, const float *input, const ptrdiff_t *source, const ptrdiff_t *target,
     ptrdiff_t edge_count, ptrdiff_t node_count, void *stream);
+/** Device forms of the or/and sweeps, `node_count` as above. */
+TT_CUDA_API tt_cuda_status tt_cuda_traverse_down_u32_or_and_dev(
+    uint32_t *output, const uint32_t *input, const ptrdiff_t *source,
+    const ptrdiff_t *target, ptrdiff_t edge_count, ptrdiff_t node_count, void *stream);
+TT_CUDA_API tt_cuda_status tt_cuda_traverse_up_u32_or_and_dev(
+    uint32_t *output, const uint32_t *weights, const ptrdiff_t *source,
+    const ptrdiff_t *target, ptrdiff_t edge_count, ptrdiff_t node_count, void *stream);
 TT_CUDA_API tt_cuda_status tt_cuda_drainagebasins_dev(
     ptrdiff_t *basins, const ptrdiff_t *source, const ptrdiff_t *target,
     ptrdiff_t edge_count, const ptrdiff_t dims[2], void *stream);

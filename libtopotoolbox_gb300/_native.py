@@ -50,6 +50,8 @@ SIGNATURES = {
     "tt_cuda_flow_accumulation_edgelist": (None, [P, P, P, P, P, I64, PD]),
     "tt_cuda_drainagebasins": (None, [P, P, P, I64, PD]),
     "tt_cuda_traverse_down_f32_add_mul": (None, [P, P, P, P, I64]),
+    "tt_cuda_traverse_down_u32_or_and": (None, [P, P, P, P, I64]),
+    "tt_cuda_traverse_up_u32_or_and": (None, [P, P, P, P, I64]),
     "tt_cuda_edgelist_degree": (None, [P, P, P, P, I64, I64]),
     "tt_cuda_compute_sfgraph": (None, [P, P, P, P, P, P, P, P, C.c_double, C.c_bool]),
     "tt_cuda_compute_drainage_area_single_flow": (None, [P, P, P, P, C.c_double]),
@@ -71,6 +73,8 @@ SIGNATURES = {
     "tt_cuda_flow_accumulation_edgelist_dev": (ST, [P, P, P, P, P, I64, PD, P]),
     "tt_cuda_drainagebasins_dev": (ST, [P, P, P, I64, PD, P]),
     "tt_cuda_traverse_down_f32_add_mul_dev": (ST, [P, P, P, P, I64, I64, P]),
+    "tt_cuda_traverse_down_u32_or_and_dev": (ST, [P, P, P, P, I64, I64, P]),
+    "tt_cuda_traverse_up_u32_or_and_dev": (ST, [P, P, P, P, I64, I64, P]),
     "tt_cuda_edgelist_degree_dev": (ST, [P, P, P, P, I64, I64, P]),
     "tt_cuda_compute_sfgraph_dev": (ST, [P, P, P, P, P, P, P, P, C.c_double, C.c_bool, P]),
     "tt_cuda_compute_drainage_area_single_flow_dev": (ST, [P, P, P, C.c_double, P]),

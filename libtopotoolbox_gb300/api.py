@@ -265,6 +265,30 @@ def traverse_down_f32_add_mul(output, input, source, target):
     return out
 
 
+def traverse_down_u32_or_and(output, input, source, target):
+    """output[target] |= output[source] & input[e] for every edge in list
+    order (include/topotoolbox.h:1235, src/streamquad.c:49-60).  Returns the
+    updated copy of `output` (uint32 node attribute list)."""
+    return _traverse_u32("tt_cuda_traverse_down_u32_or_and", output, input, source, target)
+
+
+def traverse_up_u32_or_and(output, weights, source, target):
+    """output[source] |= output[target] & weights[e] for every edge in
+    reverse list order (include/topotoolbox.h:1186, src/streamquad.c:37-47).
+    Returns the updated copy of `output` (uint32 node attribute list)."""
+    return _traverse_u32("tt_cuda_traverse_up_u32_or_and", output, weights, source, target)
+
+
+def _traverse_u32(name, output, input, source, target):
+    out = np.array(output, dtype=np.uint32, copy=True)
+    inp = np.ascontiguousarray(input, dtype=np.uint32)
+    src = np.ascontiguousarray(source, dtype=np.int64)
+    tgt = np.ascontiguousarray(target, dtype=np.int64)
+    getattr(N.lib(), name)(_ptr(out), _ptr(inp), _ptr(src), _ptr(tgt), len(src))
+    _after(name[len("tt_cuda_"):])
+    return out
+
+
 def drainagebasins(source, target, shape):
     """basins (include/topotoolbox.h:2304, src/drainagebasins.c:6-27)."""
     src = np.ascontiguousarray(source, dtype=np.int64)
@@ -493,6 +517,18 @@ class dev:  # namespace
             dev._p(output), dev._p(input), dev._p(source), dev._p(target),
             int(source.numel()), int(output.numel()), dev._stream()),
             "traverse_down_f32_add_mul_dev")
+        return output
+
+    @staticmethod
+    def traverse_u32_or_and(output, input, source, target, up=False):
+        """traverse_down_u32_or_and, or traverse_up_u32_or_and with `up`, in
+        place on the 1-D 32-bit tensor `output` (int32 tensors carry the
+        uint32 words bit for bit); returns it."""
+        name = "tt_cuda_traverse_up_u32_or_and_dev" if up else \
+            "tt_cuda_traverse_down_u32_or_and_dev"
+        N.check(getattr(N.lib(), name)(
+            dev._p(output), dev._p(input), dev._p(source), dev._p(target),
+            int(source.numel()), int(output.numel()), dev._stream()), name[len("tt_cuda_"):])
         return output
 
     @staticmethod

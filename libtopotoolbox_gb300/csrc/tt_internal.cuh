@@ -281,6 +281,13 @@ tt_cuda_status accumulate_edgelist_dev(float *acc, const ptrdiff_t *source,
 tt_cuda_status edge_sweep_dev(float *out, const float *w, const ptrdiff_t *source,
                               const ptrdiff_t *target, const float *frac, int64_t E, int64_t N,
                               cudaStream_t st);
+// The same list-order sweep in the (|, &) semiring, exact:
+// out[tgt] |= out[src] & in[e] in list order, or with `up`
+// out[src] |= out[tgt] & in[e] in reverse list order.  out = w first; `out`
+// may equal `w`.
+tt_cuda_status edge_sweep_u32_dev(uint32_t *out, const uint32_t *w, const ptrdiff_t *source,
+                                  const ptrdiff_t *target, const uint32_t *in, int64_t E,
+                                  int64_t N, bool up, cudaStream_t st);
 // 1 + the largest node index named by the edge list (INT64_MAX for a
 // negative index), read back to the host.
 tt_cuda_status edge_node_count_dev(const ptrdiff_t *source, const ptrdiff_t *target, int64_t E,

@@ -573,6 +573,37 @@ tt_cuda_status tt_cuda_traverse_down_f32_add_mul_dev(float *output, const float 
   });
 }
 
+static tt_cuda_status traverse_u32_dev(uint32_t *output, const uint32_t *input,
+                                       const ptrdiff_t *source, const ptrdiff_t *target,
+                                       ptrdiff_t edge_count, ptrdiff_t node_count, bool up,
+                                       void *stream) {
+  if (!output || (edge_count > 0 && (!source || !target || !input)) ||
+      !edges_ok(edge_count) || node_count <= 0 || node_count >= (1LL << 31))
+    return set_status(TT_CUDA_ERR_INVALID_ARGUMENT), TT_CUDA_ERR_INVALID_ARGUMENT;
+  const ptrdiff_t nd[2] = {node_count, 1};
+  return dev_call(nd, stream, [&](const GridDims &g, cudaStream_t st) {
+    return edge_sweep_u32_dev(output, output, source, target, input, edge_count, g.cells(),
+                              up, st);
+  });
+}
+
+tt_cuda_status tt_cuda_traverse_down_u32_or_and_dev(uint32_t *output, const uint32_t *input,
+                                                    const ptrdiff_t *source,
+                                                    const ptrdiff_t *target,
+                                                    ptrdiff_t edge_count, ptrdiff_t node_count,
+                                                    void *stream) {
+  return traverse_u32_dev(output, input, source, target, edge_count, node_count, false, stream);
+}
+
+tt_cuda_status tt_cuda_traverse_up_u32_or_and_dev(uint32_t *output, const uint32_t *weights,
+                                                  const ptrdiff_t *source,
+                                                  const ptrdiff_t *target,
+                                                  ptrdiff_t edge_count, ptrdiff_t node_count,
+                                                  void *stream) {
+  return traverse_u32_dev(output, weights, source, target, edge_count, node_count, true,
+                          stream);
+}
+
 tt_cuda_status tt_cuda_drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
                                           const ptrdiff_t *target, ptrdiff_t edge_count,
                                           const ptrdiff_t dims[2], void *stream) {
@@ -1111,8 +1142,16 @@ void tt_cuda_drainagebasins(ptrdiff_t *basins, ptrdiff_t *source, ptrdiff_t *tar
             });
 }
 
-void tt_cuda_traverse_down_f32_add_mul(float *output, float *input, ptrdiff_t *source,
-                                       ptrdiff_t *target, ptrdiff_t edge_count) {
+}  // extern "C"
+
+namespace {
+// Host-pointer sweeps over an edge list.  The reference's signatures carry
+// no node count: `output` spans the nodes the edges name.  V is the node
+// and edge value type; sweep(out, in, src, tgt, E, N, st) runs on device
+// copies, `out` holding the start values.
+template <class V, class Sweep>
+void host_edge_sweep(V *output, const V *input, const ptrdiff_t *source,
+                     const ptrdiff_t *target, ptrdiff_t edge_count, Sweep sweep) {
   if (!edges_ok(edge_count) ||
       (edge_count > 0 && (!output || !input || !source || !target))) {
     set_status(TT_CUDA_ERR_INVALID_ARGUMENT);
@@ -1132,33 +1171,62 @@ void tt_cuda_traverse_down_f32_add_mul(float *output, float *input, ptrdiff_t *s
   Staging sg;
   sg.add(E * 8);
   sg.add(E * 8);
-  sg.add(E * 4);
+  sg.add(E * sizeof(V));
   if (!sg.reserve()) {
     finish(TT_CUDA_ERR_ALLOC, st);
     return;
   }
   auto *dsrc = (ptrdiff_t *)sg.take(E * 8);
   auto *dtgt = (ptrdiff_t *)sg.take(E * 8);
-  auto *din = (float *)sg.take(E * 4);
+  auto *din = (V *)sg.take(E * sizeof(V));
   tt_cuda_status s = h2d(dsrc, source, E * 8, st);
   if (s == TT_CUDA_SUCCESS) s = h2d(dtgt, target, E * 8, st);
-  if (s == TT_CUDA_SUCCESS) s = h2d(din, input, E * 4, st);
-  // The reference's signature carries no node count: `output` spans the
-  // nodes the edges name.
+  if (s == TT_CUDA_SUCCESS) s = h2d(din, input, E * sizeof(V), st);
   int64_t N = 0;
   if (s == TT_CUDA_SUCCESS) s = edge_node_count_dev(dsrc, dtgt, edge_count, &N, st);
   if (s == TT_CUDA_SUCCESS && N >= (1LL << 31)) s = TT_CUDA_ERR_INVALID_ARGUMENT;
-  float *dout = nullptr;
-  if (s == TT_CUDA_SUCCESS && cudaMallocAsync((void **)&dout, (size_t)N * 4, st) != cudaSuccess) {
+  V *dout = nullptr;
+  if (s == TT_CUDA_SUCCESS &&
+      cudaMallocAsync((void **)&dout, (size_t)N * sizeof(V), st) != cudaSuccess) {
     cudaGetLastError();
     s = TT_CUDA_ERR_ALLOC;
     dout = nullptr;
   }
-  if (s == TT_CUDA_SUCCESS) s = h2d(dout, output, (size_t)N * 4, st);
-  if (s == TT_CUDA_SUCCESS) s = edge_sweep_dev(dout, dout, dsrc, dtgt, din, edge_count, N, st);
-  if (s == TT_CUDA_SUCCESS) s = d2h(output, dout, (size_t)N * 4, st);
+  if (s == TT_CUDA_SUCCESS) s = h2d(dout, output, (size_t)N * sizeof(V), st);
+  if (s == TT_CUDA_SUCCESS) s = sweep(dout, din, dsrc, dtgt, edge_count, N, st);
+  if (s == TT_CUDA_SUCCESS) s = d2h(output, dout, (size_t)N * sizeof(V), st);
   if (dout) cudaFreeAsync(dout, st);
   finish(s, st);
+}
+}  // namespace
+
+extern "C" {
+
+void tt_cuda_traverse_down_f32_add_mul(float *output, float *input, ptrdiff_t *source,
+                                       ptrdiff_t *target, ptrdiff_t edge_count) {
+  host_edge_sweep(output, input, source, target, edge_count,
+                  [](float *o, const float *in, const ptrdiff_t *src, const ptrdiff_t *tgt,
+                     int64_t E, int64_t N, cudaStream_t st) {
+                    return edge_sweep_dev(o, o, src, tgt, in, E, N, st);
+                  });
+}
+
+void tt_cuda_traverse_down_u32_or_and(uint32_t *output, uint32_t *input, ptrdiff_t *source,
+                                      ptrdiff_t *target, ptrdiff_t edge_count) {
+  host_edge_sweep(output, input, source, target, edge_count,
+                  [](uint32_t *o, const uint32_t *in, const ptrdiff_t *src,
+                     const ptrdiff_t *tgt, int64_t E, int64_t N, cudaStream_t st) {
+                    return edge_sweep_u32_dev(o, o, src, tgt, in, E, N, false, st);
+                  });
+}
+
+void tt_cuda_traverse_up_u32_or_and(uint32_t *output, uint32_t *weights, ptrdiff_t *source,
+                                    ptrdiff_t *target, ptrdiff_t edge_count) {
+  host_edge_sweep(output, weights, source, target, edge_count,
+                  [](uint32_t *o, const uint32_t *in, const ptrdiff_t *src,
+                     const ptrdiff_t *tgt, int64_t E, int64_t N, cudaStream_t st) {
+                    return edge_sweep_u32_dev(o, o, src, tgt, in, E, N, true, st);
+                  });
 }
 
 void tt_cuda_edgelist_degree(uint8_t *indegree, uint8_t *outdegree, ptrdiff_t *source,

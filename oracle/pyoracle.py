@@ -102,6 +102,8 @@ class Oracle:
             "drainagebasins": (None, [P, P, P, C.c_int64, PD]),
             "edgelist_degree": (None, [P, P, P, P, C.c_int64, C.c_int64]),
             "traverse_down_f32_add_mul": (None, [P, P, P, P, C.c_int64]),
+            "traverse_down_u32_or_and": (None, [P, P, P, P, C.c_int64]),
+            "traverse_up_u32_or_and": (None, [P, P, P, P, C.c_int64]),
             "compute_sfgraph": (None, [P, P, P, P, P, P, P, P, D,
                                        C.c_int if kind == "port" else C.c_bool]),
             "compute_drainage_area_single_flow": (None, [P, P, P, P, D]),
@@ -307,6 +309,18 @@ class Oracle:
         src = np.ascontiguousarray(source, dtype=np.int64)
         tgt = np.ascontiguousarray(target, dtype=np.int64)
         name = "traverse_down_f64_from_f32" if f64 else "traverse_down_f32_add_mul"
+        self.fn[name](_ptr(out), _ptr(inp), _ptr(src), _ptr(tgt), len(src))
+        return out
+
+    def traverse_u32_or_and(self, output, input, source, target, up=False):
+        """Updated copy of `output` (src/streamquad.c:37-60): the or/and
+        sweep down the list, or up it (reverse order, source and target
+        exchanged) with `up`."""
+        out = np.array(output, dtype=np.uint32, copy=True)
+        inp = np.ascontiguousarray(input, dtype=np.uint32)
+        src = np.ascontiguousarray(source, dtype=np.int64)
+        tgt = np.ascontiguousarray(target, dtype=np.int64)
+        name = "traverse_up_u32_or_and" if up else "traverse_down_u32_or_and"
         self.fn[name](_ptr(out), _ptr(inp), _ptr(src), _ptr(tgt), len(src))
         return out
 

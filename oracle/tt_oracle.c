@@ -760,6 +760,22 @@ void orc_traverse_down_f32_add_mul(float *output, const float *input,
   }
 }
 
+/* src/streamquad.c:49-60: in list order, out[target] |= out[source] & in[e]. */
+void orc_traverse_down_u32_or_and(uint32_t *output, const uint32_t *input,
+                                  const ptrdiff_t *source, const ptrdiff_t *target,
+                                  ptrdiff_t edge_count) {
+  for (ptrdiff_t e = 0; e < edge_count; e++)
+    output[target[e]] = output[target[e]] | (output[source[e]] & input[e]);
+}
+
+/* src/streamquad.c:37-47: in reverse list order, out[source] |= out[target] & in[e]. */
+void orc_traverse_up_u32_or_and(uint32_t *output, const uint32_t *input,
+                                const ptrdiff_t *source, const ptrdiff_t *target,
+                                ptrdiff_t edge_count) {
+  for (ptrdiff_t e = edge_count - 1; e >= 0; e--)
+    output[source[e]] = output[source[e]] | (output[target[e]] & input[e]);
+}
+
 /* The same sweep in FP64 over a float32 start and float32 edge weights. */
 void orc_traverse_down_f64_from_f32(double *output, const float *input,
                                     const ptrdiff_t *source, const ptrdiff_t *target,

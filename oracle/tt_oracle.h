@@ -123,6 +123,13 @@ void orc_drainagebasins(ptrdiff_t *basins, const ptrdiff_t *source,
 void orc_traverse_down_f32_add_mul(float *output, const float *input,
                                    const ptrdiff_t *source, const ptrdiff_t *target,
                                    ptrdiff_t edge_count);
+/* src/streamquad.c:49-60 and 37-47 */
+void orc_traverse_down_u32_or_and(uint32_t *output, const uint32_t *input,
+                                  const ptrdiff_t *source, const ptrdiff_t *target,
+                                  ptrdiff_t edge_count);
+void orc_traverse_up_u32_or_and(uint32_t *output, const uint32_t *input,
+                                const ptrdiff_t *source, const ptrdiff_t *target,
+                                ptrdiff_t edge_count);
 /* the same sweep in FP64 (start values and edge weights given as float32) */
 void orc_traverse_down_f64_from_f32(double *output, const float *input,
                                     const ptrdiff_t *source, const ptrdiff_t *target,

@@ -8,7 +8,9 @@ the same edge list is bit-identical to the oracle's reverse sweep
 unit fractions is within 1e-5 of the FP64 sweep and equal, bit for bit, to
 flow_accumulation of the same forest; any other edge list (fractions,
 several targets, any order) is within 1e-5 of the FP64 list-order sweep, as
-is traverse_down_f32_add_mul.  Both memory orders.
+is traverse_down_f32_add_mul; the or/and sweeps (traverse_down_u32_or_and,
+traverse_up_u32_or_and) are bit-identical to the oracle, and the upward one
+labels the same drainage basins.  Both memory orders.
 """
 import numpy as np
 import pytest
@@ -127,6 +129,70 @@ def test_accumulation_edgelist_general(gpu, port):
         n = int(max(s.max(initial=-1), t.max(initial=-1))) + 1
         assert rel_err(got[:n], exp[:n], tau=1e-30) <= REL_TOL, name
         assert np.array_equal(got[n:], start[n:]), name  # nodes no edge names
+
+
+def test_or_and_sweeps(gpu, port):
+    """traverse_down_u32_or_and and traverse_up_u32_or_and
+    (src/streamquad.c:37-60) equal the oracle bit for bit on every list
+    (fractional and multi-target topologies, shuffled, repeated edges and
+    self-loops, a wide fan, empty)."""
+    from conftest import edge_list_cases
+
+    from libtopotoolbox_gb300 import api
+
+    rng = np.random.default_rng(6)
+    for name, s, t, _, shape in edge_list_cases(port):
+        n = int(np.prod(shape))
+        start = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+        start[rng.random(n) < 0.5] = 0
+        w = rng.integers(0, 2**32, len(s), dtype=np.uint64).astype(np.uint32)
+        assert np.array_equal(api.traverse_down_u32_or_and(start, w, s, t),
+                              port.traverse_u32_or_and(start, w, s, t)), name
+        assert np.array_equal(api.traverse_up_u32_or_and(start, w, s, t),
+                              port.traverse_u32_or_and(start, w, s, t, up=True)), name
+
+
+@pytest.mark.parametrize("idx", range(0, len(CASES), 3))
+def test_basins_by_upward_sweep(gpu, port, idx):
+    """drainagebasins equals the upward or/and sweep started from each
+    outlet's own label with all-ones weights (test/random_dem.cpp:549-580)."""
+    from libtopotoolbox_gb300 import api
+
+    name, dem, bc = CASES[idx]
+    node, direction = _flow(CASES[idx], 0)
+    s, t = api.flow_routing_d8_edgelist(node, direction, 0)
+    basins = api.drainagebasins(s, t, dem.shape).ravel(order="F")
+    n = basins.size
+    indeg = np.bincount(t, minlength=n)
+    outdeg = np.bincount(s, minlength=n)
+    start = np.zeros(n, np.uint32)
+    outlet = (indeg > 0) & (outdeg == 0)
+    start[outlet] = basins[outlet].astype(np.uint32)
+    got = api.traverse_up_u32_or_and(start, np.full(len(s), 0xFFFFFFFF, np.uint32), s, t)
+    assert np.array_equal(got, basins.astype(np.uint32)), name
+
+
+def test_or_and_dev_mfd_1024(gpu, port):
+    """Device forms of the or/and sweeps on a 1024 x 1024 multiple-flow-
+    direction edge list (about 3.5 million edges), bit for bit."""
+    from conftest import mfd_edges
+
+    from libtopotoolbox_gb300 import dems
+    from libtopotoolbox_gb300.api import dev
+
+    torch = gpu
+    z = dems.plain_512(seed=7, size=1024)[0]
+    s, t, _ = mfd_edges(z)
+    rng = np.random.default_rng(8)
+    start = rng.integers(0, 2**32, z.size, dtype=np.uint64).astype(np.uint32)
+    w = rng.integers(0, 2**32, len(s), dtype=np.uint64).astype(np.uint32)
+    t_s, t_t = torch.from_numpy(s).cuda(), torch.from_numpy(t).cuda()
+    t_w = torch.from_numpy(w.view(np.int32)).cuda()
+    for up in (False, True):
+        out = torch.from_numpy(start.view(np.int32).copy()).cuda()
+        dev.traverse_u32_or_and(out, t_w, t_s, t_t, up=up)
+        got = out.cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, port.traverse_u32_or_and(start, w, s, t, up=up)), up
 
 
 def test_traverse_dev_and_mfd_1024(gpu, port):

@@ -233,3 +233,18 @@ def test_port_edge_sweeps_equal_reference(port, ref):
         start = w.ravel(order="F")
         assert same_float(port.traverse_down_f32_add_mul(start, f, s, t),
                           ref.traverse_down_f32_add_mul(start, f, s, t)), name
+
+
+def test_port_or_and_sweeps_equal_reference(port, ref):
+    """traverse_down_u32_or_and and traverse_up_u32_or_and
+    (src/streamquad.c:37-60) on the same edge lists, random bit patterns."""
+    rng = np.random.default_rng(4)
+    for name, s, t, _, shape in edge_list_cases(port):
+        n = int(np.prod(shape))
+        start = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+        start[rng.random(n) < 0.5] = 0
+        w = rng.integers(0, 2**32, len(s), dtype=np.uint64).astype(np.uint32)
+        for up in (False, True):
+            a = port.traverse_u32_or_and(start, w, s, t, up=up)
+            b = ref.traverse_u32_or_and(start, w, s, t, up=up)
+            assert np.array_equal(a, b), (name, up)
