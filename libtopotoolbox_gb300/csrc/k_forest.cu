@@ -438,6 +438,7 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
   const int wshift = pass_shift(a);
   // a deferred single-pass plan needs no combination: write floats
   long long *const raw_out = (a.plan && a.plan[0] == 1) ? nullptr : a.raw_out;
+  int hm = 0;  // largest height this thread wrote, over all its tiles
   for (int tile = blockIdx.x; tile < T; tile += gridDim.x) {
     const int ti = tile % a.tm, tj = tile / a.tm;
     const int64_t i0 = (int64_t)ti * kTile, j0 = (int64_t)tj * kTile;
@@ -482,7 +483,6 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
     }
     __syncthreads();
 
-    int hm = 0;
 #pragma unroll
     for (int u = 0; u < kPerThread; u++) {
       const int e = tid + u * kUpThreads;
@@ -503,8 +503,12 @@ __global__ void __launch_bounds__(kUpThreads, kFinBlocks) forest_fin_kernel(UpAr
         hm = max(hm, t.h[e]);
       }
     }
-    if (H && hm) atomicMax(a.hmax, hm);
     __syncthreads();
+  }
+  // One atomic per warp on the shared maximum, not one per thread and tile.
+  if (H) {
+    hm = __reduce_max_sync(0xffffffffu, hm);
+    if ((tid & 31) == 0 && hm) atomicMax(a.hmax, hm);
   }
 }
 
@@ -573,9 +577,9 @@ __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
                                    const int2 *__restrict__ link,
                                    CoarseCell *ccell, int *processed, int limit) {
   const int L = *lcount;
+  int n_done = 0;  // exits this thread completed, over all its leaves
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < L; a += gridDim.x * blockDim.x) {
     const int e0 = leaves[a];
-    int n_done = 0;
     // A leaf has no coarse donors: its cell was completed by earlier kernels.
     const longlong2 c0 = __ldcg(reinterpret_cast<const longlong2 *>(&ccell[e0]));
     long long v = c0.x;
@@ -614,8 +618,10 @@ __global__ void coarse_walk_kernel(const int *__restrict__ leaves,
       hv = (int)(unsigned)nhi;
       l = ln;
     }
-    atomicAdd(processed, n_done);
   }
+  // One atomic per warp on the shared count, not one per leaf.
+  n_done = __reduce_add_sync(0xffffffffu, n_done);
+  if ((threadIdx.x & 31) == 0 && n_done) atomicAdd(processed, n_done);
 }
 
 // Final exit totals back to pixel-indexed cells for the final tile pass.
