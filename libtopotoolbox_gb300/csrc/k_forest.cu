@@ -1151,7 +1151,12 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
             g.m, order, w.xmap, w.xsteps, w.link, w.ccell);
   TT_LAUNCH(coarse_leaves_kernel, lg, 256, 0, st, w.counters + 0, w.ccell, w.link, w.leaves,
             w.counters + 1);
-  TT_LAUNCH(coarse_walk_kernel, lg, 256, 0, st, w.leaves, w.counters + 1, w.link,
+  // One walker per leaf (blocks beyond the leaf count exit at once): the
+  // block scheduler hands freed SMs the next leaves, instead of each thread
+  // walking a fixed share of them one after another.
+  const int64_t exits = std::min<int64_t>(g.cells(), (int64_t)g.tiles() * kRing);
+  const int wg = (int)std::max<int64_t>(1, std::min<int64_t>((exits + 255) / 256, INT_MAX));
+  TT_LAUNCH(coarse_walk_kernel, wg, 256, 0, st, w.leaves, w.counters + 1, w.link,
             w.ccell, w.counters + 2, (int)std::min<int64_t>(g.cells(), INT_MAX));
   TT_LAUNCH(coarse_scatter_kernel, lg, 256, 0, st, w.counters + 0, w.elist, w.ccell,
             w.cell);
