@@ -1118,9 +1118,14 @@ tt_cuda_status up_run(const uint8_t *dir, const float *weights, int wshift,
   a.h_out = w.h;
   a.hmax = w.counters + 3;
   a.err = w.counters + 4;
-  // one resident wave of blocks, each looping over tiles
-  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kUpBlocks);
-  const int fgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks);
+  // The first pass takes one tile per block, so the block scheduler evens
+  // out tiles whose walks differ in length.  The final pass does the same
+  // unless it carries heights: then it stays persistent, since each block
+  // ends with an atomic on the shared maximum height (measured at 16384^2,
+  // same box: pipeline 38.77 ms with both passes persistent, 38.55 ms with
+  // this split, 39.0 ms with both one tile per block).
+  const int tgrid = (int)std::min<int64_t>(T, INT_MAX);
+  const int fgrid = want_h ? (int)std::min<int64_t>(T, (int64_t)sm_count() * kFinBlocks) : tgrid;
   void (*up)(UpArgs) = nullptr;
   void (*fin)(UpArgs) = nullptr;
   const bool u32 = !weights;  // unit weights: 32-bit counts in the tile passes
