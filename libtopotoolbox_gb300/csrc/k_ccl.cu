@@ -512,8 +512,9 @@ tt_cuda_status costs_dev(float *costs, ptrdiff_t *conncomps,
   int *larg = (int *)ws.take((size_t)N * 4);
   unsigned long long *best = (unsigned long long *)ws.take((size_t)N * 8);
   const int grid = ew_grid(N);
-  const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps,
-                                           (int64_t)sm_count() * 16);
+  // one tile per warp: the block scheduler evens out tiles whose labelling
+  // takes longer (many runs, many unions)
+  const int tgrid = (int)std::min<int64_t>((T + kCclWarps - 1) / kCclWarps, INT_MAX);
   TT_CHECK(cudaMemsetAsync(nroots, 0, sizeof(int), st));
   TT_LAUNCH(ccl_tile_kernel, tgrid, kCclWarps * 32, 0, st, L, lmax, larg, best, roots,
             nroots, edges, flats, orig, filled, g.m, g.n, g.tm, g.tn);

@@ -120,7 +120,8 @@ def test_costs(gpu, port, case):
         pairs = np.unique(np.stack([a, b], 1), axis=0)
         assert len(np.unique(pairs[:, 0])) == len(pairs) == len(np.unique(pairs[:, 1]))
         # the label is a pixel of maximal depth inside the component
-        depth = (filled - dem).ravel(order="F")
+        with np.errstate(invalid="ignore"):  # -INF nodata: -INF - -INF is NaN, never flat
+            depth = (filled - dem).ravel(order="F")
         lab = gcc.ravel(order="F")
         fl = isflat.ravel(order="F")
         for L in np.unique(lab[fl])[:200]:
