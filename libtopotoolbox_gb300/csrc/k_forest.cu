@@ -1459,7 +1459,7 @@ tt_cuda_status accumulate_backward_dev(float *grad_w, const uint8_t *dir,
   a.out = grad_w;
   a.err = counters + 4;
   const int T = g.tiles();
-  const int tgrid = (int)std::min<int64_t>(T, (int64_t)sm_count() * 16);
+  const int tgrid = (int)std::min<int64_t>(T, INT_MAX);  // one tile per block
   TT_LAUNCH(forest_down_kernel, tgrid, kDownThreads, 0, st, a);
   const int lg = list_grid(g.cells() / 8 + 1);
   TT_LAUNCH(down_init_kernel, lg, 256, 0, st, elist, counters + 0, dir, g.m, 0u,
