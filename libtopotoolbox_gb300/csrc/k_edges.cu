@@ -523,7 +523,7 @@ tt_cuda_status drainagebasins_dev(ptrdiff_t *basins, const ptrdiff_t *source,
   // jumping over the exits only, then every pixel through its terminal.
   int *term = pb, *J = key, *root = rootp;  // key is free until the keys are taken
   int *exits = ex_list, *nexits = ctl + 2;
-  TT_LAUNCH(basins_tile_kernel, (int)std::min<int64_t>(g.tiles(), (int64_t)sm_count() * 8), 256,
+  TT_LAUNCH(basins_tile_kernel, (int)std::min<int64_t>(g.tiles(), INT_MAX), 256,
             0, st, pa, g.m, g.n, g.tm, g.tn, term, J, exits, nexits, ctl);
   TT_LAUNCH(exits_init_kernel, gN, 256, 0, st, exits, nexits, term, J);
   int *h = (int *)pinned_scratch();

@@ -358,7 +358,7 @@ tt_cuda_status rootward_sum(int *out, const int *parent, const int *val, const G
   int *exits = (int *)s.take(N * 4);
   TT_CHECK(cudaMemsetAsync(ctl, 0, 256, st));
   const int gN = sf_grid(N);
-  TT_LAUNCH(rw_tile_kernel, (int)std::min<int64_t>(g.tiles(), (int64_t)sm_count() * 8), 256, 0,
+  TT_LAUNCH(rw_tile_kernel, (int)std::min<int64_t>(g.tiles(), INT_MAX), 256, 0,
             st, parent, val, g.m, g.n, g.tm, g.tn, term, psum, acc[0], x[0], acc[1], x[1],
             exits, ctl + 2, ctl);
   TT_LAUNCH(rw_exits_init_kernel, gN, 256, 0, st, exits, ctl + 2, parent, val, term, psum,
