@@ -176,10 +176,10 @@ __device__ __forceinline__ int local_receiver(const uint8_t (*dir)[36], int ii,
 //     its receivers to the in-tile terminal and records it with the number
 //     of steps (first pass only).
 constexpr int kUpThreads = 128;
-// Resident blocks per SM for the two tile passes (48 and 40 registers a
-// thread, no spills; shared memory allows 10 and 15): walks wait at block
-// barriers for the block's longest chain, so more resident blocks keep the
-// SM busy meanwhile.
+// Resident blocks per SM for the two tile passes (up to 56 and 40
+// registers a thread, no spills; shared memory allows 10 and 15): walks
+// wait at block barriers for the block's longest chain, so more resident
+// blocks keep the SM busy meanwhile.
 constexpr int kUpBlocks = 9;
 constexpr int kFinBlocks = 11;
 constexpr int kRing = 4 * kTile - 4;  // 124 ring pixels
